@@ -1,0 +1,180 @@
+"""Generate the golden vectors that pin the oracle to the reference encoder.
+
+Runs the UNMODIFIED reference hot path (``DXTImage`` constructor +
+``DXTImage::Reencode``, built from the reference sources by
+``oracle/ref/Makefile`` into ``oracle/_ref/hotpath_harness``) on seeded
+synthetic streams and on adversarial block patterns, and records:
+
+* ``golden.json``      SHA-256 per frame of the stb blocks, final blocks,
+                       motion codes and unique palette, plus PSNR, for each
+                       case (inputs are regenerated from the integer-exact
+                       synthetic generator, so only hashes are stored);
+* ``adversarial.npz``  full input frames and outputs of the adversarial case.
+
+Usage (needs the reference sources; run from the repository root):
+    make -C oracle/ref REF=<path to MPTC>
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from mptc_gb300.synth import HD720, FHD1080, SMOKE_256, StreamSpec  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "hotpath_harness")
+OUT_DIR = os.path.dirname(os.path.abspath(__file__))
+
+# (name, spec, first frame, frame count, search_area, threshold, intra_interval)
+CASES = [
+    ("smoke256_sa8_thr5", SMOKE_256, 0, 16, 8, 5, 16),
+    ("smoke256_sa4_thr0_ii4", SMOKE_256, 0, 8, 4, 0, 4),
+    ("smoke256_sa16_thr20_ii8", SMOKE_256, 0, 4, 16, 20, 8),
+    ("small64_sa1_thr5", StreamSpec(64, 64, 6, seed=7), 0, 6, 1, 5, 16),
+    ("small128x96_sa2_thrm1", StreamSpec(128, 96, 5, seed=8), 0, 5, 2, -1, 2),
+    ("small96x64_sa4_thr30_allintra", StreamSpec(96, 64, 6, seed=9), 0, 6, 4, 30, 1),
+    ("small64_sa63_thr5", StreamSpec(64, 64, 4, seed=10), 0, 4, 63, 5, 2),
+    ("small160x120_sa8_thr1000", StreamSpec(160, 120, 3, seed=11), 0, 3, 8, 1000, 2),
+    ("small200x52_sa3_thr2", StreamSpec(200, 52, 5, seed=12, square_size=24), 0, 5, 3, 2, 3),
+    ("hd720_cut_sa8_thr5", HD720, 30, 4, 8, 5, 16),
+    ("fhd1080_sa8_thr5", FHD1080, 0, 2, 8, 5, 16),
+]
+
+
+def adversarial_frames(n_frames: int = 4, size: int = 64, seed: int = 1234) -> np.ndarray:
+    """Blocks that exercise stb_dxt's special cases and the refit edge cases:
+    constant colours (incl. 0/255), two-colour splits, ramps, saturated
+    channels, single outliers, near-constant blocks and pure noise. Later
+    frames shift the pattern by whole blocks so that inter matches exist."""
+    rng = np.random.default_rng(seed)
+    nb = size // 4
+    base = np.zeros((size, size, 3), np.uint8)
+    kinds = 12
+    for by in range(nb):
+        for bx in range(nb):
+            k = (by * nb + bx) % kinds
+            blk = np.zeros((4, 4, 3), np.int32)
+            c0 = rng.integers(0, 256, 3)
+            c1 = rng.integers(0, 256, 3)
+            if k == 0:
+                blk[:] = c0
+            elif k == 1:
+                blk[:] = 0
+            elif k == 2:
+                blk[:] = 255
+            elif k == 3:
+                m = rng.integers(0, 2, (4, 4)).astype(bool)
+                blk[m] = c0
+                blk[~m] = c1
+            elif k == 4:
+                t = np.linspace(0, 1, 4)[None, :, None]
+                blk[:] = (c0 * (1 - t) + c1 * t).round().astype(np.int32)
+            elif k == 5:
+                t = np.linspace(0, 1, 4)[:, None, None]
+                blk[:] = (c0 * (1 - t) + c1 * t).round().astype(np.int32)
+            elif k == 6:
+                blk[..., 0] = 255
+                blk[..., 1] = np.arange(16).reshape(4, 4) * 17
+                blk[..., 2] = 0
+            elif k == 7:
+                blk[:] = c0
+                blk[rng.integers(0, 4), rng.integers(0, 4)] = c1
+            elif k == 8:
+                blk[:] = c0
+                blk += rng.integers(-1, 2, (4, 4, 3))
+            elif k == 9:
+                blk[:] = rng.integers(0, 256, (4, 4, 3))
+            elif k == 10:
+                g = np.arange(16).reshape(4, 4, 1) * 16
+                blk[:] = g
+            else:
+                pal = rng.integers(0, 256, (4, 3))
+                blk[:] = pal[rng.integers(0, 4, (4, 4))]
+            base[4 * by:4 * by + 4, 4 * bx:4 * bx + 4] = np.clip(blk, 0, 255)
+    frames = []
+    for f in range(n_frames):
+        fr = np.roll(base, shift=(4 * (f % 2), 4 * f), axis=(0, 1)).copy()
+        if f >= 2:  # perturb a few blocks so that some searches fail
+            fr[::8, ::8] = 255 - fr[::8, ::8]
+        frames.append(fr)
+    return np.stack(frames)
+
+
+def run_reference(frames: np.ndarray, sa: int, thr: int, ii: int):
+    n, h, w, _ = frames.shape
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.rgb")
+        outp = os.path.join(td, "out.bin")
+        np.ascontiguousarray(frames).tofile(inp)
+        subprocess.check_call([HARNESS, inp, str(w), str(h), str(n), str(sa), str(thr), str(ii),
+                               outp, td])
+        buf = open(outp, "rb").read()
+    nblk = (w // 4) * (h // 4)
+    off = 0
+    res = []
+    for _ in range(n):
+        stb = np.frombuffer(buf, np.uint64, nblk, off); off += 8 * nblk
+        fin = np.frombuffer(buf, np.uint64, nblk, off); off += 8 * nblk
+        mot = np.frombuffer(buf, np.uint8, 2 * nblk, off); off += 2 * nblk
+        nu = int(np.frombuffer(buf, np.uint32, 1, off)[0]); off += 4
+        uni = np.frombuffer(buf, np.uint32, nu, off); off += 4 * nu
+        psnr = float(np.frombuffer(buf, np.float64, 1, off)[0]); off += 8
+        res.append(dict(stb=stb, final=fin, motion=mot, unique=uni, psnr=psnr))
+    assert off == len(buf)
+    return res
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def frame_record(r) -> dict:
+    mot = r["motion"].reshape(-1, 2)
+    kinds = np.where((mot[:, 0] == 255) & (mot[:, 1] == 255), 0,
+                     np.where(mot[:, 0] & 0x80, 2, 1))
+    return dict(stb=sha(r["stb"]), final=sha(r["final"]), motion=sha(r["motion"]),
+                unique=sha(r["unique"]), n_unique=int(r["unique"].size),
+                n_inter=int((kinds == 2).sum()), n_intra=int((kinds == 1).sum()),
+                psnr=r["psnr"])
+
+
+def main() -> None:
+    if not os.path.exists(HARNESS):
+        sys.exit(f"{HARNESS} missing: build it with make -C oracle/ref")
+    golden = {"generator": "mptc_gb300/csrc/synth_frames.c", "cases": []}
+    for name, spec, first, count, sa, thr, ii in CASES:
+        frames = spec.generate(first, count)
+        res = run_reference(frames, sa, thr, ii)
+        golden["cases"].append(dict(
+            name=name, spec=spec.__dict__, first=first, count=count, search_area=sa,
+            threshold=thr, intra_interval=ii, input_sha=[sha(f) for f in frames],
+            frames=[frame_record(r) for r in res]))
+        print(name, [(fr["n_inter"], fr["n_intra"], fr["n_unique"]) for fr in golden["cases"][-1]["frames"]])
+    adv = adversarial_frames()
+    for sa, thr, ii in [(4, 5, 16), (2, 0, 1)]:
+        res = run_reference(adv, sa, thr, ii)
+        key = f"adv_sa{sa}_thr{thr}_ii{ii}"
+        np.savez_compressed(os.path.join(OUT_DIR, f"{key}.npz"), frames=adv,
+                            stb=np.stack([r["stb"] for r in res]),
+                            final=np.stack([r["final"] for r in res]),
+                            motion=np.stack([r["motion"] for r in res]),
+                            unique=np.concatenate([r["unique"] for r in res]),
+                            n_unique=np.array([r["unique"].size for r in res]),
+                            psnr=np.array([r["psnr"] for r in res]),
+                            params=np.array([sa, thr, ii]))
+        print(key, [r["unique"].size for r in res])
+    with open(os.path.join(OUT_DIR, "golden.json"), "w") as f:
+        json.dump(golden, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

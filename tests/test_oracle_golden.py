@@ -1,0 +1,68 @@
+"""The oracle against the golden vectors recorded from the unmodified reference
+encoder (DXTImage ctor + Reencode, codec/dxt_image.cpp:385-436, :868-957)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from mptc_gb300.synth import StreamSpec
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def load_cases():
+    with open(os.path.join(GOLDEN, "golden.json")) as f:
+        return json.load(f)["cases"]
+
+
+CASES = load_cases()
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_oracle_matches_reference_stream(case):
+    spec = StreamSpec(**case["spec"])
+    frames = spec.generate(case["first"], case["count"])
+    # the generator is integer-exact: the inputs must be the reference's inputs
+    assert [sha(f) for f in frames] == case["input_sha"]
+    res = oracle.encode_stream(frames, case["search_area"], case["threshold"],
+                               case["intra_interval"], threads=8)
+    for k, (r, g) in enumerate(zip(res, case["frames"])):
+        assert sha(r.stb) == g["stb"], f"frame {k}: stb blocks"
+        assert sha(r.final) == g["final"], f"frame {k}: final blocks"
+        assert sha(r.motion) == g["motion"], f"frame {k}: motion codes"
+        assert sha(r.unique) == g["unique"], f"frame {k}: unique palette"
+        assert r.stats.n_unique == g["n_unique"]
+        assert r.stats.n_inter == g["n_inter"] and r.stats.n_intra == g["n_intra"]
+        assert abs(r.psnr - g["psnr"]) <= 1e-9 * abs(g["psnr"])
+
+
+@pytest.mark.parametrize("key", ["adv_sa4_thr5_ii16", "adv_sa2_thr0_ii1"])
+def test_oracle_matches_reference_adversarial(key):
+    z = np.load(os.path.join(GOLDEN, f"{key}.npz"))
+    sa, thr, ii = (int(v) for v in z["params"])
+    res = oracle.encode_stream(z["frames"], sa, thr, ii)
+    np.testing.assert_array_equal(np.stack([r.stb for r in res]), z["stb"])
+    np.testing.assert_array_equal(np.stack([r.final for r in res]), z["final"])
+    np.testing.assert_array_equal(np.stack([r.motion for r in res]), z["motion"])
+    np.testing.assert_array_equal(np.concatenate([r.unique for r in res]), z["unique"])
+    np.testing.assert_allclose([r.psnr for r in res], z["psnr"], rtol=1e-12)
+
+
+def test_oracle_threaded_equals_single_thread():
+    frames = StreamSpec(128, 128, 3, seed=3).generate()
+    a = oracle.encode_stream(frames, 8, 5, 16, threads=1)
+    b = oracle.encode_stream(frames, 8, 5, 16, threads=5)
+    for x, y in zip(a, b):
+        assert np.array_equal(x.final, y.final) and np.array_equal(x.motion, y.motion)
+
+
+def test_oracle_rejects_bad_sizes():
+    with pytest.raises(ValueError):
+        oracle.dxt1_encode(np.zeros((6, 8, 3), np.uint8))
