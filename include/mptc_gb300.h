@@ -1,0 +1,121 @@
+/*
+ * mptc_gb300 — GB300 (sm_103a) MPTC encoder hot path behind a C ABI.
+ *
+ * The reference encoder's hot path is the C++ class MPTC::DXTImage
+ * (codec/dxt_image.h:46-198): its constructor DXT1-encodes a frame with
+ * stb_dxt and DXTImage::Reencode runs the index-block search. This library
+ * replaces those two steps with CUDA kernels and returns exactly the data the
+ * rest of the reference codec reads from a DXTImage: the final physical
+ * blocks (_physical_blocks), the motion codes (_motion_indices) and the unique
+ * index palette (_unique_palette). Results are bit-identical to the reference.
+ *
+ * Conventions: every call returns an mptc_status; buffers are caller-owned;
+ * `_dev` pointers are device memory, `_host` pointers host memory; `stream` is
+ * a cudaStream_t passed as void* (NULL = legacy default stream). Frame width
+ * and height must be multiples of 4 (the reference reads past the frame
+ * otherwise, codec/dxt_image.cpp:128-139).
+ *
+ * Layouts (little-endian, raster order of 4x4 blocks, blocks_wide = width/4):
+ *   block  u64 = ep1 | ep2 << 16 | interp << 32   (PhysicalDXTBlock, dxt_image.h:16-23)
+ *   motion u8[2] per block = (x, y); (255,255) marks a unique block,
+ *          x|0x80,y|0x80 an inter match, plain x,y an intra match
+ *          (codec/dxt_image.cpp:701, :761, :892-894, :953)
+ *   unique u32 interp per unique block, in raster order (codec/dxt_image.cpp:954)
+ */
+#ifndef MPTC_GB300_H_
+#define MPTC_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mptc_status {
+  MPTC_OK = 0,
+  MPTC_EINVAL = 1,    /* bad argument: size, search area, NULL pointer */
+  MPTC_ENOMEM = 2,    /* device or pinned allocation failed */
+  MPTC_ETIMEOUT = 3,  /* a bounded device-side wait expired; results invalid */
+  MPTC_ECUDA = 4,     /* a CUDA runtime call failed */
+  MPTC_ESTATE = 5     /* call order: e.g. an inter frame without a previous frame */
+} mptc_status;
+
+/* Encoder parameters. The reference takes them as required command-line
+ * arguments (codec/encoder.cpp:467-470): search_area in blocks (1..63; 64
+ * would collide with the unique sentinel), err_threshold on the per-block
+ * error increase (DXTImage::DXTImage err_threshold, codec/dxt_image.cpp:385-394),
+ * intra_interval as in CompressMultiUnique (codec/codec.cpp:1462-1469). */
+typedef struct mptc_config {
+  int32_t search_area;
+  int32_t err_threshold;
+  int32_t intra_interval;
+  int32_t reserved;
+} mptc_config;
+
+typedef struct mptc_ctx mptc_ctx;
+
+/* Per-frame counters of the last reencode on a context (host-side copy). */
+typedef struct mptc_frame_stats {
+  uint32_t n_inter, n_intra, n_unique;
+  uint32_t is_intra;
+} mptc_frame_stats;
+
+/* Replaces the state the reference keeps in DXTImage statics and in the
+ * constructor's arguments (codec/dxt_image.cpp:25, :357-358, :385-394) with an
+ * explicit context for frames of `width` x `height`; allocates the device
+ * scratch the kernels need. */
+mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t height,
+                            mptc_ctx **out_ctx);
+mptc_status mptc_ctx_destroy(mptc_ctx *ctx);
+
+/* Stage 1, the DXTImage constructor's stb_dxt pass: CompressRGB + the block
+ * loop, codec/dxt_image.cpp:123-149 and :419-431 (stb_compress_dxt_block with
+ * alpha=0, STB_DXT_HIGHQUAL, Include/stb_dxt.h:613-627).
+ * rgb_dev: width*height*3 bytes, row-major RGB8. blocks_dev: blocks u64.
+ * orig_err_dev: per block floor(SSE/48) of the stb block (CompressedBlock::Error,
+ * codec/dxt_image.cpp:258-276), consumed by mptc_reencode; may be NULL. */
+mptc_status mptc_dxt1_encode(mptc_ctx *ctx, const uint8_t *rgb_dev, uint64_t *blocks_dev,
+                             int32_t *orig_err_dev, void *stream);
+
+/* Stage 2, DXTImage::Reencode(prev, ref) (codec/dxt_image.cpp:868-957): the
+ * inter search over prev_final_dev (the previous frame's final blocks; NULL
+ * makes this an intra frame), the causal intra search over this frame, and the
+ * unique palette. stb_dev / orig_err_dev come from mptc_dxt1_encode on the same
+ * frame. Writes final_dev (blocks), motion_dev (2 bytes/block), unique_dev
+ * (up to blocks u32) and *n_unique_dev (device u32). */
+mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev,
+                          const int32_t *orig_err_dev, const uint64_t *prev_final_dev,
+                          uint64_t *final_dev, uint8_t *motion_dev, uint32_t *unique_dev,
+                          uint32_t *n_unique_dev, void *stream);
+
+/* Stage 1 + 2 on one device-resident frame, using context-owned stb/orig_err
+ * scratch. stb_dev may be NULL when the caller does not need the stb blocks. */
+mptc_status mptc_encode_frame(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *prev_final_dev,
+                              uint64_t *stb_dev, uint64_t *final_dev, uint8_t *motion_dev,
+                              uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream);
+
+/* The DXTImage(file, is_intra, ...) + Reencode pair on HOST buffers, the call a
+ * host encoder loop makes per frame (codec/codec.cpp:1388-1394). The context
+ * keeps the previous frame's final blocks on the device, so successive calls
+ * form a stream; is_intra=1 starts (or restarts) it. Copies in on `stream`
+ * through pinned staging, runs both stages and copies the outputs back before
+ * returning. stb_host may be NULL. Returns the number of unique blocks in
+ * *n_unique_host. */
+mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32_t is_intra,
+                                   uint64_t *stb_host, uint64_t *final_host, uint8_t *motion_host,
+                                   uint32_t *unique_host, uint32_t *n_unique_host, void *stream);
+
+/* Counters of the last frame reencoded on this context (synchronises `stream`). */
+mptc_status mptc_last_frame_stats(mptc_ctx *ctx, mptc_frame_stats *out, void *stream);
+
+/* Human-readable text of the last error on this context (never NULL). */
+const char *mptc_last_error(const mptc_ctx *ctx);
+
+/* Library version and the device architecture it was built for (e.g. 1030). */
+int32_t mptc_version(void);
+int32_t mptc_built_arch(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,73 @@
+"""ctypes binding of ``libmptc_gb300.so`` (the C ABI in include/mptc_gb300.h).
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmptc_gb300.so")
+
+MPTC_OK, MPTC_EINVAL, MPTC_ENOMEM, MPTC_ETIMEOUT, MPTC_ECUDA, MPTC_ESTATE = range(6)
+STATUS_NAMES = {0: "MPTC_OK", 1: "MPTC_EINVAL", 2: "MPTC_ENOMEM", 3: "MPTC_ETIMEOUT",
+                4: "MPTC_ECUDA", 5: "MPTC_ESTATE"}
+
+# Every symbol include/mptc_gb300.h declares.
+EXPORTED = [
+    "mptc_ctx_create", "mptc_ctx_destroy", "mptc_dxt1_encode", "mptc_reencode",
+    "mptc_encode_frame", "mptc_encode_frame_host", "mptc_last_frame_stats", "mptc_last_error",
+    "mptc_version", "mptc_built_arch",
+]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("search_area", ctypes.c_int32), ("err_threshold", ctypes.c_int32),
+                ("intra_interval", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class FrameStats(ctypes.Structure):
+    _fields_ = [("n_inter", ctypes.c_uint32), ("n_intra", ctypes.c_uint32),
+                ("n_unique", ctypes.c_uint32), ("is_intra", ctypes.c_uint32)]
+
+
+class MptcError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+_LIB = None
+
+
+def lib() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() "
+                               "(the encoder has no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, u32p = ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p
+        L.mptc_ctx_create.argtypes = [ctypes.POINTER(Config), i32, i32, ctypes.POINTER(vp)]
+        L.mptc_ctx_destroy.argtypes = [vp]
+        L.mptc_dxt1_encode.argtypes = [vp, vp, vp, vp, vp]
+        L.mptc_reencode.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, u32p, vp]
+        L.mptc_encode_frame.argtypes = [vp, vp, vp, vp, vp, vp, vp, u32p, vp]
+        L.mptc_encode_frame_host.argtypes = [vp, vp, i32, vp, vp, vp, vp, u32p, vp]
+        L.mptc_last_frame_stats.argtypes = [vp, ctypes.POINTER(FrameStats), vp]
+        L.mptc_last_error.argtypes = [vp]
+        L.mptc_last_error.restype = ctypes.c_char_p
+        L.mptc_version.restype = i32
+        L.mptc_built_arch.restype = i32
+        for name in EXPORTED:
+            if name not in ("mptc_last_error", "mptc_version", "mptc_built_arch"):
+                getattr(L, name).restype = ctypes.c_int
+        _LIB = L
+    return _LIB
+
+
+def check(status: int, ctx=None) -> None:
+    if status != MPTC_OK:
+        msg = lib().mptc_last_error(ctx).decode() if ctx else ""
+        raise MptcError(status, msg)

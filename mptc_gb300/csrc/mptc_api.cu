@@ -1,0 +1,334 @@
+// C ABI of the GB300 MPTC encoder hot path (declared in include/mptc_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "../../include/mptc_gb300.h"
+#include "dxt1_encode.cuh"
+#include "search.cuh"
+
+namespace {
+
+constexpr int kSearchWarps = 8;
+
+struct Stats3 {
+  uint32_t n_inter, n_intra, n_unique;
+};
+
+}  // namespace
+
+struct mptc_ctx {
+  mptc_config cfg{};
+  int width = 0, height = 0, bw = 0, bh = 0, nblk = 0, ntiles = 0;
+  int device = 0, sm_count = 0, intra_grid = 0;
+  // device scratch
+  uint32_t *done = nullptr;        // per block
+  uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats
+  uint32_t *tile_counts = nullptr; // per unique tile
+  uint64_t *stb = nullptr;         // stb blocks (encode_frame / host path)
+  int32_t *orig_err = nullptr;
+  // host-path buffers
+  uint8_t *rgb_dev = nullptr;
+  uint64_t *final_dev[2] = {nullptr, nullptr};
+  uint8_t *motion_dev = nullptr;
+  uint32_t *unique_dev = nullptr;
+  uint32_t *n_unique_dev = nullptr;
+  uint8_t *pin_in = nullptr;   // pinned staging
+  uint8_t *pin_out = nullptr;
+  int cur = 0;                 // which final_dev holds the latest frame
+  bool have_prev = false;
+  uint32_t last_is_intra = 0;
+  std::string err;
+};
+
+namespace {
+
+std::once_flag g_tables_once;
+cudaError_t g_tables_err = cudaSuccess;
+
+// stb__PrepareOptTable semantics (Include/stb_dxt.h:111-137): for every 8-bit
+// value, the (max, min) endpoint pair whose 1/3 interpolation is closest,
+// with the DX10 3% slack term; earliest pair wins ties.
+void build_opt_table(uint8_t table[256][2], int bits) {
+  const int size = 1 << bits;
+  for (int v = 0; v < 256; ++v) {
+    int best = 256;
+    for (int lo = 0; lo < size; ++lo) {
+      for (int hi = 0; hi < size; ++hi) {
+        const int elo = bits == 5 ? ((lo << 3) | (lo >> 2)) : ((lo << 2) | (lo >> 4));
+        const int ehi = bits == 5 ? ((hi << 3) | (hi >> 2)) : ((hi << 2) | (hi >> 4));
+        int d = (2 * ehi + elo) / 3 - v;
+        int err = (d < 0 ? -d : d) + (ehi > elo ? ehi - elo : elo - ehi) * 3 / 100;
+        if (err < best) {
+          table[v][0] = (uint8_t)hi;
+          table[v][1] = (uint8_t)lo;
+          best = err;
+        }
+      }
+    }
+  }
+}
+
+void upload_tables() {
+  static uint8_t t5[256][2], t6[256][2];
+  build_opt_table(t5, 5);
+  build_opt_table(t6, 6);
+  g_tables_err = cudaMemcpyToSymbol(mptc::c_omatch5, t5, sizeof(t5));
+  if (g_tables_err == cudaSuccess) g_tables_err = cudaMemcpyToSymbol(mptc::c_omatch6, t6, sizeof(t6));
+}
+
+mptc_status fail(mptc_ctx *ctx, mptc_status st, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return st;
+}
+
+mptc_status cuda_fail(mptc_ctx *ctx, cudaError_t e, const char *what) {
+  return fail(ctx, MPTC_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define MPTC_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t n) {
+  return cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T) + 16);
+}
+
+mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t *stb, const int32_t *orig,
+                               const uint64_t *prev, uint64_t *fin, uint8_t *motion) {
+  mptc::SearchParams P;
+  P.rgb = rgb;
+  P.stb = stb;
+  P.orig_err = orig;
+  P.prev = prev;
+  P.final_blk = fin;
+  P.motion = reinterpret_cast<uint16_t *>(motion);
+  P.done = ctx->done;
+  P.work = ctx->work;
+  P.status = ctx->work + 1;
+  P.width = ctx->width;
+  P.bw = ctx->bw;
+  P.bh = ctx->bh;
+  P.sa = ctx->cfg.search_area;
+  P.thr = ctx->cfg.err_threshold;
+  return P;
+}
+
+__global__ void frame_stats_kernel(const uint16_t *__restrict__ motion, int nblk, uint32_t *__restrict__ stats) {
+  int ni = 0, na = 0, nu = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
+    const uint16_t m = motion[i];
+    nu += m == 0xFFFFu;
+    ni += m != 0xFFFFu && (m & 0x80u);
+    na += m != 0xFFFFu && !(m & 0x80u);
+  }
+  ni = __reduce_add_sync(0xffffffffu, ni);
+  na = __reduce_add_sync(0xffffffffu, na);
+  nu = __reduce_add_sync(0xffffffffu, nu);
+  if ((threadIdx.x & 31) == 0) {
+    if (ni) atomicAdd(stats + 0, (uint32_t)ni);
+    if (na) atomicAdd(stats + 1, (uint32_t)na);
+    if (nu) atomicAdd(stats + 2, (uint32_t)nu);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mptc_version(void) { return 100; }
+int32_t mptc_built_arch(void) { return 1030; }
+
+const char *mptc_last_error(const mptc_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t height, mptc_ctx **out_ctx) {
+  if (!cfg || !out_ctx) return MPTC_EINVAL;
+  *out_ctx = nullptr;
+  if (width <= 0 || height <= 0 || (width & 3) || (height & 3)) return MPTC_EINVAL;
+  if (cfg->search_area < 1 || cfg->search_area > 63) return MPTC_EINVAL;
+  if (cfg->err_threshold == 0x7fffffff) return MPTC_EINVAL;  // would accept "no candidate"
+  if ((int64_t)width * height > (int64_t)1 << 30) return MPTC_EINVAL;
+  mptc_ctx *ctx = new (std::nothrow) mptc_ctx();
+  if (!ctx) return MPTC_ENOMEM;
+  ctx->cfg = *cfg;
+  ctx->width = width;
+  ctx->height = height;
+  ctx->bw = width / 4;
+  ctx->bh = height / 4;
+  ctx->nblk = ctx->bw * ctx->bh;
+  ctx->ntiles = (ctx->nblk + mptc::kUniqTile - 1) / mptc::kUniqTile;
+  auto bad = [&](mptc_status st) {
+    mptc_ctx_destroy(ctx);
+    return st;
+  };
+  if (cudaGetDevice(&ctx->device) != cudaSuccess) return bad(MPTC_ECUDA);
+  if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
+    return bad(MPTC_ECUDA);
+  std::call_once(g_tables_once, upload_tables);
+  if (g_tables_err != cudaSuccess) return bad(MPTC_ECUDA);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_search_kernel<kSearchWarps>,
+                                                    kSearchWarps * 32, 0) != cudaSuccess)
+    return bad(MPTC_ECUDA);
+  ctx->intra_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
+  const size_t n = (size_t)ctx->nblk;
+  if (dalloc(&ctx->done, n) || dalloc(&ctx->work, 8) || dalloc(&ctx->tile_counts, (size_t)ctx->ntiles) ||
+      dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
+      dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
+      dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1))
+    return bad(MPTC_ENOMEM);
+  if (cudaMemset(ctx->work, 0, 8 * sizeof(uint32_t)) != cudaSuccess) return bad(MPTC_ECUDA);
+  if (cudaMallocHost(reinterpret_cast<void **>(&ctx->pin_in), n * 48) != cudaSuccess ||
+      cudaMallocHost(reinterpret_cast<void **>(&ctx->pin_out), n * (8 + 2 + 4) + 64) != cudaSuccess)
+    return bad(MPTC_ENOMEM);
+  *out_ctx = ctx;
+  return MPTC_OK;
+}
+
+mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
+  if (!ctx) return MPTC_EINVAL;
+  cudaFree(ctx->done);
+  cudaFree(ctx->work);
+  cudaFree(ctx->tile_counts);
+  cudaFree(ctx->stb);
+  cudaFree(ctx->orig_err);
+  cudaFree(ctx->rgb_dev);
+  cudaFree(ctx->final_dev[0]);
+  cudaFree(ctx->final_dev[1]);
+  cudaFree(ctx->motion_dev);
+  cudaFree(ctx->unique_dev);
+  cudaFree(ctx->n_unique_dev);
+  if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
+  if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
+  delete ctx;
+  return MPTC_OK;
+}
+
+mptc_status mptc_dxt1_encode(mptc_ctx *ctx, const uint8_t *rgb_dev, uint64_t *blocks_dev, int32_t *orig_err_dev,
+                             void *stream) {
+  if (!ctx) return MPTC_EINVAL;
+  if (!rgb_dev || !blocks_dev || !aligned(rgb_dev, 16) || !aligned(blocks_dev, 8) ||
+      (orig_err_dev && !aligned(orig_err_dev, 4)))
+    return fail(ctx, MPTC_EINVAL, "mptc_dxt1_encode: null or misaligned pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int threads = 128;
+  int grid = (ctx->nblk + threads - 1) / threads;
+  mptc::dxt1_encode_kernel<<<grid, threads, 0, s>>>(rgb_dev, ctx->width, ctx->bw, ctx->nblk, blocks_dev,
+                                                     orig_err_dev);
+  MPTC_CUDA(cudaGetLastError());
+  return MPTC_OK;
+}
+
+mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev, const int32_t *orig_err_dev,
+                          const uint64_t *prev_final_dev, uint64_t *final_dev, uint8_t *motion_dev,
+                          uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream) {
+  if (!ctx) return MPTC_EINVAL;
+  if (!rgb_dev || !stb_dev || !orig_err_dev || !final_dev || !motion_dev || !unique_dev || !n_unique_dev)
+    return fail(ctx, MPTC_EINVAL, "mptc_reencode: null pointer");
+  if (!aligned(rgb_dev, 16) || !aligned(stb_dev, 8) || !aligned(final_dev, 8) || !aligned(motion_dev, 2) ||
+      (prev_final_dev && !aligned(prev_final_dev, 8)) || !aligned(orig_err_dev, 4) || !aligned(unique_dev, 4))
+    return fail(ctx, MPTC_EINVAL, "mptc_reencode: misaligned pointer");
+  if (prev_final_dev == final_dev) return fail(ctx, MPTC_EINVAL, "mptc_reencode: prev and final alias");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  mptc::SearchParams P = make_params(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev);
+  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, 8 * sizeof(uint32_t), s));
+  if (prev_final_dev) {
+    int grid = (ctx->nblk + kSearchWarps - 1) / kSearchWarps;
+    mptc::inter_search_kernel<kSearchWarps><<<grid, kSearchWarps * 32, 0, s>>>(P);
+    MPTC_CUDA(cudaGetLastError());
+  } else {
+    MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint32_t), s));
+  }
+  mptc::intra_search_kernel<kSearchWarps><<<ctx->intra_grid, kSearchWarps * 32, 0, s>>>(P);
+  MPTC_CUDA(cudaGetLastError());
+  const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
+  mptc::unique_count_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, ctx->nblk, ctx->tile_counts);
+  mptc::unique_scatter_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, stb_dev, ctx->nblk, ctx->tile_counts, ctx->ntiles,
+                                                         unique_dev, n_unique_dev);
+  frame_stats_kernel<<<ctx->sm_count, 256, 0, s>>>(m16, ctx->nblk, ctx->work + 2);
+  MPTC_CUDA(cudaGetLastError());
+  ctx->last_is_intra = prev_final_dev ? 0u : 1u;
+  return MPTC_OK;
+}
+
+mptc_status mptc_encode_frame(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *prev_final_dev, uint64_t *stb_dev,
+                              uint64_t *final_dev, uint8_t *motion_dev, uint32_t *unique_dev, uint32_t *n_unique_dev,
+                              void *stream) {
+  if (!ctx) return MPTC_EINVAL;
+  uint64_t *stb = stb_dev ? stb_dev : ctx->stb;
+  mptc_status st = mptc_dxt1_encode(ctx, rgb_dev, stb, ctx->orig_err, stream);
+  if (st != MPTC_OK) return st;
+  return mptc_reencode(ctx, rgb_dev, stb, ctx->orig_err, prev_final_dev, final_dev, motion_dev, unique_dev,
+                       n_unique_dev, stream);
+}
+
+mptc_status mptc_last_frame_stats(mptc_ctx *ctx, mptc_frame_stats *out, void *stream) {
+  if (!ctx || !out) return MPTC_EINVAL;
+  uint32_t w[5];
+  MPTC_CUDA(cudaMemcpyAsync(w, ctx->work, sizeof(w), cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream)));
+  MPTC_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  out->n_inter = w[2];
+  out->n_intra = w[3];
+  out->n_unique = w[4];
+  out->is_intra = ctx->last_is_intra;
+  if (w[1] & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
+  return MPTC_OK;
+}
+
+mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32_t is_intra, uint64_t *stb_host,
+                                   uint64_t *final_host, uint8_t *motion_host, uint32_t *unique_host,
+                                   uint32_t *n_unique_host, void *stream) {
+  if (!ctx) return MPTC_EINVAL;
+  if (!rgb_host || !final_host || !motion_host || !unique_host || !n_unique_host)
+    return fail(ctx, MPTC_EINVAL, "mptc_encode_frame_host: null pointer");
+  if (!is_intra && !ctx->have_prev)
+    return fail(ctx, MPTC_ESTATE, "mptc_encode_frame_host: inter frame without a previous frame");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)ctx->nblk, in_bytes = n * 48;
+  // Pinned caller buffers are copied directly; pageable ones go through staging.
+  cudaPointerAttributes attr;
+  const bool in_pinned = cudaPointerGetAttributes(&attr, rgb_host) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  if (in_pinned) {
+    MPTC_CUDA(cudaMemcpyAsync(ctx->rgb_dev, rgb_host, in_bytes, cudaMemcpyHostToDevice, s));
+  } else {
+    std::memcpy(ctx->pin_in, rgb_host, in_bytes);
+    MPTC_CUDA(cudaMemcpyAsync(ctx->rgb_dev, ctx->pin_in, in_bytes, cudaMemcpyHostToDevice, s));
+  }
+  const int nxt = ctx->have_prev ? 1 - ctx->cur : ctx->cur;
+  const uint64_t *prev = is_intra ? nullptr : ctx->final_dev[ctx->cur];
+  mptc_status st = mptc_encode_frame(ctx, ctx->rgb_dev, prev, ctx->stb, ctx->final_dev[nxt], ctx->motion_dev,
+                                     ctx->unique_dev, ctx->n_unique_dev, stream);
+  if (st != MPTC_OK) return st;
+  uint8_t *o = ctx->pin_out;
+  MPTC_CUDA(cudaMemcpyAsync(o, ctx->final_dev[nxt], n * 8, cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(o + n * 8, ctx->motion_dev, n * 2, cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(o + n * 10, ctx->unique_dev, n * 4, cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(o + n * 14, ctx->n_unique_dev, 4, cudaMemcpyDeviceToHost, s));
+  if (stb_host) MPTC_CUDA(cudaMemcpyAsync(stb_host, ctx->stb, n * 8, cudaMemcpyDeviceToHost, s));
+  uint32_t w[2];
+  MPTC_CUDA(cudaMemcpyAsync(w, ctx->work, sizeof(w), cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaStreamSynchronize(s));
+  if (w[1] & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
+  uint32_t nu;
+  std::memcpy(&nu, o + n * 14, 4);
+  std::memcpy(final_host, o, n * 8);
+  std::memcpy(motion_host, o + n * 8, n * 2);
+  std::memcpy(unique_host, o + n * 10, (size_t)nu * 4);
+  *n_unique_host = nu;
+  ctx->cur = nxt;
+  ctx->have_prev = true;
+  return MPTC_OK;
+}
+
+}  // extern "C"

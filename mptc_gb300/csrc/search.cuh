@@ -1,0 +1,461 @@
+// K-b: the index-block search of DXTImage::Reencode (codec/dxt_image.cpp:652-957).
+//
+// For a block and a candidate index word (the interp of a block in the search
+// window) the reference assigns the candidate's indices, refits both endpoints
+// by least squares in float, snaps them with ToFiveBits/ToSixBits, and keeps
+// the candidate only if Pack565(ep1) > Pack565(ep2); the candidate's error is
+// floor(SSE/48) against the block's own pixels, compared with the block's stb
+// error (orig_err). A warp evaluates one block, its lanes walking the window in
+// 32-position chunks of the reference's scan order; a warp-uniform state
+// machine then applies the reference's selection rule exactly:
+//
+//   positions are scanned row by row; a candidate replaces the running minimum
+//   when err_diff < min; the first err_diff <= 0 pins min to 0 and ends that
+//   ROW only (the `break` leaves the inner loop), so a later row can still
+//   replace the selection with a strictly negative err_diff.
+//
+// The inter search reads the previous frame only and runs fully parallel. The
+// intra search reads this frame's blocks as already finalised in raster order,
+// so it runs as a dataflow over blocks: each block waits (bounded) on per-block
+// release flags of every block in its causal window, then decides and
+// publishes its own flag.
+#pragma once
+#include <cstdint>
+
+namespace mptc {
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kInvalid = 0x7fffffff;  // invalid candidate / no selection (INT_MAX)
+
+// Device status bits (OR-ed into the context's status word).
+constexpr uint32_t kDevTimeout = 1u;
+
+// Per-warp staging of the block being searched.
+struct __align__(16) WarpBlock {
+  float4 p[16];   // pixel r, g, b as float
+  float4 q[16];   // fl(px * fl(1/3)) per channel
+  float4 q2[16];  // fl(px * fl(2/3)) = 2 * q (exact)
+  uint32_t pk[16];  // packed r | g<<8 | b<<16 for the integer error
+};
+
+// Selection state of the reference's candidate loop (warp-uniform).
+struct SelState {
+  int min_e;        // running min err_diff, kInvalid when nothing valid yet
+  int broken_row;   // row left by `break` (-1 none)
+  int sel_pos;      // scan position of the selection
+  uint32_t sel_cand;
+  uint32_t sel_eps;   // ep1 | ep2 << 16 (RGB565) of the refit, 0 for identity
+  int sel_refit;
+};
+
+__device__ __forceinline__ void sel_init(SelState &s) {
+  s.min_e = kInvalid;
+  s.broken_row = -1;
+  s.sel_pos = -1;
+  s.sel_cand = 0;
+  s.sel_eps = 0;
+  s.sel_refit = 0;
+}
+
+// One 32-position chunk (positions strictly increasing with the lane) of the
+// reference loop; `e` is kInvalid for skipped positions.
+__device__ __forceinline__ void sel_chunk(SelState &s, int lane, int row, int e, int pos, uint32_t cand,
+                                          uint32_t eps, int refit) {
+  bool active = (e != kInvalid) && (row != s.broken_row);
+  if (s.min_e > 0) {
+    const unsigned le0 = __ballot_sync(kFull, active && e <= 0);
+    const int first = le0 ? __ffs(le0) - 1 : 32;
+    const bool pre = active && lane < first;  // all positive here
+    const int m = __reduce_min_sync(kFull, pre ? e : kInvalid);
+    if (m < s.min_e) {
+      const int who = __ffs(__ballot_sync(kFull, pre && e == m)) - 1;
+      s.min_e = m;
+      s.sel_pos = __shfl_sync(kFull, pos, who);
+      s.sel_cand = __shfl_sync(kFull, cand, who);
+      s.sel_eps = __shfl_sync(kFull, eps, who);
+      s.sel_refit = __shfl_sync(kFull, refit, who);
+    }
+    if (!le0) return;
+    s.min_e = 0;
+    s.sel_pos = __shfl_sync(kFull, pos, first);
+    s.sel_cand = __shfl_sync(kFull, cand, first);
+    s.sel_eps = __shfl_sync(kFull, eps, first);
+    s.sel_refit = __shfl_sync(kFull, refit, first);
+    s.broken_row = __shfl_sync(kFull, row, first);
+    active = active && lane > first && row != s.broken_row;
+  }
+  // min is 0: only err_diff < 0 in a row not yet left can replace it, and the
+  // first such position of each later row does (then leaves that row).
+  const bool neg = active && e < 0;
+  if (__any_sync(kFull, neg)) {
+    const int maxrow = __reduce_max_sync(kFull, neg ? row : -1);
+    const int who = __ffs(__ballot_sync(kFull, neg && row == maxrow)) - 1;
+    s.sel_pos = __shfl_sync(kFull, pos, who);
+    s.sel_cand = __shfl_sync(kFull, cand, who);
+    s.sel_eps = __shfl_sync(kFull, eps, who);
+    s.sel_refit = __shfl_sync(kFull, refit, who);
+    s.broken_row = maxrow;
+  }
+}
+
+// ToFiveBits / ToSixBits (codec/dxt_image.cpp:72-121) as 256-entry tables,
+// built per CTA in shared memory: value -> snapped 8-bit value.
+__device__ __forceinline__ uint8_t snap_value(uint32_t x, uint32_t keep, uint32_t step, uint32_t sh) {
+  uint32_t base = x & keep;
+  uint32_t high = (base == 255u) ? base : base + step;
+  uint32_t low = (base == 0u) ? base : base - step;
+  base = (base | (base >> sh)) & 0xFF;
+  high = (high | (high >> sh)) & 0xFF;
+  low = (low | (low >> sh)) & 0xFF;
+  const uint32_t db = x > base ? x - base : base - x;
+  const uint32_t dh = x > high ? x - high : high - x;
+  const uint32_t dl = x > low ? x - low : low - x;
+  if (db <= dh) return (uint8_t)(db < dl ? base : low);
+  return (uint8_t)high;
+}
+
+__device__ __forceinline__ void build_snap_tables(uint8_t *snap5, uint8_t *snap6) {
+  for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+    snap5[t] = snap_value((uint32_t)t, 0xF8u, 4u, 5u);
+    snap6[t] = snap_value((uint32_t)t, 0xFCu, 2u, 6u);
+  }
+}
+
+// Stages block (bx, by) for the warp: pixels, their fl(px/3) products and the
+// block's sum of squares.
+__device__ __forceinline__ int stage_block(WarpBlock &wb, const uint8_t *__restrict__ rgb, int width,
+                                           int bx, int by, int lane) {
+  int sq = 0;
+  if (lane < 16) {
+    const int r = lane >> 2, c = lane & 3;
+    const uint8_t *p = rgb + ((size_t)(4 * by + r) * width + 4 * bx + c) * 3;
+    const uint32_t R = p[0], G = p[1], B = p[2];
+    const float third = __fdiv_rn(1.0f, 3.0f);
+    const float fr = __uint2float_rn(R), fg = __uint2float_rn(G), fb = __uint2float_rn(B);
+    const float qr = __fmul_rn(fr, third), qg = __fmul_rn(fg, third), qb = __fmul_rn(fb, third);
+    wb.p[lane] = make_float4(fr, fg, fb, 0.0f);
+    wb.q[lane] = make_float4(qr, qg, qb, 0.0f);
+    wb.q2[lane] = make_float4(__fadd_rn(qr, qr), __fadd_rn(qg, qg), __fadd_rn(qb, qb), 0.0f);
+    wb.pk[lane] = R | (G << 8) | (B << 16);
+    sq = (int)(R * R + G * G + B * B);
+  }
+  __syncwarp();
+  return __reduce_add_sync(kFull, sq);
+}
+
+// x86 cvttss2si of v followed by max(0, min(255, .)) (codec/dxt_image.cpp:330-331):
+// NaN and |v| >= 2^31 convert to INT_MIN and therefore clamp to 0.
+__device__ __forceinline__ uint32_t quantize_endpoint(float v) {
+  float w = (v < 2147483648.0f) ? v : 0.0f;  // also maps NaN to 0
+  w = fminf(fmaxf(w, 0.0f), 255.0f);
+  return __float_as_uint(__fadd_rd(w, 8388608.0f)) - 0x4B000000u;  // floor(w)
+}
+
+__device__ __forceinline__ uint32_t pack565(uint32_t r, uint32_t g, uint32_t b) {
+  return ((r & 0xF8u) << 8) | ((g & 0xFCu) << 3) | (b >> 3);
+}
+
+// Evaluates candidate `cand` on the staged block. Returns err_diff, or
+// kInvalid when the refit would swap the endpoints (the candidate is skipped).
+// `own` is the block's stb interp: AssignIndices with it is the identity
+// (blk == blk2), which keeps the stb block with err_diff 0 and no refit.
+__device__ __forceinline__ int eval_candidate(const WarpBlock &wb, const uint8_t *snap5,
+                                              const uint8_t *snap6, uint32_t cand, uint32_t own,
+                                              int orig_err, int sumsq, uint32_t &eps, int &refit) {
+  if (cand == own) {
+    eps = 0;
+    refit = 0;
+    return 0;
+  }
+  refit = 1;
+  // a = (3 - order)/3, b = order/3 with order = {0,3,1,2}[index]; the products
+  // px*a, px*b are {px,0}, {0,px}, {2q,q}, {q,2q}; a*a etc. are constants.
+  const float third = __fdiv_rn(1.0f, 3.0f), two3 = __fdiv_rn(2.0f, 3.0f);
+  const float k49 = __fmul_rn(two3, two3), k19 = __fmul_rn(third, third), k29 = __fmul_rn(two3, third);
+  float asq = 0.f, bsq = 0.f, ab = 0.f;
+  float ax0 = 0.f, ax1 = 0.f, ax2 = 0.f, bx0 = 0.f, bx1 = 0.f, bx2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const bool b0 = (cand >> (2 * i)) & 1u;
+    const bool b1 = (cand >> (2 * i + 1)) & 1u;
+    const float4 P = wb.p[i], Q = wb.q[i], Q2 = wb.q2[i];
+    const float xa = b1 ? k49 : 1.0f, ya = b1 ? k19 : 0.0f;
+    asq = __fadd_rn(asq, b0 ? ya : xa);
+    bsq = __fadd_rn(bsq, b0 ? xa : ya);
+    ab = __fadd_rn(ab, b1 ? k29 : 0.0f);
+    const float x0 = b1 ? Q2.x : P.x, y0 = b1 ? Q.x : 0.0f;
+    const float x1 = b1 ? Q2.y : P.y, y1 = b1 ? Q.y : 0.0f;
+    const float x2 = b1 ? Q2.z : P.z, y2 = b1 ? Q.z : 0.0f;
+    ax0 = __fadd_rn(ax0, b0 ? y0 : x0);
+    bx0 = __fadd_rn(bx0, b0 ? x0 : y0);
+    ax1 = __fadd_rn(ax1, b0 ? y1 : x1);
+    bx1 = __fadd_rn(bx1, b0 ? x1 : y1);
+    ax2 = __fadd_rn(ax2, b0 ? y2 : x2);
+    bx2 = __fadd_rn(bx2, b0 ? x2 : y2);
+  }
+  const float f = __frcp_rn(__fsub_rn(__fmul_rn(asq, bsq), __fmul_rn(ab, ab)));
+  const float p1r = __fmul_rn(f, __fsub_rn(__fmul_rn(ax0, bsq), __fmul_rn(bx0, ab)));
+  const float p1g = __fmul_rn(f, __fsub_rn(__fmul_rn(ax1, bsq), __fmul_rn(bx1, ab)));
+  const float p1b = __fmul_rn(f, __fsub_rn(__fmul_rn(ax2, bsq), __fmul_rn(bx2, ab)));
+  const float p2r = __fmul_rn(f, __fsub_rn(__fmul_rn(bx0, asq), __fmul_rn(ax0, ab)));
+  const float p2g = __fmul_rn(f, __fsub_rn(__fmul_rn(bx1, asq), __fmul_rn(ax1, ab)));
+  const float p2b = __fmul_rn(f, __fsub_rn(__fmul_rn(bx2, asq), __fmul_rn(ax2, ab)));
+  const uint32_t e1r = snap5[quantize_endpoint(__fadd_rn(p1r, 0.5f))];
+  const uint32_t e1g = snap6[quantize_endpoint(__fadd_rn(p1g, 0.5f))];
+  const uint32_t e1b = snap5[quantize_endpoint(__fadd_rn(p1b, 0.5f))];
+  const uint32_t e2r = snap5[quantize_endpoint(__fadd_rn(p2r, 0.5f))];
+  const uint32_t e2g = snap6[quantize_endpoint(__fadd_rn(p2g, 0.5f))];
+  const uint32_t e2b = snap5[quantize_endpoint(__fadd_rn(p2b, 0.5f))];
+  const uint32_t q1 = pack565(e1r, e1g, e1b), q2 = pack565(e2r, e2g, e2b);
+  if (q1 <= q2) return kInvalid;  // LogicalToPhysical would swap: skipped
+  eps = q1 | (q2 << 16);
+  // 4-colour palette of the refit (LerpChannels 1/3, 2/3, :346-347)
+  const uint32_t c0 = e1r | (e1g << 8) | (e1b << 16);
+  const uint32_t c1 = e2r | (e2g << 8) | (e2b << 16);
+  const uint32_t c2 = ((2 * e1r + e2r) / 3) | (((2 * e1g + e2g) / 3) << 8) | (((2 * e1b + e2b) / 3) << 16);
+  const uint32_t c3 = ((e1r + 2 * e2r) / 3) | (((e1g + 2 * e2g) / 3) << 8) | (((e1b + 2 * e2b) / 3) << 16);
+  // SSE = sum|s|^2 - 2 sum s.pal[idx] + sum_k n_k |pal_k|^2, all exact integers
+  const uint32_t lo = cand & 0x55555555u, hi = (cand >> 1) & 0x55555555u;
+  const int n3 = __popc(lo & hi), n1 = __popc(lo & ~hi), n2 = __popc(hi & ~lo);
+  const int n0 = 16 - n1 - n2 - n3;
+  uint32_t cross = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const bool b0 = (cand >> (2 * i)) & 1u;
+    const bool b1 = (cand >> (2 * i + 1)) & 1u;
+    const uint32_t pal = b1 ? (b0 ? c3 : c2) : (b0 ? c1 : c0);
+    cross = __dp4a(wb.pk[i], pal, cross);
+  }
+  const uint32_t z = 0u;
+  const int sse = sumsq - 2 * (int)cross + n0 * (int)__dp4a(c0, c0, z) + n1 * (int)__dp4a(c1, c1, z) +
+                  n2 * (int)__dp4a(c2, c2, z) + n3 * (int)__dp4a(c3, c3, z);
+  return (int)((uint32_t)sse / 48u) - orig_err;
+}
+
+struct SearchParams {
+  const uint8_t *rgb;
+  const uint64_t *stb;
+  const int32_t *orig_err;
+  const uint64_t *prev;   // previous frame's final blocks (inter)
+  uint64_t *final_blk;
+  uint16_t *motion;       // (x | y << 8) per block
+  uint32_t *done;         // per block: 1 once final (release/acquire)
+  uint32_t *work;         // dataflow work counter
+  uint32_t *status;       // device status bits
+  int width, bw, bh, sa, thr;
+};
+
+// ------------------------------------------------------------------ inter --
+// InterBlockSearch, codec/dxt_image.cpp:715-774: rows j = by-sa .. by+sa-1,
+// columns i = bx-sa .. bx+sa-1 (both ascending); motion (i-bx+sa)|0x80,
+// (j-by+sa)|0x80. Accepted blocks become final here; the others are left for
+// the intra pass (done = 0).
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P) {
+  __shared__ WarpBlock s_wb[WARPS];
+  __shared__ uint8_t s_snap5[256], s_snap6[256];
+  build_snap_tables(s_snap5, s_snap6);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpBlock &wb = s_wb[warp];
+  const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
+  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
+  for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
+    const int by = idx / P.bw, bx = idx - by * P.bw;
+    const int sumsq = stage_block(wb, P.rgb, P.width, bx, by, lane);
+    const uint64_t stb = P.stb[idx];
+    const uint32_t own = (uint32_t)(stb >> 32);
+    const int orig = P.orig_err[idx];
+    SelState st;
+    sel_init(st);
+    for (int base = 0; base < npos; base += 32) {
+      const int pos = base + lane;
+      const int row = pos / w2, col = pos - row * w2;
+      const int j = by - P.sa + row, i = bx - P.sa + col;
+      int e = kInvalid, refit = 0;
+      uint32_t cand = 0, eps = 0;
+      if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
+        cand = __ldg(prev_hi + 2 * ((size_t)j * P.bw + i));
+        e = eval_candidate(wb, s_snap5, s_snap6, cand, own, orig, sumsq, eps, refit);
+      }
+      sel_chunk(st, lane, row, e, pos, cand, eps, refit);
+    }
+    if (lane == 0) {
+      const bool accept = st.min_e <= P.thr;
+      if (accept) {
+        const int row = st.sel_pos / w2, col = st.sel_pos - (st.sel_pos / w2) * w2;
+        P.final_blk[idx] = st.sel_refit ? ((uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32)) : stb;
+        P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
+      }
+      P.done[idx] = accept ? 1u : 0u;
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------ intra --
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits until done[idx] != 0. Gives up after ~1 s, or at once when another
+// wait of this launch already gave up (sets kDevTimeout and returns false), so
+// a broken dependency can never hang the GPU: every later wait falls through.
+__device__ __forceinline__ bool wait_done(const uint32_t *done, size_t idx, uint32_t *status) {
+  if (ld_acquire(done + idx)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 0; it < (1u << 24); ++it) {
+    __nanosleep(32);
+    if (ld_acquire(done + idx)) return true;
+    if ((it & 63u) == 63u) {
+      if (ld_acquire(status) & kDevTimeout) return false;
+      if (global_ns() - t0 > 1000000000ull) break;
+    }
+  }
+  atomicOr(status, kDevTimeout);
+  return false;
+}
+
+// IntraSearch, codec/dxt_image.cpp:652-713, over blocks in raster order:
+// rows j = by .. by-2sa+1 (descending), columns i = bx+sa-1 .. bx-sa
+// (descending), skipping j == by && i >= bx; motion (i-bx+sa, j-by+2sa-1).
+// Unaccepted blocks are unique: motion (255,255), final = stb block.
+// Warps claim 32 consecutive blocks at a time from P.work and finish them in
+// order, so every block a warp waits on is owned by an earlier, running warp.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) intra_search_kernel(SearchParams P) {
+  __shared__ WarpBlock s_wb[WARPS];
+  __shared__ uint8_t s_snap5[256], s_snap6[256];
+  build_snap_tables(s_snap5, s_snap6);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpBlock &wb = s_wb[warp];
+  const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
+  const uint32_t *fin_hi = reinterpret_cast<const uint32_t *>(P.final_blk) + 1;
+  while (true) {
+    int base = 0;
+    if (lane == 0) base = (int)atomicAdd(P.work, 32u);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= nblk) break;
+    const int lim = min(32, nblk - base);
+    // blocks the inter pass already finalised need nothing here
+    const uint32_t mine = (lane < lim) ? __ldcg(P.done + base + lane) : 1u;
+    unsigned pending = __ballot_sync(kFull, mine == 0u);
+    while (pending) {
+      const int k = __ffs(pending) - 1;
+      pending &= pending - 1;
+      const int idx = base + k;
+      const int by = idx / P.bw, bx = idx - by * P.bw;
+      const int sumsq = stage_block(wb, P.rgb, P.width, bx, by, lane);
+      const uint64_t stb = P.stb[idx];
+      const uint32_t own = (uint32_t)(stb >> 32);
+      const int orig = P.orig_err[idx];
+      SelState st;
+      sel_init(st);
+      for (int pb = 0; pb < npos; pb += 32) {
+        const int pos = pb + lane;
+        const int row = pos / w2, col = pos - row * w2;
+        const int j = by - row, i = bx + P.sa - 1 - col;
+        int e = kInvalid, refit = 0;
+        uint32_t cand = 0, eps = 0;
+        if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
+          const size_t nidx = (size_t)j * P.bw + i;
+          if (wait_done(P.done, nidx, P.status)) {
+            cand = __ldcg(fin_hi + 2 * nidx);
+            e = eval_candidate(wb, s_snap5, s_snap6, cand, own, orig, sumsq, eps, refit);
+          }
+        }
+        sel_chunk(st, lane, row, e, pos, cand, eps, refit);
+      }
+      if (lane == 0) {
+        uint16_t m;
+        uint64_t blk = stb;
+        if (st.min_e <= P.thr) {
+          const int row = st.sel_pos / w2, col = st.sel_pos - (st.sel_pos / w2) * w2;
+          m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
+          if (st.sel_refit) blk = (uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32);
+        } else {
+          m = 0xFFFFu;
+        }
+        P.final_blk[idx] = blk;
+        P.motion[idx] = m;
+        __threadfence();
+        st_release(P.done + idx, 1u);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ----------------------------------------------------------------- unique --
+// The unique palette lists the stb interp of every unaccepted block in raster
+// order (codec/dxt_image.cpp:953-954). Two passes: per-tile counts, then a
+// scan of the tile counts and an ordered scatter.
+constexpr int kUniqTile = 4096;
+
+__global__ void __launch_bounds__(256) unique_count_kernel(const uint16_t *__restrict__ motion, int nblk,
+                                                           uint32_t *__restrict__ tile_counts) {
+  const int t0 = blockIdx.x * kUniqTile;
+  int c = 0;
+  for (int i = t0 + threadIdx.x; i < min(nblk, t0 + kUniqTile); i += blockDim.x) c += motion[i] == 0xFFFFu;
+  c = __reduce_add_sync(kFull, c);
+  __shared__ int s[8];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < 8; ++w) t += s[w];
+    tile_counts[blockIdx.x] = (uint32_t)t;
+  }
+}
+
+__global__ void __launch_bounds__(256) unique_scatter_kernel(const uint16_t *__restrict__ motion,
+                                                             const uint64_t *__restrict__ stb, int nblk,
+                                                             const uint32_t *__restrict__ tile_counts,
+                                                             int ntiles, uint32_t *__restrict__ unique,
+                                                             uint32_t *__restrict__ n_unique) {
+  __shared__ uint32_t s_base;
+  __shared__ uint32_t s_warp[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    uint32_t b = 0, total = 0;
+    for (int t = 0; t < ntiles; ++t) {
+      if (t < (int)blockIdx.x) b += tile_counts[t];
+      total += tile_counts[t];
+    }
+    s_base = b;
+    if (blockIdx.x == 0) *n_unique = total;
+  }
+  __syncthreads();
+  const int t0 = blockIdx.x * kUniqTile, t1 = min(nblk, t0 + kUniqTile);
+  for (int c0 = t0; c0 < t1; c0 += 256) {
+    const int i = c0 + threadIdx.x;
+    const bool u = i < t1 && motion[i] == 0xFFFFu;
+    const unsigned bal = __ballot_sync(kFull, u);
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t off = s_base;
+    for (int w = 0; w < warp; ++w) off += s_warp[w];
+    off += __popc(bal & ((1u << lane) - 1u));
+    if (u) unique[off] = (uint32_t)(stb[i] >> 32);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t t = 0;
+      for (int w = 0; w < 8; ++w) t += s_warp[w];
+      s_base += t;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace mptc

@@ -1,0 +1,114 @@
+"""Host-side mirror of the reference encoder loop over the C ABI.
+
+``Encoder`` owns an ``mptc_ctx`` for one stream resolution and exposes the
+two calls the reference makes per frame (``DXTImage(...)`` + ``Reencode``,
+codec/codec.cpp:1388-1394) on device tensors or on host arrays. Device memory
+and streams come from PyTorch; the work runs in libmptc_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import Config, FrameStats, check, lib
+
+
+@dataclass
+class FrameOutput:
+    final: np.ndarray    # u64 per block (PhysicalDXTBlock)
+    motion: np.ndarray   # u8, (x, y) per block
+    unique: np.ndarray   # u32 unique palette in raster order
+    stb: np.ndarray | None = None
+
+
+class Encoder:
+    """One MPTC stream of fixed resolution (width, height multiples of 4)."""
+
+    def __init__(self, width: int, height: int, search_area: int = 8, err_threshold: int = 5,
+                 intra_interval: int = 16):
+        self.width, self.height = width, height
+        self.bw, self.bh = width // 4, height // 4
+        self.nblk = self.bw * self.bh
+        self.intra_interval = intra_interval
+        cfg = Config(search_area, err_threshold, intra_interval, 0)
+        h = ctypes.c_void_p()
+        check(lib().mptc_ctx_create(ctypes.byref(cfg), width, height, ctypes.byref(h)))
+        self._ctx = h
+        self._intra_num = 1
+        self._next_intra = True
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            lib().mptc_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._ctx
+
+    # -- device API ---------------------------------------------------------
+    def encode_frame_device(self, rgb, prev_final, stb, final, motion, unique, n_unique, stream=None):
+        """All arguments are torch CUDA tensors (prev_final may be None)."""
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_encode_frame(self._ctx, rgb.data_ptr(),
+                                      prev_final.data_ptr() if prev_final is not None else None,
+                                      stb.data_ptr() if stb is not None else None, final.data_ptr(),
+                                      motion.data_ptr(), unique.data_ptr(), n_unique.data_ptr(), s),
+              self._ctx)
+
+    def dxt1_encode_device(self, rgb, stb, orig_err, stream=None):
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_dxt1_encode(self._ctx, rgb.data_ptr(), stb.data_ptr(),
+                                     orig_err.data_ptr() if orig_err is not None else None, s),
+              self._ctx)
+
+    def reencode_device(self, rgb, stb, orig_err, prev_final, final, motion, unique, n_unique,
+                        stream=None):
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_reencode(self._ctx, rgb.data_ptr(), stb.data_ptr(), orig_err.data_ptr(),
+                                  prev_final.data_ptr() if prev_final is not None else None,
+                                  final.data_ptr(), motion.data_ptr(), unique.data_ptr(),
+                                  n_unique.data_ptr(), s), self._ctx)
+
+    def stats(self, stream=None) -> FrameStats:
+        st = FrameStats()
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_last_frame_stats(self._ctx, ctypes.byref(st), s), self._ctx)
+        return st
+
+    # -- host API -----------------------------------------------------------
+    def encode_frame_host(self, frame: np.ndarray, is_intra: bool | None = None,
+                          want_stb: bool = False, out: FrameOutput | None = None) -> FrameOutput:
+        """One frame from host memory; successive calls form a stream. With
+        is_intra=None the reference's intra-interval schedule is applied
+        (frame 1 intra, then every intra_interval-th, codec/codec.cpp:1462-1469)."""
+        if is_intra is None:
+            is_intra = self._next_intra
+            if self._intra_num <= self.intra_interval:
+                self._next_intra = False
+                if self._intra_num == self.intra_interval:
+                    self._next_intra = True
+                    self._intra_num = 1
+                else:
+                    self._intra_num += 1
+        f = np.ascontiguousarray(frame, dtype=np.uint8)
+        assert f.shape == (self.height, self.width, 3)
+        if out is None:
+            out = FrameOutput(np.empty(self.nblk, np.uint64), np.empty(2 * self.nblk, np.uint8),
+                              np.empty(self.nblk, np.uint32),
+                              np.empty(self.nblk, np.uint64) if want_stb else None)
+        nu = ctypes.c_uint32(0)
+        check(lib().mptc_encode_frame_host(self._ctx, f.ctypes.data, int(bool(is_intra)),
+                                           out.stb.ctypes.data if out.stb is not None else None,
+                                           out.final.ctypes.data, out.motion.ctypes.data,
+                                           out.unique.ctypes.data, ctypes.byref(nu), None),
+              self._ctx)
+        return FrameOutput(out.final, out.motion, out.unique[: nu.value], out.stb)
