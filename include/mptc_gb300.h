@@ -108,6 +108,25 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
 /* Counters of the last frame reencoded on this context (synchronises `stream`). */
 mptc_status mptc_last_frame_stats(mptc_ctx *ctx, mptc_frame_stats *out, void *stream);
 
+/* Opt-in CUDA-event timing of every kernel this context launches (off by
+ * default). Timing brackets each launch with events on the launching stream. */
+typedef struct mptc_kernel_time {
+  char name[32];
+  int32_t launches;
+  double total_ms;
+} mptc_kernel_time;
+mptc_status mptc_set_kernel_timing(mptc_ctx *ctx, int32_t enable);
+/* Sums the recorded launches per kernel (synchronises on the recorded events)
+ * and clears the record. Writes up to max_entries entries and their count. */
+mptc_status mptc_kernel_times(mptc_ctx *ctx, mptc_kernel_time *out, int32_t max_entries,
+                              int32_t *n_entries);
+
+/* Scalar-ALU throughput probe: `threads` x `iters` x 32 dependent-chain-free
+ * fp32 add/int32 add pairs. Writes a checksum to *sink_dev (device int32) so
+ * nothing is optimised away; the caller times the launch. Returns the op count
+ * per launch in *ops (2 ops per pair). */
+mptc_status mptc_alu_probe(int32_t blocks, int32_t iters, int32_t *sink_dev, double *ops, void *stream);
+
 /* Human-readable text of the last error on this context (never NULL). */
 const char *mptc_last_error(const mptc_ctx *ctx);
 

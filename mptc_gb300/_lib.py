@@ -18,7 +18,8 @@ STATUS_NAMES = {0: "MPTC_OK", 1: "MPTC_EINVAL", 2: "MPTC_ENOMEM", 3: "MPTC_ETIME
 EXPORTED = [
     "mptc_ctx_create", "mptc_ctx_destroy", "mptc_dxt1_encode", "mptc_reencode",
     "mptc_encode_frame", "mptc_encode_frame_host", "mptc_last_frame_stats", "mptc_last_error",
-    "mptc_version", "mptc_built_arch",
+    "mptc_version", "mptc_built_arch", "mptc_set_kernel_timing", "mptc_kernel_times",
+    "mptc_alu_probe",
 ]
 
 
@@ -30,6 +31,11 @@ class Config(ctypes.Structure):
 class FrameStats(ctypes.Structure):
     _fields_ = [("n_inter", ctypes.c_uint32), ("n_intra", ctypes.c_uint32),
                 ("n_unique", ctypes.c_uint32), ("is_intra", ctypes.c_uint32)]
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int32),
+                ("total_ms", ctypes.c_double)]
 
 
 class MptcError(RuntimeError):
@@ -58,6 +64,10 @@ def lib() -> ctypes.CDLL:
         L.mptc_last_frame_stats.argtypes = [vp, ctypes.POINTER(FrameStats), vp]
         L.mptc_last_error.argtypes = [vp]
         L.mptc_last_error.restype = ctypes.c_char_p
+        L.mptc_set_kernel_timing.argtypes = [vp, i32]
+        L.mptc_kernel_times.argtypes = [vp, ctypes.POINTER(KernelTime), i32,
+                                        ctypes.POINTER(ctypes.c_int32)]
+        L.mptc_alu_probe.argtypes = [i32, i32, vp, ctypes.POINTER(ctypes.c_double), vp]
         L.mptc_version.restype = i32
         L.mptc_built_arch.restype = i32
         for name in EXPORTED:

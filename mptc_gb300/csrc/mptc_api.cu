@@ -7,6 +7,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/mptc_gb300.h"
 #include "dxt1_encode.cuh"
@@ -15,10 +16,6 @@
 namespace {
 
 constexpr int kSearchWarps = 8;
-
-struct Stats3 {
-  uint32_t n_inter, n_intra, n_unique;
-};
 
 }  // namespace
 
@@ -44,6 +41,15 @@ struct mptc_ctx {
   bool have_prev = false;
   uint32_t last_is_intra = 0;
   std::string err;
+  // opt-in per-kernel event timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  struct Rec {
+    int kernel;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
+  size_t ev_used = 0;
 };
 
 namespace {
@@ -97,6 +103,13 @@ mptc_status cuda_fail(mptc_ctx *ctx, cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
   } while (0)
 
+bool is_pinned(const void *p) {
+  cudaPointerAttributes a;
+  const bool ok = cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  return ok;
+}
+
 bool aligned(const void *p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
 template <typename T>
@@ -122,6 +135,55 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
   P.sa = ctx->cfg.search_area;
   P.thr = ctx->cfg.err_threshold;
   return P;
+}
+
+enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_UNIQUE, K_STATS, K_COUNT };
+const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel", "inter_search_kernel", "intra_search_kernel",
+                                     "unique_kernels", "frame_stats_kernel"};
+
+cudaEvent_t pool_event(mptc_ctx *ctx) {
+  if (ctx->ev_used == ctx->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    ctx->ev_pool.push_back(e);
+  }
+  return ctx->ev_pool[ctx->ev_used++];
+}
+
+// Brackets the launches issued in its scope with events on the launching
+// stream when the context's kernel timing is on.
+struct KernelTimer {
+  mptc_ctx *ctx;
+  int id;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr;
+  KernelTimer(mptc_ctx *c, int k, cudaStream_t st) : ctx(c), id(k), s(st) {
+    if (ctx->timing && (a = pool_event(ctx))) cudaEventRecord(a, s);
+  }
+  ~KernelTimer() {
+    if (!a) return;
+    cudaEvent_t b = pool_event(ctx);
+    if (!b) return;
+    cudaEventRecord(b, s);
+    ctx->recs.push_back({id, a, b});
+  }
+};
+
+__global__ void alu_probe_kernel(int iters, int32_t *sink) {
+  // 8 independent fp32 add chains per thread; adding a constant cannot be
+  // reassociated without fast-math, so every add is issued.
+  float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
+  float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
+  const float c = 1.0e-9f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      a0 = __fadd_rn(a0, c); a1 = __fadd_rn(a1, c); a2 = __fadd_rn(a2, c); a3 = __fadd_rn(a3, c);
+      a4 = __fadd_rn(a4, c); a5 = __fadd_rn(a5, c); a6 = __fadd_rn(a6, c); a7 = __fadd_rn(a7, c);
+    }
+  }
+  const float t = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (t == 12345.678f) *sink = (int32_t)t;  // never true; keeps the chains live
 }
 
 __global__ void frame_stats_kernel(const uint16_t *__restrict__ motion, int nblk, uint32_t *__restrict__ stats) {
@@ -210,6 +272,7 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->n_unique_dev);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
+  for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
   delete ctx;
   return MPTC_OK;
 }
@@ -223,8 +286,11 @@ mptc_status mptc_dxt1_encode(mptc_ctx *ctx, const uint8_t *rgb_dev, uint64_t *bl
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int threads = 128;
   int grid = (ctx->nblk + threads - 1) / threads;
-  mptc::dxt1_encode_kernel<<<grid, threads, 0, s>>>(rgb_dev, ctx->width, ctx->bw, ctx->nblk, blocks_dev,
-                                                     orig_err_dev);
+  {
+    KernelTimer t(ctx, K_DXT1, s);
+    mptc::dxt1_encode_kernel<<<grid, threads, 0, s>>>(rgb_dev, ctx->width, ctx->bw, ctx->nblk, blocks_dev,
+                                                       orig_err_dev);
+  }
   MPTC_CUDA(cudaGetLastError());
   return MPTC_OK;
 }
@@ -244,18 +310,28 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, 8 * sizeof(uint32_t), s));
   if (prev_final_dev) {
     int grid = (ctx->nblk + kSearchWarps - 1) / kSearchWarps;
+    KernelTimer t(ctx, K_INTER, s);
     mptc::inter_search_kernel<kSearchWarps><<<grid, kSearchWarps * 32, 0, s>>>(P);
     MPTC_CUDA(cudaGetLastError());
   } else {
     MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint32_t), s));
   }
-  mptc::intra_search_kernel<kSearchWarps><<<ctx->intra_grid, kSearchWarps * 32, 0, s>>>(P);
+  {
+    KernelTimer t(ctx, K_INTRA, s);
+    mptc::intra_search_kernel<kSearchWarps><<<ctx->intra_grid, kSearchWarps * 32, 0, s>>>(P);
+  }
   MPTC_CUDA(cudaGetLastError());
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
-  mptc::unique_count_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, ctx->nblk, ctx->tile_counts);
-  mptc::unique_scatter_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, stb_dev, ctx->nblk, ctx->tile_counts, ctx->ntiles,
-                                                         unique_dev, n_unique_dev);
-  frame_stats_kernel<<<ctx->sm_count, 256, 0, s>>>(m16, ctx->nblk, ctx->work + 2);
+  {
+    KernelTimer t(ctx, K_UNIQUE, s);
+    mptc::unique_count_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, ctx->nblk, ctx->tile_counts);
+    mptc::unique_scatter_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, stb_dev, ctx->nblk, ctx->tile_counts,
+                                                           ctx->ntiles, unique_dev, n_unique_dev);
+  }
+  {
+    KernelTimer t(ctx, K_STATS, s);
+    frame_stats_kernel<<<ctx->sm_count, 256, 0, s>>>(m16, ctx->nblk, ctx->work + 2);
+  }
   MPTC_CUDA(cudaGetLastError());
   ctx->last_is_intra = prev_final_dev ? 0u : 1u;
   return MPTC_OK;
@@ -296,10 +372,7 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t n = (size_t)ctx->nblk, in_bytes = n * 48;
   // Pinned caller buffers are copied directly; pageable ones go through staging.
-  cudaPointerAttributes attr;
-  const bool in_pinned = cudaPointerGetAttributes(&attr, rgb_host) == cudaSuccess && attr.type == cudaMemoryTypeHost;
-  cudaGetLastError();
-  if (in_pinned) {
+  if (is_pinned(rgb_host)) {
     MPTC_CUDA(cudaMemcpyAsync(ctx->rgb_dev, rgb_host, in_bytes, cudaMemcpyHostToDevice, s));
   } else {
     std::memcpy(ctx->pin_in, rgb_host, in_bytes);
@@ -310,24 +383,69 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
   mptc_status st = mptc_encode_frame(ctx, ctx->rgb_dev, prev, ctx->stb, ctx->final_dev[nxt], ctx->motion_dev,
                                      ctx->unique_dev, ctx->n_unique_dev, stream);
   if (st != MPTC_OK) return st;
+  // Outputs: pinned caller buffers receive the copies directly, pageable ones
+  // are filled from the context's pinned staging after the stream completes.
   uint8_t *o = ctx->pin_out;
-  MPTC_CUDA(cudaMemcpyAsync(o, ctx->final_dev[nxt], n * 8, cudaMemcpyDeviceToHost, s));
-  MPTC_CUDA(cudaMemcpyAsync(o + n * 8, ctx->motion_dev, n * 2, cudaMemcpyDeviceToHost, s));
-  MPTC_CUDA(cudaMemcpyAsync(o + n * 10, ctx->unique_dev, n * 4, cudaMemcpyDeviceToHost, s));
-  MPTC_CUDA(cudaMemcpyAsync(o + n * 14, ctx->n_unique_dev, 4, cudaMemcpyDeviceToHost, s));
+  const bool fin_p = is_pinned(final_host), mot_p = is_pinned(motion_host), uni_p = is_pinned(unique_host);
+  MPTC_CUDA(cudaMemcpyAsync(fin_p ? (void *)final_host : (void *)o, ctx->final_dev[nxt], n * 8,
+                            cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(mot_p ? (void *)motion_host : (void *)(o + n * 8), ctx->motion_dev, n * 2,
+                            cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(uni_p ? (void *)unique_host : (void *)(o + n * 10), ctx->unique_dev, n * 4,
+                            cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(o + n * 14, ctx->work, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(o + n * 14 + 8, ctx->n_unique_dev, 4, cudaMemcpyDeviceToHost, s));
   if (stb_host) MPTC_CUDA(cudaMemcpyAsync(stb_host, ctx->stb, n * 8, cudaMemcpyDeviceToHost, s));
-  uint32_t w[2];
-  MPTC_CUDA(cudaMemcpyAsync(w, ctx->work, sizeof(w), cudaMemcpyDeviceToHost, s));
   MPTC_CUDA(cudaStreamSynchronize(s));
+  uint32_t w[3];
+  std::memcpy(w, o + n * 14, sizeof(w));
   if (w[1] & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
-  uint32_t nu;
-  std::memcpy(&nu, o + n * 14, 4);
-  std::memcpy(final_host, o, n * 8);
-  std::memcpy(motion_host, o + n * 8, n * 2);
-  std::memcpy(unique_host, o + n * 10, (size_t)nu * 4);
+  const uint32_t nu = w[2];
+  if (!fin_p) std::memcpy(final_host, o, n * 8);
+  if (!mot_p) std::memcpy(motion_host, o + n * 8, n * 2);
+  if (!uni_p) std::memcpy(unique_host, o + n * 10, (size_t)nu * 4);
   *n_unique_host = nu;
   ctx->cur = nxt;
   ctx->have_prev = true;
+  return MPTC_OK;
+}
+
+mptc_status mptc_set_kernel_timing(mptc_ctx *ctx, int32_t enable) {
+  if (!ctx) return MPTC_EINVAL;
+  ctx->timing = enable != 0;
+  return MPTC_OK;
+}
+
+mptc_status mptc_kernel_times(mptc_ctx *ctx, mptc_kernel_time *out, int32_t max_entries, int32_t *n_entries) {
+  if (!ctx || !n_entries || (max_entries > 0 && !out)) return MPTC_EINVAL;
+  double ms[K_COUNT] = {0};
+  int cnt[K_COUNT] = {0};
+  for (const auto &r : ctx->recs) {
+    MPTC_CUDA(cudaEventSynchronize(r.b));
+    float t = 0.f;
+    MPTC_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+    ms[r.kernel] += t;
+    cnt[r.kernel] += 1;
+  }
+  ctx->recs.clear();
+  ctx->ev_used = 0;
+  int n = 0;
+  for (int k = 0; k < K_COUNT && n < max_entries; ++k) {
+    if (!cnt[k]) continue;
+    std::snprintf(out[n].name, sizeof(out[n].name), "%s", kKernelNames[k]);
+    out[n].launches = cnt[k];
+    out[n].total_ms = ms[k];
+    ++n;
+  }
+  *n_entries = n;
+  return MPTC_OK;
+}
+
+mptc_status mptc_alu_probe(int32_t blocks, int32_t iters, int32_t *sink_dev, double *ops, void *stream) {
+  if (blocks <= 0 || iters <= 0 || !sink_dev || !ops) return MPTC_EINVAL;
+  alu_probe_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(iters, sink_dev);
+  if (cudaGetLastError() != cudaSuccess) return MPTC_ECUDA;
+  *ops = (double)blocks * 256.0 * (double)iters * 32.0 * 8.0;
   return MPTC_OK;
 }
 

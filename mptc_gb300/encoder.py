@@ -12,7 +12,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import Config, FrameStats, check, lib
+from ._lib import Config, FrameStats, KernelTime, check, lib
 
 
 @dataclass
@@ -83,6 +83,16 @@ class Encoder:
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
         check(lib().mptc_last_frame_stats(self._ctx, ctypes.byref(st), s), self._ctx)
         return st
+
+    def set_kernel_timing(self, enable: bool) -> None:
+        check(lib().mptc_set_kernel_timing(self._ctx, int(enable)), self._ctx)
+
+    def kernel_times(self) -> dict:
+        """{kernel name: (launches, total ms)} since the last call."""
+        arr = (KernelTime * 16)()
+        n = ctypes.c_int32(0)
+        check(lib().mptc_kernel_times(self._ctx, arr, 16, ctypes.byref(n)), self._ctx)
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(n.value)}
 
     # -- host API -----------------------------------------------------------
     def encode_frame_host(self, frame: np.ndarray, is_intra: bool | None = None,
