@@ -54,8 +54,10 @@ struct mptc_ctx {
 
 namespace {
 
-std::once_flag g_tables_once;
-cudaError_t g_tables_err = cudaSuccess;
+// __constant__ memory is per device: the tables are uploaded once per device.
+constexpr int kMaxDevices = 64;
+std::mutex g_tables_mu;
+bool g_tables_done[kMaxDevices] = {};
 
 // stb__PrepareOptTable semantics (Include/stb_dxt.h:111-137): for every 8-bit
 // value, the (max, min) endpoint pair whose 1/3 interpolation is closest,
@@ -80,12 +82,22 @@ void build_opt_table(uint8_t table[256][2], int bits) {
   }
 }
 
-void upload_tables() {
+// Uploads the OMatch tables to the current device if it has not got them yet.
+cudaError_t ensure_tables(int device) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_tables_mu);
+  if (g_tables_done[device]) return cudaSuccess;
   static uint8_t t5[256][2], t6[256][2];
-  build_opt_table(t5, 5);
-  build_opt_table(t6, 6);
-  g_tables_err = cudaMemcpyToSymbol(mptc::c_omatch5, t5, sizeof(t5));
-  if (g_tables_err == cudaSuccess) g_tables_err = cudaMemcpyToSymbol(mptc::c_omatch6, t6, sizeof(t6));
+  static bool built = false;
+  if (!built) {
+    build_opt_table(t5, 5);
+    build_opt_table(t6, 6);
+    built = true;
+  }
+  cudaError_t e = cudaMemcpyToSymbol(mptc::c_omatch5, t5, sizeof(t5));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(mptc::c_omatch6, t6, sizeof(t6));
+  if (e == cudaSuccess) g_tables_done[device] = true;
+  return e;
 }
 
 mptc_status fail(mptc_ctx *ctx, mptc_status st, const std::string &msg) {
@@ -236,8 +248,7 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
   if (cudaGetDevice(&ctx->device) != cudaSuccess) return bad(MPTC_ECUDA);
   if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
     return bad(MPTC_ECUDA);
-  std::call_once(g_tables_once, upload_tables);
-  if (g_tables_err != cudaSuccess) return bad(MPTC_ECUDA);
+  if (ensure_tables(ctx->device) != cudaSuccess) return bad(MPTC_ECUDA);
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_search_kernel<kSearchWarps>,
                                                     kSearchWarps * 32, 0) != cudaSuccess)
