@@ -105,6 +105,37 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
                                    uint64_t *stb_host, uint64_t *final_host, uint8_t *motion_host,
                                    uint32_t *unique_host, uint32_t *n_unique_host, void *stream);
 
+/* Largest frame, in 4x4 blocks, that mptc_encode_frame_noalloc accepts
+ * (131072 blocks: 1920x1080 is 129600, 2048x1024 is 131072). */
+#define MPTC_NOALLOC_MAX_BLOCKS 131072
+
+/* mptc_encode_frame without any allocation. This entry point has no
+ * counterpart in the reference, whose encoder allocates freely.
+ *
+ * For callers that may not allocate device memory: host applications that
+ * reserve the whole device memory budget up front and forbid plugins from
+ * calling cudaMalloc, and frame loops with a latency budget that cannot absorb
+ * the allocator (cudaFree synchronises the whole device). It takes no context:
+ * the caller passes the configuration, the frame size, the input frame and
+ * every output buffer; the kernels' scratch (per-block completion flags, the
+ * stb error of each block, work counters, tile counts) lives in one
+ * file-scope device array of about 2 MiB inside the library, which every GPU
+ * that loads the library holds until the process exits.
+ *
+ * Frames larger than MPTC_NOALLOC_MAX_BLOCKS blocks are rejected with
+ * MPTC_EINVAL. The first call on a device sets that device up (looks up the
+ * scratch array's device address and uploads the stb tables); make that first
+ * call before any stream capture. All calls share the one scratch array, so
+ * calls that overlap on the GPU (on different streams, or from several host
+ * threads) race and corrupt each other's results: serialise them. Outputs and
+ * their layouts are those of mptc_encode_frame; stb_dev may be NULL. If a
+ * bounded device-side wait expired, *n_unique_dev reads 0xFFFFFFFF and the
+ * outputs are invalid. */
+mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t width, int32_t height,
+                                      const uint8_t *rgb_dev, const uint64_t *prev_final_dev,
+                                      uint64_t *stb_dev, uint64_t *final_dev, uint8_t *motion_dev,
+                                      uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream);
+
 /* Counters of the last frame reencoded on this context (synchronises `stream`). */
 mptc_status mptc_last_frame_stats(mptc_ctx *ctx, mptc_frame_stats *out, void *stream);
 

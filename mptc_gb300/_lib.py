@@ -19,8 +19,10 @@ EXPORTED = [
     "mptc_ctx_create", "mptc_ctx_destroy", "mptc_dxt1_encode", "mptc_reencode",
     "mptc_encode_frame", "mptc_encode_frame_host", "mptc_last_frame_stats", "mptc_last_error",
     "mptc_version", "mptc_built_arch", "mptc_set_kernel_timing", "mptc_kernel_times",
-    "mptc_alu_probe",
+    "mptc_alu_probe", "mptc_encode_frame_noalloc",
 ]
+
+NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
 
 
 class Config(ctypes.Structure):
@@ -68,6 +70,8 @@ def lib() -> ctypes.CDLL:
         L.mptc_kernel_times.argtypes = [vp, ctypes.POINTER(KernelTime), i32,
                                         ctypes.POINTER(ctypes.c_int32)]
         L.mptc_alu_probe.argtypes = [i32, i32, vp, ctypes.POINTER(ctypes.c_double), vp]
+        L.mptc_encode_frame_noalloc.argtypes = [ctypes.POINTER(Config), i32, i32, vp, vp, vp, vp, vp,
+                                                vp, u32p, vp]
         L.mptc_version.restype = i32
         L.mptc_built_arch.restype = i32
         for name in EXPORTED:

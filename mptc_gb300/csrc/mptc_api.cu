@@ -461,3 +461,120 @@ mptc_status mptc_alu_probe(int32_t blocks, int32_t iters, int32_t *sink_dev, dou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// mptc_encode_frame_noalloc: the encode pipeline with its scratch in a
+// file-scope device array instead of context allocations.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNaMaxBlocks = MPTC_NOALLOC_MAX_BLOCKS;
+constexpr size_t kNaTiles = (kNaMaxBlocks + mptc::kUniqTile - 1) / mptc::kUniqTile;
+// byte offsets inside the scratch array (each 256-byte aligned)
+constexpr size_t kNaDone = 0;                                   // u32 per block
+constexpr size_t kNaStb = kNaDone + kNaMaxBlocks * 4;           // u64 per block
+constexpr size_t kNaOrig = kNaStb + kNaMaxBlocks * 8;           // i32 per block
+constexpr size_t kNaWork = kNaOrig + kNaMaxBlocks * 4;          // u32[8]
+constexpr size_t kNaTileCounts = kNaWork + 256;                 // u32 per tile
+constexpr size_t kNaBytes = kNaTileCounts + ((kNaTiles * 4 + 255) / 256) * 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+struct NoallocDevice {
+  bool ready = false;
+  unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+  int sm_count = 0;
+  int intra_grid = 0;
+};
+std::mutex g_na_mu;
+NoallocDevice g_na_dev[kMaxDevices];
+
+// Sets DEVICE up once: device address of the scratch array (host code may not
+// use the symbol itself as a pointer), stb tables, launch geometry.
+mptc_status noalloc_setup(int device, NoallocDevice **out) {
+  if (device < 0 || device >= kMaxDevices) return MPTC_ECUDA;
+  std::lock_guard<std::mutex> lock(g_na_mu);
+  NoallocDevice &d = g_na_dev[device];
+  if (!d.ready) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return MPTC_ECUDA;
+    if (ensure_tables(device) != cudaSuccess) return MPTC_ECUDA;
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return MPTC_ECUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_search_kernel<kSearchWarps>,
+                                                      kSearchWarps * 32, 0) != cudaSuccess)
+      return MPTC_ECUDA;
+    d.scratch = static_cast<unsigned char *>(p);
+    d.sm_count = sms;
+    d.intra_grid = sms * (per_sm > 0 ? per_sm : 1);
+    d.ready = true;
+  }
+  *out = &d;
+  return MPTC_OK;
+}
+
+// After the unique palette: flags an expired device-side wait through the
+// unique count, since this entry point has no context to report it on.
+__global__ void noalloc_status_kernel(const uint32_t *__restrict__ work, uint32_t *__restrict__ n_unique) {
+  if (threadIdx.x == 0 && (work[1] & mptc::kDevTimeout)) *n_unique = 0xFFFFFFFFu;
+}
+
+}  // namespace
+
+extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t width, int32_t height,
+                                                 const uint8_t *rgb_dev, const uint64_t *prev_final_dev,
+                                                 uint64_t *stb_dev, uint64_t *final_dev, uint8_t *motion_dev,
+                                                 uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream) {
+  if (!cfg || width <= 0 || height <= 0 || (width & 3) || (height & 3)) return MPTC_EINVAL;
+  if (cfg->search_area < 1 || cfg->search_area > 63 || cfg->err_threshold == 0x7fffffff) return MPTC_EINVAL;
+  const size_t nblk = (size_t)(width / 4) * (size_t)(height / 4);
+  if (nblk > kNaMaxBlocks) return MPTC_EINVAL;  // beyond the fixed scratch
+  if (!rgb_dev || !final_dev || !motion_dev || !unique_dev || !n_unique_dev) return MPTC_EINVAL;
+  if (!aligned(rgb_dev, 16) || !aligned(final_dev, 8) || !aligned(motion_dev, 2) || !aligned(unique_dev, 4) ||
+      (stb_dev && !aligned(stb_dev, 8)) || (prev_final_dev && !aligned(prev_final_dev, 8)) ||
+      prev_final_dev == final_dev)
+    return MPTC_EINVAL;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return MPTC_ECUDA;
+  NoallocDevice *d = nullptr;
+  mptc_status st = noalloc_setup(device, &d);
+  if (st != MPTC_OK) return st;
+
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  uint32_t *done = reinterpret_cast<uint32_t *>(d->scratch + kNaDone);
+  uint64_t *stb = stb_dev ? stb_dev : reinterpret_cast<uint64_t *>(d->scratch + kNaStb);
+  int32_t *orig = reinterpret_cast<int32_t *>(d->scratch + kNaOrig);
+  uint32_t *work = reinterpret_cast<uint32_t *>(d->scratch + kNaWork);
+  uint32_t *tiles = reinterpret_cast<uint32_t *>(d->scratch + kNaTileCounts);
+  const int bw = width / 4, bh = height / 4, n = (int)nblk;
+  const int ntiles = (n + mptc::kUniqTile - 1) / mptc::kUniqTile;
+
+  // The scratch keeps the previous call's contents: clear the counters, and
+  // the completion flags when no inter pass will write them.
+  if (cudaMemsetAsync(work, 0, 8 * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
+  if (!prev_final_dev && cudaMemsetAsync(done, 0, nblk * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
+  mptc::dxt1_encode_kernel<<<(n + 127) / 128, 128, 0, s>>>(rgb_dev, width, bw, n, stb, orig);
+  mptc::SearchParams P;
+  P.rgb = rgb_dev;
+  P.stb = stb;
+  P.orig_err = orig;
+  P.prev = prev_final_dev;
+  P.final_blk = final_dev;
+  P.motion = reinterpret_cast<uint16_t *>(motion_dev);
+  P.done = done;
+  P.work = work;
+  P.status = work + 1;
+  P.width = width;
+  P.bw = bw;
+  P.bh = bh;
+  P.sa = cfg->search_area;
+  P.thr = cfg->err_threshold;
+  if (prev_final_dev)
+    mptc::inter_search_kernel<kSearchWarps><<<(n + kSearchWarps - 1) / kSearchWarps, kSearchWarps * 32, 0, s>>>(P);
+  mptc::intra_search_kernel<kSearchWarps><<<d->intra_grid, kSearchWarps * 32, 0, s>>>(P);
+  const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
+  mptc::unique_count_kernel<<<ntiles, 256, 0, s>>>(m16, n, tiles);
+  mptc::unique_scatter_kernel<<<ntiles, 256, 0, s>>>(m16, stb, n, tiles, ntiles, unique_dev, n_unique_dev);
+  noalloc_status_kernel<<<1, 32, 0, s>>>(work, n_unique_dev);
+  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
+}
