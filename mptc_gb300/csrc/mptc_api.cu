@@ -15,7 +15,8 @@
 
 namespace {
 
-constexpr int kSearchWarps = 8;
+constexpr int kSearchWarps = 8;     // inter search: warps per CTA, one block per warp
+constexpr int kIntraThreads = 256;  // intra search: one block per CTA
 
 }  // namespace
 
@@ -25,7 +26,9 @@ struct mptc_ctx {
   int device = 0, sm_count = 0, intra_grid = 0;
   // device scratch
   uint32_t *done = nullptr;        // per block
-  uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats
+  uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count
+  uint32_t *order = nullptr;       // blocks in wavefront order
+  uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
   uint32_t *tile_counts = nullptr; // per unique tile
   uint64_t *stb = nullptr;         // stb blocks (encode_frame / host path)
   int32_t *orig_err = nullptr;
@@ -250,17 +253,20 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
     return bad(MPTC_ECUDA);
   if (ensure_tables(ctx->device) != cudaSuccess) return bad(MPTC_ECUDA);
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_search_kernel<kSearchWarps>,
-                                                    kSearchWarps * 32, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_search_kernel<kIntraThreads>,
+                                                    kIntraThreads, 0) != cudaSuccess)
     return bad(MPTC_ECUDA);
   ctx->intra_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
   const size_t n = (size_t)ctx->nblk;
   if (dalloc(&ctx->done, n) || dalloc(&ctx->work, 8) || dalloc(&ctx->tile_counts, (size_t)ctx->ntiles) ||
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
       dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
-      dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1))
+      dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1) || dalloc(&ctx->order, n) ||
+      dalloc(&ctx->pending, n))
     return bad(MPTC_ENOMEM);
   if (cudaMemset(ctx->work, 0, 8 * sizeof(uint32_t)) != cudaSuccess) return bad(MPTC_ECUDA);
+  mptc::wavefront_order_kernel<<<(ctx->nblk + 255) / 256, 256>>>(ctx->bw, ctx->bh, cfg->search_area, ctx->order);
+  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return bad(MPTC_ECUDA);
   if (cudaMallocHost(reinterpret_cast<void **>(&ctx->pin_in), n * 48) != cudaSuccess ||
       cudaMallocHost(reinterpret_cast<void **>(&ctx->pin_out), n * (8 + 2 + 4) + 64) != cudaSuccess)
     return bad(MPTC_ENOMEM);
@@ -281,6 +287,8 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->motion_dev);
   cudaFree(ctx->unique_dev);
   cudaFree(ctx->n_unique_dev);
+  cudaFree(ctx->order);
+  cudaFree(ctx->pending);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -327,9 +335,20 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   } else {
     MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint32_t), s));
   }
+  if (prev_final_dev) {
+    // pending = blocks the inter pass left open, in wavefront order
+    mptc::pending_count_kernel<<<ctx->ntiles, 256, 0, s>>>(ctx->order, ctx->done, ctx->nblk, ctx->tile_counts);
+    mptc::pending_scatter_kernel<<<ctx->ntiles, 256, 0, s>>>(ctx->order, ctx->done, ctx->nblk, ctx->tile_counts,
+                                                            ctx->ntiles, ctx->pending, ctx->work + 5);
+  }
   {
     KernelTimer t(ctx, K_INTRA, s);
-    mptc::intra_search_kernel<kSearchWarps><<<ctx->intra_grid, kSearchWarps * 32, 0, s>>>(P);
+    if (prev_final_dev)
+      mptc::intra_search_kernel<kIntraThreads><<<ctx->intra_grid, kIntraThreads, 0, s>>>(P, ctx->pending,
+                                                                                        ctx->work + 5, -1);
+    else
+      mptc::intra_search_kernel<kIntraThreads><<<ctx->intra_grid, kIntraThreads, 0, s>>>(P, ctx->order, nullptr,
+                                                                                        ctx->nblk);
   }
   MPTC_CUDA(cudaGetLastError());
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
@@ -474,7 +493,9 @@ constexpr size_t kNaTiles = (kNaMaxBlocks + mptc::kUniqTile - 1) / mptc::kUniqTi
 constexpr size_t kNaDone = 0;                                   // u32 per block
 constexpr size_t kNaStb = kNaDone + kNaMaxBlocks * 4;           // u64 per block
 constexpr size_t kNaOrig = kNaStb + kNaMaxBlocks * 8;           // i32 per block
-constexpr size_t kNaWork = kNaOrig + kNaMaxBlocks * 4;          // u32[8]
+constexpr size_t kNaOrder = kNaOrig + kNaMaxBlocks * 4;         // u32 per block
+constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
+constexpr size_t kNaWork = kNaPending + kNaMaxBlocks * 4;       // u32[8]
 constexpr size_t kNaTileCounts = kNaWork + 256;                 // u32 per tile
 constexpr size_t kNaBytes = kNaTileCounts + ((kNaTiles * 4 + 255) / 256) * 256;
 
@@ -501,8 +522,8 @@ mptc_status noalloc_setup(int device, NoallocDevice **out) {
     if (ensure_tables(device) != cudaSuccess) return MPTC_ECUDA;
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return MPTC_ECUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_search_kernel<kSearchWarps>,
-                                                      kSearchWarps * 32, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_search_kernel<kIntraThreads>,
+                                                      kIntraThreads, 0) != cudaSuccess)
       return MPTC_ECUDA;
     d.scratch = static_cast<unsigned char *>(p);
     d.sm_count = sms;
@@ -546,6 +567,8 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   int32_t *orig = reinterpret_cast<int32_t *>(d->scratch + kNaOrig);
   uint32_t *work = reinterpret_cast<uint32_t *>(d->scratch + kNaWork);
   uint32_t *tiles = reinterpret_cast<uint32_t *>(d->scratch + kNaTileCounts);
+  uint32_t *order = reinterpret_cast<uint32_t *>(d->scratch + kNaOrder);
+  uint32_t *pend = reinterpret_cast<uint32_t *>(d->scratch + kNaPending);
   const int bw = width / 4, bh = height / 4, n = (int)nblk;
   const int ntiles = (n + mptc::kUniqTile - 1) / mptc::kUniqTile;
 
@@ -553,6 +576,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   // the completion flags when no inter pass will write them.
   if (cudaMemsetAsync(work, 0, 8 * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
   if (!prev_final_dev && cudaMemsetAsync(done, 0, nblk * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
+  mptc::wavefront_order_kernel<<<(n + 255) / 256, 256, 0, s>>>(bw, bh, cfg->search_area, order);
   mptc::dxt1_encode_kernel<<<(n + 127) / 128, 128, 0, s>>>(rgb_dev, width, bw, n, stb, orig);
   mptc::SearchParams P;
   P.rgb = rgb_dev;
@@ -569,9 +593,14 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   P.bh = bh;
   P.sa = cfg->search_area;
   P.thr = cfg->err_threshold;
-  if (prev_final_dev)
+  if (prev_final_dev) {
     mptc::inter_search_kernel<kSearchWarps><<<(n + kSearchWarps - 1) / kSearchWarps, kSearchWarps * 32, 0, s>>>(P);
-  mptc::intra_search_kernel<kSearchWarps><<<d->intra_grid, kSearchWarps * 32, 0, s>>>(P);
+    mptc::pending_count_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles);
+    mptc::pending_scatter_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles, ntiles, pend, work + 5);
+    mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, pend, work + 5, -1);
+  } else {
+    mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, order, nullptr, n);
+  }
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
   mptc::unique_count_kernel<<<ntiles, 256, 0, s>>>(m16, n, tiles);
   mptc::unique_scatter_kernel<<<ntiles, 256, 0, s>>>(m16, stb, n, tiles, ntiles, unique_dev, n_unique_dev);

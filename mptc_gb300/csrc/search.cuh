@@ -326,74 +326,252 @@ __device__ __forceinline__ bool wait_done(const uint32_t *done, size_t idx, uint
   return false;
 }
 
-// IntraSearch, codec/dxt_image.cpp:652-713, over blocks in raster order:
-// rows j = by .. by-2sa+1 (descending), columns i = bx+sa-1 .. bx-sa
-// (descending), skipping j == by && i >= bx; motion (i-bx+sa, j-by+2sa-1).
-// Unaccepted blocks are unique: motion (255,255), final = stb block.
-// Warps claim 32 consecutive blocks at a time from P.work and finish them in
-// order, so every block a warp waits on is owned by an earlier, running warp.
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) intra_search_kernel(SearchParams P) {
-  __shared__ WarpBlock s_wb[WARPS];
-  __shared__ uint8_t s_snap5[256], s_snap6[256];
-  build_snap_tables(s_snap5, s_snap6);
+// Wavefront order of the intra dataflow. Block (x, y) reads, in this frame,
+// only blocks of rows y-2sa+1 .. y-1 with columns up to x+sa-1 and blocks of
+// row y left of x; with t = x + sa*y every such block has a smaller t. Blocks
+// are therefore ranked by (t, y): order[rank] = block index. Blocks of equal t
+// never read each other.
+__global__ void __launch_bounds__(256) wavefront_order_kernel(int bw, int bh, int sa, uint32_t *__restrict__ order) {
+  const int n = bw * bh;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int y = idx / bw, x = idx - y * bw;
+    const long long t = (long long)x + (long long)sa * y;
+    long long rank = 0;
+    for (int yy = 0; yy < bh; ++yy) {  // blocks with t' < t: x' < t - sa*y'
+      const long long c = t - (long long)sa * yy;
+      if (c <= 0) break;
+      rank += c < bw ? c : bw;
+    }
+    for (int yy = 0; yy < y; ++yy) {  // blocks with t' == t and y' < y
+      const long long xp = t - (long long)sa * yy;
+      rank += (xp >= 0 && xp < bw);
+    }
+    order[rank] = (uint32_t)idx;
+  }
+}
+
+// Block-wide reductions for the intra CTA (THREADS/32 warps). `buf` holds two
+// alternating rows of per-warp partials so one barrier per reduction suffices.
+template <int THREADS>
+struct CtaReduce {
+  int *buf;  // [2][THREADS/32]
+  int phase;
+  __device__ __forceinline__ int min(int v) {
+    const int w = __reduce_min_sync(kFull, v);
+    int *b = buf + phase * (THREADS / 32);
+    phase ^= 1;
+    if ((threadIdx.x & 31) == 0) b[threadIdx.x >> 5] = w;
+    __syncthreads();
+    int r = b[0];
+#pragma unroll
+    for (int k = 1; k < THREADS / 32; ++k) r = r < b[k] ? r : b[k];
+    return r;
+  }
+  __device__ __forceinline__ int max(int v) { return -min(-v); }
+};
+
+// Selection state shared by the CTA (written by one thread between barriers).
+struct CtaSel {
+  int min_e, broken_row, sel_pos, sel_refit;
+  uint32_t sel_cand, sel_eps;
+};
+
+// The selection rule of the reference loop (as in sel_chunk) over one round
+// of THREADS consecutive scan positions, thread k holding position base + k.
+template <int THREADS>
+__device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red, int row, int e, int pos,
+                                              uint32_t cand, uint32_t eps, int refit) {
+  const int tid = threadIdx.x;
+  const int min_e = s.min_e, broken = s.broken_row;
+  bool active = (e != kInvalid) && (row != broken);
+  int first = 0x7fffffff;
+  if (min_e > 0) {
+    first = red.min(active && e <= 0 ? tid : 0x7fffffff);
+    const bool pre = active && tid < first;  // all positive here
+    const int m = red.min(pre ? e : kInvalid);
+    if (m < min_e) {
+      const int who = red.min(pre && e == m ? tid : 0x7fffffff);
+      if (tid == who) {
+        s.min_e = m;
+        s.sel_pos = pos;
+        s.sel_cand = cand;
+        s.sel_eps = eps;
+        s.sel_refit = refit;
+      }
+    }
+    if (first != 0x7fffffff) {
+      __syncthreads();  // the update above lands before the first-e<=0 one
+      if (tid == first) {
+        s.min_e = 0;
+        s.sel_pos = pos;
+        s.sel_cand = cand;
+        s.sel_eps = eps;
+        s.sel_refit = refit;
+        s.broken_row = row;
+      }
+      __syncthreads();
+      active = active && tid > first && row != s.broken_row;
+    } else {
+      active = false;  // min stays positive: no position of this round is <= 0
+    }
+  }
+  if (min_e > 0 && first == 0x7fffffff) {
+    __syncthreads();
+    return;
+  }
+  // min is 0: the first err_diff < 0 of the last row that has one wins.
+  const bool neg = active && e < 0;
+  const int key = red.max(neg ? ((row << 16) | (0xFFFF - tid)) : -1);
+  if (key >= 0 && tid == 0xFFFF - (key & 0xFFFF)) {
+    s.sel_pos = pos;
+    s.sel_cand = cand;
+    s.sel_eps = eps;
+    s.sel_refit = refit;
+    s.broken_row = row;
+  }
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpBlock &wb = s_wb[warp];
-  const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
+}
+
+// IntraSearch, codec/dxt_image.cpp:652-713, as a dataflow over the blocks
+// still pending after the inter pass, in wavefront order: rows j = by ..
+// by-2sa+1 (descending), columns i = bx+sa-1 .. bx-sa (descending), skipping
+// j == by && i >= bx; motion (i-bx+sa, j-by+2sa-1). Unaccepted blocks are
+// unique: motion (255,255), final = stb block.
+// One CTA per block, one window position per thread and round; CTAs claim
+// pending blocks one at a time from P.work, so every block a CTA waits on was
+// claimed earlier by a running CTA and the dataflow cannot deadlock.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, const uint32_t *__restrict__ pending,
+                                                               const uint32_t *__restrict__ n_pending_dev,
+                                                               int n_pending_host) {
+  __shared__ WarpBlock s_wb;
+  __shared__ uint8_t s_snap5[256], s_snap6[256];
+  __shared__ int s_red[2 * (THREADS / 32)];
+  __shared__ CtaSel s_sel;
+  __shared__ int s_claim, s_sumsq;
+  build_snap_tables(s_snap5, s_snap6);
+  CtaReduce<THREADS> red{s_red, 0};
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int n_pend = n_pending_host >= 0 ? n_pending_host : (int)__ldcg(n_pending_dev);
+  const int w2 = 2 * P.sa, npos = w2 * w2;
   const uint32_t *fin_hi = reinterpret_cast<const uint32_t *>(P.final_blk) + 1;
   while (true) {
-    int base = 0;
-    if (lane == 0) base = (int)atomicAdd(P.work, 32u);
-    base = __shfl_sync(kFull, base, 0);
-    if (base >= nblk) break;
-    const int lim = min(32, nblk - base);
-    // blocks the inter pass already finalised need nothing here
-    const uint32_t mine = (lane < lim) ? __ldcg(P.done + base + lane) : 1u;
-    unsigned pending = __ballot_sync(kFull, mine == 0u);
-    while (pending) {
-      const int k = __ffs(pending) - 1;
-      pending &= pending - 1;
-      const int idx = base + k;
-      const int by = idx / P.bw, bx = idx - by * P.bw;
-      const int sumsq = stage_block(wb, P.rgb, P.width, bx, by, lane);
-      const uint64_t stb = P.stb[idx];
-      const uint32_t own = (uint32_t)(stb >> 32);
-      const int orig = P.orig_err[idx];
-      SelState st;
-      sel_init(st);
-      for (int pb = 0; pb < npos; pb += 32) {
-        const int pos = pb + lane;
-        const int row = pos / w2, col = pos - row * w2;
-        const int j = by - row, i = bx + P.sa - 1 - col;
-        int e = kInvalid, refit = 0;
-        uint32_t cand = 0, eps = 0;
-        if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
-          const size_t nidx = (size_t)j * P.bw + i;
-          if (wait_done(P.done, nidx, P.status)) {
-            cand = __ldcg(fin_hi + 2 * nidx);
-            e = eval_candidate(wb, s_snap5, s_snap6, cand, own, orig, sumsq, eps, refit);
-          }
-        }
-        sel_chunk(st, lane, row, e, pos, cand, eps, refit);
+    if (tid == 0) s_claim = (int)atomicAdd(P.work, 1u);
+    __syncthreads();
+    const int k = s_claim;
+    if (k >= n_pend) break;
+    const int idx = (int)__ldcg(pending + k);
+    const int by = idx / P.bw, bx = idx - by * P.bw;
+    if (tid < 32) {
+      const int sq = stage_block(s_wb, P.rgb, P.width, bx, by, lane);
+      if (tid == 0) {
+        s_sumsq = sq;
+        s_sel.min_e = kInvalid;
+        s_sel.broken_row = -1;
+        s_sel.sel_pos = -1;
+        s_sel.sel_cand = 0;
+        s_sel.sel_eps = 0;
+        s_sel.sel_refit = 0;
       }
-      if (lane == 0) {
-        uint16_t m;
-        uint64_t blk = stb;
-        if (st.min_e <= P.thr) {
-          const int row = st.sel_pos / w2, col = st.sel_pos - (st.sel_pos / w2) * w2;
-          m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
-          if (st.sel_refit) blk = (uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32);
-        } else {
-          m = 0xFFFFu;
-        }
-        P.final_blk[idx] = blk;
-        P.motion[idx] = m;
-        __threadfence();
-        st_release(P.done + idx, 1u);
-      }
-      __syncwarp();
     }
+    __syncthreads();
+    const uint64_t stb = __ldg(P.stb + idx);
+    const uint32_t own = (uint32_t)(stb >> 32);
+    const int orig = __ldg(P.orig_err + idx);
+    const int sumsq = s_sumsq;
+    for (int base = 0; base < npos; base += THREADS) {
+      const int pos = base + tid;
+      const int row = pos / w2, col = pos - row * w2;
+      const int j = by - row, i = bx + P.sa - 1 - col;
+      int e = kInvalid, refit = 0;
+      uint32_t cand = 0, eps = 0;
+      if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
+        const size_t nidx = (size_t)j * P.bw + i;
+        if (wait_done(P.done, nidx, P.status)) {
+          cand = __ldcg(fin_hi + 2 * nidx);
+          e = eval_candidate(s_wb, s_snap5, s_snap6, cand, own, orig, sumsq, eps, refit);
+        }
+      }
+      cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
+    }
+    if (tid == 0) {
+      uint16_t m;
+      uint64_t blk = stb;
+      if (s_sel.min_e <= P.thr) {
+        const int row = s_sel.sel_pos / w2, col = s_sel.sel_pos - (s_sel.sel_pos / w2) * w2;
+        m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
+        if (s_sel.sel_refit) blk = (uint64_t)s_sel.sel_eps | ((uint64_t)s_sel.sel_cand << 32);
+      } else {
+        m = 0xFFFFu;
+      }
+      P.final_blk[idx] = blk;
+      P.motion[idx] = m;
+      __threadfence();
+      st_release(P.done + idx, 1u);
+    }
+    __syncthreads();
+  }
+}
+
+// Order-preserving compaction of the pending blocks (done == 0) of the
+// wavefront order: per-tile counts, then a scan of the counts and an ordered
+// scatter, as for the unique palette below.
+constexpr int kPendTile = 4096;
+
+__global__ void __launch_bounds__(256) pending_count_kernel(const uint32_t *__restrict__ order,
+                                                            const uint32_t *__restrict__ done, int n,
+                                                            uint32_t *__restrict__ tile_counts) {
+  const int t0 = blockIdx.x * kPendTile;
+  int c = 0;
+  for (int i = t0 + threadIdx.x; i < min(n, t0 + kPendTile); i += blockDim.x) c += __ldg(done + order[i]) == 0u;
+  c = __reduce_add_sync(kFull, c);
+  __shared__ int s[8];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < 8; ++w) t += s[w];
+    tile_counts[blockIdx.x] = (uint32_t)t;
+  }
+}
+
+__global__ void __launch_bounds__(256) pending_scatter_kernel(const uint32_t *__restrict__ order,
+                                                              const uint32_t *__restrict__ done, int n,
+                                                              const uint32_t *__restrict__ tile_counts, int ntiles,
+                                                              uint32_t *__restrict__ pending,
+                                                              uint32_t *__restrict__ n_pending) {
+  __shared__ uint32_t s_base;
+  __shared__ uint32_t s_warp[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    uint32_t b = 0, total = 0;
+    for (int t = 0; t < ntiles; ++t) {
+      if (t < (int)blockIdx.x) b += tile_counts[t];
+      total += tile_counts[t];
+    }
+    s_base = b;
+    if (blockIdx.x == 0) *n_pending = total;
+  }
+  __syncthreads();
+  const int t0 = blockIdx.x * kPendTile, t1 = min(n, t0 + kPendTile);
+  for (int c0 = t0; c0 < t1; c0 += 256) {
+    const int i = c0 + threadIdx.x;
+    const uint32_t blk = i < t1 ? order[i] : 0u;
+    const bool u = i < t1 && __ldg(done + blk) == 0u;
+    const unsigned bal = __ballot_sync(kFull, u);
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t off = s_base;
+    for (int w = 0; w < warp; ++w) off += s_warp[w];
+    off += __popc(bal & ((1u << lane) - 1u));
+    if (u) pending[off] = blk;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t t = 0;
+      for (int w = 0; w < 8; ++w) t += s_warp[w];
+      s_base += t;
+    }
+    __syncthreads();
   }
 }
 
