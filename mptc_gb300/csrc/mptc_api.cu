@@ -29,6 +29,7 @@ struct mptc_ctx {
   uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count
   uint32_t *order = nullptr;       // blocks in wavefront order
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
+  float4 *wdesc = nullptr;         // refit weight sums of the previous frame's blocks
   uint32_t *tile_counts = nullptr; // per unique tile
   uint64_t *stb = nullptr;         // stb blocks (encode_frame / host path)
   int32_t *orig_err = nullptr;
@@ -136,6 +137,7 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
                                const uint64_t *prev, uint64_t *fin, uint8_t *motion) {
   mptc::SearchParams P;
   P.rgb = rgb;
+  P.wdesc = ctx->wdesc;
   P.stb = stb;
   P.orig_err = orig;
   P.prev = prev;
@@ -262,7 +264,7 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
       dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
       dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1) || dalloc(&ctx->order, n) ||
-      dalloc(&ctx->pending, n))
+      dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n))
     return bad(MPTC_ENOMEM);
   if (cudaMemset(ctx->work, 0, 8 * sizeof(uint32_t)) != cudaSuccess) return bad(MPTC_ECUDA);
   mptc::wavefront_order_kernel<<<(ctx->nblk + 255) / 256, 256>>>(ctx->bw, ctx->bh, cfg->search_area, ctx->order);
@@ -289,6 +291,7 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->n_unique_dev);
   cudaFree(ctx->order);
   cudaFree(ctx->pending);
+  cudaFree(ctx->wdesc);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -330,6 +333,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   if (prev_final_dev) {
     int grid = (ctx->nblk + kSearchWarps - 1) / kSearchWarps;
     KernelTimer t(ctx, K_INTER, s);
+    mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
     mptc::inter_search_kernel<kSearchWarps><<<grid, kSearchWarps * 32, 0, s>>>(P);
     MPTC_CUDA(cudaGetLastError());
   } else {
@@ -495,7 +499,8 @@ constexpr size_t kNaStb = kNaDone + kNaMaxBlocks * 4;           // u64 per block
 constexpr size_t kNaOrig = kNaStb + kNaMaxBlocks * 8;           // i32 per block
 constexpr size_t kNaOrder = kNaOrig + kNaMaxBlocks * 4;         // u32 per block
 constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
-constexpr size_t kNaWork = kNaPending + kNaMaxBlocks * 4;       // u32[8]
+constexpr size_t kNaWdesc = kNaPending + kNaMaxBlocks * 4;      // float4 per block
+constexpr size_t kNaWork = kNaWdesc + kNaMaxBlocks * 16;        // u32[8]
 constexpr size_t kNaTileCounts = kNaWork + 256;                 // u32 per tile
 constexpr size_t kNaBytes = kNaTileCounts + ((kNaTiles * 4 + 255) / 256) * 256;
 
@@ -569,6 +574,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   uint32_t *tiles = reinterpret_cast<uint32_t *>(d->scratch + kNaTileCounts);
   uint32_t *order = reinterpret_cast<uint32_t *>(d->scratch + kNaOrder);
   uint32_t *pend = reinterpret_cast<uint32_t *>(d->scratch + kNaPending);
+  float4 *wdesc = reinterpret_cast<float4 *>(d->scratch + kNaWdesc);
   const int bw = width / 4, bh = height / 4, n = (int)nblk;
   const int ntiles = (n + mptc::kUniqTile - 1) / mptc::kUniqTile;
 
@@ -580,6 +586,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   mptc::dxt1_encode_kernel<<<(n + 127) / 128, 128, 0, s>>>(rgb_dev, width, bw, n, stb, orig);
   mptc::SearchParams P;
   P.rgb = rgb_dev;
+  P.wdesc = wdesc;
   P.stb = stb;
   P.orig_err = orig;
   P.prev = prev_final_dev;
@@ -594,6 +601,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   P.sa = cfg->search_area;
   P.thr = cfg->err_threshold;
   if (prev_final_dev) {
+    mptc::weight_desc_kernel<<<(n + 255) / 256, 256, 0, s>>>(prev_final_dev, n, wdesc);
     mptc::inter_search_kernel<kSearchWarps><<<(n + kSearchWarps - 1) / kSearchWarps, kSearchWarps * 32, 0, s>>>(P);
     mptc::pending_count_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles);
     mptc::pending_scatter_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles, ntiles, pend, work + 5);

@@ -30,12 +30,23 @@ constexpr int kInvalid = 0x7fffffff;  // invalid candidate / no selection (INT_M
 // Device status bits (OR-ed into the context's status word).
 constexpr uint32_t kDevTimeout = 1u;
 
-// Per-warp staging of the block being searched.
-struct __align__(16) WarpBlock {
-  float4 p[16];   // pixel r, g, b as float
-  float4 q[16];   // fl(px * fl(1/3)) per channel
-  float4 q2[16];  // fl(px * fl(2/3)) = 2 * q (exact)
-  uint32_t pk[16];  // packed r | g<<8 | b<<16 for the integer error
+// Staging of the block being searched (one per warp in the inter search, one
+// per CTA in the intra search).
+//
+// The refit accumulates, per pixel i and channel c, ax += px*a and bx += px*b
+// with (a, b) = ((3-order)/3, order/3), order = {0,3,1,2}[index]. For the four
+// index values the products are exactly (px, 0), (0, px), (2q, q), (q, 2q)
+// with q = fl(px * fl(1/3)) (fl(2/3) = 2 fl(1/3), and doubling is exact), so
+// the block keeps them as a table ab[i][index] = {A.xyz, B.xyz} and a
+// candidate's refit becomes one lookup and six adds per pixel.
+struct __align__(16) BlockTab {
+  float4 ab[16][4][2];  // [pixel][index][0] = (A_r, A_g, A_b, 0), [1] = (B_r, B_g, B_b, 0)
+  uint32_t pg[3][4];    // channel c bytes of pixels 4g .. 4g+3 (for dp4a)
+};
+
+// Per-candidate weight sums of the refit (they depend on the index word only).
+struct WeightSums {
+  float asq, bsq, ab, f;  // f = 1 / (asq*bsq - ab*ab)
 };
 
 // Selection state of the reference's candidate loop (warp-uniform).
@@ -121,11 +132,12 @@ __device__ __forceinline__ void build_snap_tables(uint8_t *snap5, uint8_t *snap6
   }
 }
 
-// Stages block (bx, by) for the warp: pixels, their fl(px/3) products and the
-// block's sum of squares.
-__device__ __forceinline__ int stage_block(WarpBlock &wb, const uint8_t *__restrict__ rgb, int width,
-                                           int bx, int by, int lane) {
+// Stages block (bx, by) into `t` with the 32 lanes of one warp and returns
+// the block's sum of squared pixel values (all lanes).
+__device__ __forceinline__ int stage_block(BlockTab &t, const uint8_t *__restrict__ rgb, int width, int bx, int by,
+                                           int lane) {
   int sq = 0;
+  uint32_t pk = 0;
   if (lane < 16) {
     const int r = lane >> 2, c = lane & 3;
     const uint8_t *p = rgb + ((size_t)(4 * by + r) * width + 4 * bx + c) * 3;
@@ -133,14 +145,68 @@ __device__ __forceinline__ int stage_block(WarpBlock &wb, const uint8_t *__restr
     const float third = __fdiv_rn(1.0f, 3.0f);
     const float fr = __uint2float_rn(R), fg = __uint2float_rn(G), fb = __uint2float_rn(B);
     const float qr = __fmul_rn(fr, third), qg = __fmul_rn(fg, third), qb = __fmul_rn(fb, third);
-    wb.p[lane] = make_float4(fr, fg, fb, 0.0f);
-    wb.q[lane] = make_float4(qr, qg, qb, 0.0f);
-    wb.q2[lane] = make_float4(__fadd_rn(qr, qr), __fadd_rn(qg, qg), __fadd_rn(qb, qb), 0.0f);
-    wb.pk[lane] = R | (G << 8) | (B << 16);
+    const float4 P = make_float4(fr, fg, fb, 0.0f), Z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 Q = make_float4(qr, qg, qb, 0.0f);
+    const float4 Q2 = make_float4(__fadd_rn(qr, qr), __fadd_rn(qg, qg), __fadd_rn(qb, qb), 0.0f);
+    t.ab[lane][0][0] = P;   // index 0: a = 1, b = 0
+    t.ab[lane][0][1] = Z;
+    t.ab[lane][1][0] = Z;   // index 1: a = 0, b = 1
+    t.ab[lane][1][1] = P;
+    t.ab[lane][2][0] = Q2;  // index 2: a = 2/3, b = 1/3
+    t.ab[lane][2][1] = Q;
+    t.ab[lane][3][0] = Q;   // index 3: a = 1/3, b = 2/3
+    t.ab[lane][3][1] = Q2;
+    pk = R | (G << 8) | (B << 16);
     sq = (int)(R * R + G * G + B * B);
+  }
+  // channel bytes of each group of four pixels
+  const int c = lane >> 2, g = lane & 3;
+  const uint32_t p0 = __shfl_sync(kFull, pk, 4 * g + 0), p1 = __shfl_sync(kFull, pk, 4 * g + 1);
+  const uint32_t p2 = __shfl_sync(kFull, pk, 4 * g + 2), p3 = __shfl_sync(kFull, pk, 4 * g + 3);
+  if (lane < 12) {
+    const uint32_t sh = 8 * c;
+    t.pg[c][g] = ((p0 >> sh) & 0xFF) | (((p1 >> sh) & 0xFF) << 8) | (((p2 >> sh) & 0xFF) << 16) |
+                 (((p3 >> sh) & 0xFF) << 24);
   }
   __syncwarp();
   return __reduce_add_sync(kFull, sq);
+}
+
+// Weight sums of the refit for index word `cand`, accumulated in the
+// reference's order (codec/dxt_image.cpp:307-312) from the per-index constants
+// wk[index] = (a*a, b*b, a*b).
+__device__ __forceinline__ WeightSums weight_sums(uint32_t cand, const float4 *wk) {
+  float asq = 0.f, bsq = 0.f, ab = 0.f;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const float4 w = wk[(cand >> (2 * i)) & 3u];
+    asq = __fadd_rn(asq, w.x);
+    bsq = __fadd_rn(bsq, w.y);
+    ab = __fadd_rn(ab, w.z);
+  }
+  WeightSums r;
+  r.asq = asq;
+  r.bsq = bsq;
+  r.ab = ab;
+  r.f = __frcp_rn(__fsub_rn(__fmul_rn(asq, bsq), __fmul_rn(ab, ab)));
+  return r;
+}
+
+// The per-index constants (a*a, b*b, a*b) with a, b as the reference computes
+// them: a = (3-order)/3.0f, b = order/3.0f.
+__device__ __forceinline__ void build_weight_table(float4 *wk) {
+  if (threadIdx.x < 4) {
+    const float order = threadIdx.x == 0 ? 0.f : threadIdx.x == 1 ? 3.f : threadIdx.x == 2 ? 1.f : 2.f;
+    const float a = __fdiv_rn(__fsub_rn(3.0f, order), 3.0f), b = __fdiv_rn(order, 3.0f);
+    wk[threadIdx.x] = make_float4(__fmul_rn(a, a), __fmul_rn(b, b), __fmul_rn(a, b), 0.0f);
+  }
+}
+
+// Byte selector for __byte_perm from one byte of an index word: the four 2-bit
+// indices of a group of pixels, spread to nibbles.
+__device__ __forceinline__ void build_spread_table(uint32_t *spread) {
+  for (int b = threadIdx.x; b < 256; b += blockDim.x)
+    spread[b] = (uint32_t)((b & 3) | ((b & 0xC) << 2) | ((b & 0x30) << 4) | ((b & 0xC0) << 6));
 }
 
 // x86 cvttss2si of v followed by max(0, min(255, .)) (codec/dxt_image.cpp:330-331):
@@ -159,47 +225,38 @@ __device__ __forceinline__ uint32_t pack565(uint32_t r, uint32_t g, uint32_t b) 
 // kInvalid when the refit would swap the endpoints (the candidate is skipped).
 // `own` is the block's stb interp: AssignIndices with it is the identity
 // (blk == blk2), which keeps the stb block with err_diff 0 and no refit.
-__device__ __forceinline__ int eval_candidate(const WarpBlock &wb, const uint8_t *snap5,
-                                              const uint8_t *snap6, uint32_t cand, uint32_t own,
-                                              int orig_err, int sumsq, uint32_t &eps, int &refit) {
+// ws holds the candidate's weight sums.
+__device__ __forceinline__ int eval_candidate(const BlockTab &t, const uint8_t *snap5, const uint8_t *snap6,
+                                              const uint32_t *spread, uint32_t cand, const WeightSums &ws,
+                                              uint32_t own, int orig_err, int sumsq, uint32_t &eps, int &refit) {
   if (cand == own) {
     eps = 0;
     refit = 0;
     return 0;
   }
   refit = 1;
-  // a = (3 - order)/3, b = order/3 with order = {0,3,1,2}[index]; the products
-  // px*a, px*b are {px,0}, {0,px}, {2q,q}, {q,2q}; a*a etc. are constants.
-  const float third = __fdiv_rn(1.0f, 3.0f), two3 = __fdiv_rn(2.0f, 3.0f);
-  const float k49 = __fmul_rn(two3, two3), k19 = __fmul_rn(third, third), k29 = __fmul_rn(two3, third);
-  float asq = 0.f, bsq = 0.f, ab = 0.f;
+  // refit sums, pixel by pixel in the reference's order (codec/dxt_image.cpp:298-318)
   float ax0 = 0.f, ax1 = 0.f, ax2 = 0.f, bx0 = 0.f, bx1 = 0.f, bx2 = 0.f;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
-    const bool b0 = (cand >> (2 * i)) & 1u;
-    const bool b1 = (cand >> (2 * i + 1)) & 1u;
-    const float4 P = wb.p[i], Q = wb.q[i], Q2 = wb.q2[i];
-    const float xa = b1 ? k49 : 1.0f, ya = b1 ? k19 : 0.0f;
-    asq = __fadd_rn(asq, b0 ? ya : xa);
-    bsq = __fadd_rn(bsq, b0 ? xa : ya);
-    ab = __fadd_rn(ab, b1 ? k29 : 0.0f);
-    const float x0 = b1 ? Q2.x : P.x, y0 = b1 ? Q.x : 0.0f;
-    const float x1 = b1 ? Q2.y : P.y, y1 = b1 ? Q.y : 0.0f;
-    const float x2 = b1 ? Q2.z : P.z, y2 = b1 ? Q.z : 0.0f;
-    ax0 = __fadd_rn(ax0, b0 ? y0 : x0);
-    bx0 = __fadd_rn(bx0, b0 ? x0 : y0);
-    ax1 = __fadd_rn(ax1, b0 ? y1 : x1);
-    bx1 = __fadd_rn(bx1, b0 ? x1 : y1);
-    ax2 = __fadd_rn(ax2, b0 ? y2 : x2);
-    bx2 = __fadd_rn(bx2, b0 ? x2 : y2);
+    const float4 *e = t.ab[i][(cand >> (2 * i)) & 3u];
+    const float4 A = e[0], B = e[1];
+    ax0 = __fadd_rn(ax0, A.x);
+    bx0 = __fadd_rn(bx0, B.x);
+    ax1 = __fadd_rn(ax1, A.y);
+    bx1 = __fadd_rn(bx1, B.y);
+    ax2 = __fadd_rn(ax2, A.z);
+    bx2 = __fadd_rn(bx2, B.z);
   }
-  const float f = __frcp_rn(__fsub_rn(__fmul_rn(asq, bsq), __fmul_rn(ab, ab)));
+  // 2x2 solve (codec/dxt_image.cpp:320-326)
+  const float f = ws.f, asq = ws.asq, bsq = ws.bsq, ab = ws.ab;
   const float p1r = __fmul_rn(f, __fsub_rn(__fmul_rn(ax0, bsq), __fmul_rn(bx0, ab)));
   const float p1g = __fmul_rn(f, __fsub_rn(__fmul_rn(ax1, bsq), __fmul_rn(bx1, ab)));
   const float p1b = __fmul_rn(f, __fsub_rn(__fmul_rn(ax2, bsq), __fmul_rn(bx2, ab)));
   const float p2r = __fmul_rn(f, __fsub_rn(__fmul_rn(bx0, asq), __fmul_rn(ax0, ab)));
   const float p2g = __fmul_rn(f, __fsub_rn(__fmul_rn(bx1, asq), __fmul_rn(ax1, ab)));
   const float p2b = __fmul_rn(f, __fsub_rn(__fmul_rn(bx2, asq), __fmul_rn(ax2, ab)));
+  // quantise + snap (codec/dxt_image.cpp:329-341)
   const uint32_t e1r = snap5[quantize_endpoint(__fadd_rn(p1r, 0.5f))];
   const uint32_t e1g = snap6[quantize_endpoint(__fadd_rn(p1g, 0.5f))];
   const uint32_t e1b = snap5[quantize_endpoint(__fadd_rn(p1b, 0.5f))];
@@ -209,31 +266,32 @@ __device__ __forceinline__ int eval_candidate(const WarpBlock &wb, const uint8_t
   const uint32_t q1 = pack565(e1r, e1g, e1b), q2 = pack565(e2r, e2g, e2b);
   if (q1 <= q2) return kInvalid;  // LogicalToPhysical would swap: skipped
   eps = q1 | (q2 << 16);
-  // 4-colour palette of the refit (LerpChannels 1/3, 2/3, :346-347)
-  const uint32_t c0 = e1r | (e1g << 8) | (e1b << 16);
-  const uint32_t c1 = e2r | (e2g << 8) | (e2b << 16);
-  const uint32_t c2 = ((2 * e1r + e2r) / 3) | (((2 * e1g + e2g) / 3) << 8) | (((2 * e1b + e2b) / 3) << 16);
-  const uint32_t c3 = ((e1r + 2 * e2r) / 3) | (((e1g + 2 * e2g) / 3) << 8) | (((e1b + 2 * e2b) / 3) << 16);
-  // SSE = sum|s|^2 - 2 sum s.pal[idx] + sum_k n_k |pal_k|^2, all exact integers
-  const uint32_t lo = cand & 0x55555555u, hi = (cand >> 1) & 0x55555555u;
-  const int n3 = __popc(lo & hi), n1 = __popc(lo & ~hi), n2 = __popc(hi & ~lo);
-  const int n0 = 16 - n1 - n2 - n3;
-  uint32_t cross = 0;
+  // 4-colour palette of the refit (LerpChannels 1/3, 2/3, :346-347), one word
+  // per channel holding the channel's four palette bytes
+  const uint32_t wr = e1r | (e2r << 8) | (((2 * e1r + e2r) / 3) << 16) | (((e1r + 2 * e2r) / 3) << 24);
+  const uint32_t wg = e1g | (e2g << 8) | (((2 * e1g + e2g) / 3) << 16) | (((e1g + 2 * e2g) / 3) << 24);
+  const uint32_t wb = e1b | (e2b << 8) | (((2 * e1b + e2b) / 3) << 16) | (((e1b + 2 * e2b) / 3) << 24);
+  // SSE = sum|s|^2 - 2 sum s.pal[idx] + sum |pal[idx]|^2 over four-pixel groups:
+  // __byte_perm gathers the indexed palette bytes, dp4a multiplies-adds them.
+  uint32_t cross = 0, norm = 0;
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const bool b0 = (cand >> (2 * i)) & 1u;
-    const bool b1 = (cand >> (2 * i + 1)) & 1u;
-    const uint32_t pal = b1 ? (b0 ? c3 : c2) : (b0 ? c1 : c0);
-    cross = __dp4a(wb.pk[i], pal, cross);
+  for (int g = 0; g < 4; ++g) {
+    const uint32_t sel = spread[(cand >> (8 * g)) & 0xFFu];
+    const uint32_t vr = __byte_perm(wr, 0u, sel), vg = __byte_perm(wg, 0u, sel), vb = __byte_perm(wb, 0u, sel);
+    cross = __dp4a(t.pg[0][g], vr, cross);
+    cross = __dp4a(t.pg[1][g], vg, cross);
+    cross = __dp4a(t.pg[2][g], vb, cross);
+    norm = __dp4a(vr, vr, norm);
+    norm = __dp4a(vg, vg, norm);
+    norm = __dp4a(vb, vb, norm);
   }
-  const uint32_t z = 0u;
-  const int sse = sumsq - 2 * (int)cross + n0 * (int)__dp4a(c0, c0, z) + n1 * (int)__dp4a(c1, c1, z) +
-                  n2 * (int)__dp4a(c2, c2, z) + n3 * (int)__dp4a(c3, c3, z);
+  const int sse = sumsq - 2 * (int)cross + (int)norm;
   return (int)((uint32_t)sse / 48u) - orig_err;
 }
 
 struct SearchParams {
   const uint8_t *rgb;
+  const float4 *wdesc;    // weight sums of the previous frame's final blocks (inter)
   const uint64_t *stb;
   const int32_t *orig_err;
   const uint64_t *prev;   // previous frame's final blocks (inter)
@@ -252,17 +310,19 @@ struct SearchParams {
 // the intra pass (done = 0).
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P) {
-  __shared__ WarpBlock s_wb[WARPS];
+  __shared__ BlockTab s_tab[WARPS];
   __shared__ uint8_t s_snap5[256], s_snap6[256];
+  __shared__ uint32_t s_spread[256];
   build_snap_tables(s_snap5, s_snap6);
+  build_spread_table(s_spread);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpBlock &wb = s_wb[warp];
+  BlockTab &tab = s_tab[warp];
   const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
   const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
   for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
     const int by = idx / P.bw, bx = idx - by * P.bw;
-    const int sumsq = stage_block(wb, P.rgb, P.width, bx, by, lane);
+    const int sumsq = stage_block(tab, P.rgb, P.width, bx, by, lane);
     const uint64_t stb = P.stb[idx];
     const uint32_t own = (uint32_t)(stb >> 32);
     const int orig = P.orig_err[idx];
@@ -275,8 +335,11 @@ __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P
       int e = kInvalid, refit = 0;
       uint32_t cand = 0, eps = 0;
       if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
-        cand = __ldg(prev_hi + 2 * ((size_t)j * P.bw + i));
-        e = eval_candidate(wb, s_snap5, s_snap6, cand, own, orig, sumsq, eps, refit);
+        const size_t nidx = (size_t)j * P.bw + i;
+        cand = __ldg(prev_hi + 2 * nidx);
+        const float4 d = __ldg(P.wdesc + nidx);
+        const WeightSums ws{d.x, d.y, d.z, d.w};
+        e = eval_candidate(tab, s_snap5, s_snap6, s_spread, cand, ws, own, orig, sumsq, eps, refit);
       }
       sel_chunk(st, lane, row, e, pos, cand, eps, refit);
     }
@@ -290,6 +353,19 @@ __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P
       P.done[idx] = accept ? 1u : 0u;
     }
     __syncwarp();
+  }
+}
+
+// Weight sums of the refit for every block's index word (the candidates the
+// next inter search reads), one thread per block.
+__global__ void __launch_bounds__(256) weight_desc_kernel(const uint64_t *__restrict__ blocks, int n,
+                                                          float4 *__restrict__ desc) {
+  __shared__ float4 s_wk[4];
+  build_weight_table(s_wk);
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const WeightSums w = weight_sums((uint32_t)(__ldg(blocks + i) >> 32), s_wk);
+    desc[i] = make_float4(w.asq, w.bsq, w.ab, w.f);
   }
 }
 
@@ -444,12 +520,16 @@ template <int THREADS>
 __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, const uint32_t *__restrict__ pending,
                                                                const uint32_t *__restrict__ n_pending_dev,
                                                                int n_pending_host) {
-  __shared__ WarpBlock s_wb;
+  __shared__ BlockTab s_tab;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
+  __shared__ uint32_t s_spread[256];
+  __shared__ float4 s_wk[4];
   __shared__ int s_red[2 * (THREADS / 32)];
   __shared__ CtaSel s_sel;
   __shared__ int s_claim, s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
+  build_spread_table(s_spread);
+  build_weight_table(s_wk);
   CtaReduce<THREADS> red{s_red, 0};
   const int tid = threadIdx.x, lane = tid & 31;
   const int n_pend = n_pending_host >= 0 ? n_pending_host : (int)__ldcg(n_pending_dev);
@@ -463,7 +543,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
     const int idx = (int)__ldcg(pending + k);
     const int by = idx / P.bw, bx = idx - by * P.bw;
     if (tid < 32) {
-      const int sq = stage_block(s_wb, P.rgb, P.width, bx, by, lane);
+      const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
       if (tid == 0) {
         s_sumsq = sq;
         s_sel.min_e = kInvalid;
@@ -489,7 +569,8 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
         const size_t nidx = (size_t)j * P.bw + i;
         if (wait_done(P.done, nidx, P.status)) {
           cand = __ldcg(fin_hi + 2 * nidx);
-          e = eval_candidate(s_wb, s_snap5, s_snap6, cand, own, orig, sumsq, eps, refit);
+          const WeightSums ws = weight_sums(cand, s_wk);
+          e = eval_candidate(s_tab, s_snap5, s_snap6, s_spread, cand, ws, own, orig, sumsq, eps, refit);
         }
       }
       cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
