@@ -154,9 +154,10 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
   return P;
 }
 
-enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_UNIQUE, K_STATS, K_COUNT };
-const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel", "inter_search_kernel", "intra_search_kernel",
-                                     "unique_kernels", "frame_stats_kernel"};
+enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_STATS, K_COUNT };
+const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_search_kernel",
+                                     "intra_search_kernel",     "intra_search_kernel/inter_frame",
+                                     "unique_kernels",          "frame_stats_kernel"};
 
 cudaEvent_t pool_event(mptc_ctx *ctx) {
   if (ctx->ev_used == ctx->ev_pool.size()) {
@@ -346,7 +347,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
                                                             ctx->ntiles, ctx->pending, ctx->work + 5);
   }
   {
-    KernelTimer t(ctx, K_INTRA, s);
+    KernelTimer t(ctx, prev_final_dev ? K_PENDING : K_INTRA, s);
     if (prev_final_dev)
       mptc::intra_search_kernel<kIntraThreads><<<ctx->intra_grid, kIntraThreads, 0, s>>>(P, ctx->pending,
                                                                                         ctx->work + 5, -1);

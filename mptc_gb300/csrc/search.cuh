@@ -39,10 +39,28 @@ constexpr uint32_t kDevTimeout = 1u;
 // with q = fl(px * fl(1/3)) (fl(2/3) = 2 fl(1/3), and doubling is exact), so
 // the block keeps them as a table ab[i][index] = {A.xyz, B.xyz} and a
 // candidate's refit becomes one lookup and six adds per pixel.
+//
+// Layout ab[pixel][part][index] (float2): part 0 = (A_r, A_g), 1 = (A_b, B_r),
+// 2 = (B_g, B_b). The four index variants of one (pixel, part) are adjacent,
+// so the lanes of a warp, whatever their indices, read distinct banks.
 struct __align__(16) BlockTab {
-  float4 ab[16][4][2];  // [pixel][index][0] = (A_r, A_g, A_b, 0), [1] = (B_r, B_g, B_b, 0)
+  float2 ab[16][3][4];
   uint32_t pg[3][4];    // channel c bytes of pixels 4g .. 4g+3 (for dp4a)
 };
+
+// The twelve channel-group words of the staged block, held in registers.
+struct PixelGroups {
+  uint32_t w[3][4];
+};
+
+__device__ __forceinline__ PixelGroups load_groups(const BlockTab &t) {
+  PixelGroups g;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) g.w[c][k] = t.pg[c][k];
+  return g;
+}
 
 // Per-candidate weight sums of the refit (they depend on the index word only).
 struct WeightSums {
@@ -148,14 +166,14 @@ __device__ __forceinline__ int stage_block(BlockTab &t, const uint8_t *__restric
     const float4 P = make_float4(fr, fg, fb, 0.0f), Z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float4 Q = make_float4(qr, qg, qb, 0.0f);
     const float4 Q2 = make_float4(__fadd_rn(qr, qr), __fadd_rn(qg, qg), __fadd_rn(qb, qb), 0.0f);
-    t.ab[lane][0][0] = P;   // index 0: a = 1, b = 0
-    t.ab[lane][0][1] = Z;
-    t.ab[lane][1][0] = Z;   // index 1: a = 0, b = 1
-    t.ab[lane][1][1] = P;
-    t.ab[lane][2][0] = Q2;  // index 2: a = 2/3, b = 1/3
-    t.ab[lane][2][1] = Q;
-    t.ab[lane][3][0] = Q;   // index 3: a = 1/3, b = 2/3
-    t.ab[lane][3][1] = Q2;
+    // (A, B) per index: 0: (px, 0), 1: (0, px), 2: (2q, q), 3: (q, 2q)
+    const float4 va[4] = {P, Z, Q2, Q}, vb[4] = {Z, P, Q, Q2};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      t.ab[lane][0][k] = make_float2(va[k].x, va[k].y);
+      t.ab[lane][1][k] = make_float2(va[k].z, vb[k].x);
+      t.ab[lane][2][k] = make_float2(vb[k].y, vb[k].z);
+    }
     pk = R | (G << 8) | (B << 16);
     sq = (int)(R * R + G * G + B * B);
   }
@@ -204,9 +222,9 @@ __device__ __forceinline__ void build_weight_table(float4 *wk) {
 
 // Byte selector for __byte_perm from one byte of an index word: the four 2-bit
 // indices of a group of pixels, spread to nibbles.
-__device__ __forceinline__ void build_spread_table(uint32_t *spread) {
-  for (int b = threadIdx.x; b < 256; b += blockDim.x)
-    spread[b] = (uint32_t)((b & 3) | ((b & 0xC) << 2) | ((b & 0x30) << 4) | ((b & 0xC0) << 6));
+__device__ __forceinline__ uint32_t spread_nibbles(uint32_t b) {
+  b = (b | (b << 4)) & 0x0F0Fu;
+  return (b | (b << 2)) & 0x3333u;
 }
 
 // x86 cvttss2si of v followed by max(0, min(255, .)) (codec/dxt_image.cpp:330-331):
@@ -226,8 +244,8 @@ __device__ __forceinline__ uint32_t pack565(uint32_t r, uint32_t g, uint32_t b) 
 // `own` is the block's stb interp: AssignIndices with it is the identity
 // (blk == blk2), which keeps the stb block with err_diff 0 and no refit.
 // ws holds the candidate's weight sums.
-__device__ __forceinline__ int eval_candidate(const BlockTab &t, const uint8_t *snap5, const uint8_t *snap6,
-                                              const uint32_t *spread, uint32_t cand, const WeightSums &ws,
+__device__ __forceinline__ int eval_candidate(const BlockTab &t, const PixelGroups &pg, const uint8_t *snap5,
+                                              const uint8_t *snap6, uint32_t cand, const WeightSums &ws,
                                               uint32_t own, int orig_err, int sumsq, uint32_t &eps, int &refit) {
   if (cand == own) {
     eps = 0;
@@ -239,14 +257,14 @@ __device__ __forceinline__ int eval_candidate(const BlockTab &t, const uint8_t *
   float ax0 = 0.f, ax1 = 0.f, ax2 = 0.f, bx0 = 0.f, bx1 = 0.f, bx2 = 0.f;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
-    const float4 *e = t.ab[i][(cand >> (2 * i)) & 3u];
-    const float4 A = e[0], B = e[1];
-    ax0 = __fadd_rn(ax0, A.x);
-    bx0 = __fadd_rn(bx0, B.x);
-    ax1 = __fadd_rn(ax1, A.y);
-    bx1 = __fadd_rn(bx1, B.y);
-    ax2 = __fadd_rn(ax2, A.z);
-    bx2 = __fadd_rn(bx2, B.z);
+    const uint32_t k = (cand >> (2 * i)) & 3u;
+    const float2 u = t.ab[i][0][k], v = t.ab[i][1][k], w = t.ab[i][2][k];
+    ax0 = __fadd_rn(ax0, u.x);
+    bx0 = __fadd_rn(bx0, v.y);
+    ax1 = __fadd_rn(ax1, u.y);
+    bx1 = __fadd_rn(bx1, w.x);
+    ax2 = __fadd_rn(ax2, v.x);
+    bx2 = __fadd_rn(bx2, w.y);
   }
   // 2x2 solve (codec/dxt_image.cpp:320-326)
   const float f = ws.f, asq = ws.asq, bsq = ws.bsq, ab = ws.ab;
@@ -276,11 +294,11 @@ __device__ __forceinline__ int eval_candidate(const BlockTab &t, const uint8_t *
   uint32_t cross = 0, norm = 0;
 #pragma unroll
   for (int g = 0; g < 4; ++g) {
-    const uint32_t sel = spread[(cand >> (8 * g)) & 0xFFu];
+    const uint32_t sel = spread_nibbles((cand >> (8 * g)) & 0xFFu);
     const uint32_t vr = __byte_perm(wr, 0u, sel), vg = __byte_perm(wg, 0u, sel), vb = __byte_perm(wb, 0u, sel);
-    cross = __dp4a(t.pg[0][g], vr, cross);
-    cross = __dp4a(t.pg[1][g], vg, cross);
-    cross = __dp4a(t.pg[2][g], vb, cross);
+    cross = __dp4a(pg.w[0][g], vr, cross);
+    cross = __dp4a(pg.w[1][g], vg, cross);
+    cross = __dp4a(pg.w[2][g], vb, cross);
     norm = __dp4a(vr, vr, norm);
     norm = __dp4a(vg, vg, norm);
     norm = __dp4a(vb, vb, norm);
@@ -312,9 +330,7 @@ template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P) {
   __shared__ BlockTab s_tab[WARPS];
   __shared__ uint8_t s_snap5[256], s_snap6[256];
-  __shared__ uint32_t s_spread[256];
   build_snap_tables(s_snap5, s_snap6);
-  build_spread_table(s_spread);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   BlockTab &tab = s_tab[warp];
@@ -323,6 +339,7 @@ __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P
   for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
     const int by = idx / P.bw, bx = idx - by * P.bw;
     const int sumsq = stage_block(tab, P.rgb, P.width, bx, by, lane);
+    const PixelGroups pg = load_groups(tab);
     const uint64_t stb = P.stb[idx];
     const uint32_t own = (uint32_t)(stb >> 32);
     const int orig = P.orig_err[idx];
@@ -339,7 +356,7 @@ __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P
         cand = __ldg(prev_hi + 2 * nidx);
         const float4 d = __ldg(P.wdesc + nidx);
         const WeightSums ws{d.x, d.y, d.z, d.w};
-        e = eval_candidate(tab, s_snap5, s_snap6, s_spread, cand, ws, own, orig, sumsq, eps, refit);
+        e = eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
       }
       sel_chunk(st, lane, row, e, pos, cand, eps, refit);
     }
@@ -522,13 +539,11 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
                                                                int n_pending_host) {
   __shared__ BlockTab s_tab;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
-  __shared__ uint32_t s_spread[256];
   __shared__ float4 s_wk[4];
   __shared__ int s_red[2 * (THREADS / 32)];
   __shared__ CtaSel s_sel;
   __shared__ int s_claim, s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
-  build_spread_table(s_spread);
   build_weight_table(s_wk);
   CtaReduce<THREADS> red{s_red, 0};
   const int tid = threadIdx.x, lane = tid & 31;
@@ -559,6 +574,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
     const uint32_t own = (uint32_t)(stb >> 32);
     const int orig = __ldg(P.orig_err + idx);
     const int sumsq = s_sumsq;
+    const PixelGroups pg = load_groups(s_tab);
     for (int base = 0; base < npos; base += THREADS) {
       const int pos = base + tid;
       const int row = pos / w2, col = pos - row * w2;
@@ -570,7 +586,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
         if (wait_done(P.done, nidx, P.status)) {
           cand = __ldcg(fin_hi + 2 * nidx);
           const WeightSums ws = weight_sums(cand, s_wk);
-          e = eval_candidate(s_tab, s_snap5, s_snap6, s_spread, cand, ws, own, orig, sumsq, eps, refit);
+          e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
         }
       }
       cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
@@ -587,8 +603,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
       }
       P.final_blk[idx] = blk;
       P.motion[idx] = m;
-      __threadfence();
-      st_release(P.done + idx, 1u);
+      st_release(P.done + idx, 1u);  // orders the two stores above before the flag
     }
     __syncthreads();
   }
