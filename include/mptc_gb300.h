@@ -138,6 +138,43 @@ mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t width, int
                                       uint64_t *stb_dev, uint64_t *final_dev, uint8_t *motion_dev,
                                       uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream);
 
+/* Batched encoding of many independent streams (resolutions may differ); the
+ * multi-stream form of the reference's per-stream encoder loop
+ * (codec/codec.cpp:1383-1509, and ThreadedCompressMultiUnique's one thread per
+ * chunk, :1781-1856). One call encodes one frame of every stream. The batch
+ * owns each stream's input buffer, its previous/current final blocks and its
+ * outputs; the work of all streams is launched as one CUDA graph (captured on
+ * first use of each intra/inter pattern) whose per-stream branches run
+ * concurrently, so one stream's latency-bound intra search overlaps the other
+ * streams' inter searches. */
+typedef struct mptc_batch mptc_batch;
+mptc_status mptc_batch_create(const mptc_config *cfg, int32_t n_streams, const int32_t *widths,
+                              const int32_t *heights, mptc_batch **out_batch);
+mptc_status mptc_batch_destroy(mptc_batch *batch);
+/* Device buffer (width*height*3 bytes) that receives stream i's next frame. */
+mptc_status mptc_batch_input(mptc_batch *batch, int32_t i, uint8_t **rgb_dev);
+/* Device outputs of stream i's last encoded frame (valid until the next call). */
+mptc_status mptc_batch_output(mptc_batch *batch, int32_t i, const uint64_t **final_dev,
+                              const uint8_t **motion_dev, const uint32_t **unique_dev,
+                              const uint32_t **n_unique_dev);
+/* Copies a frame (host or device memory, width*height*3 bytes) into stream
+ * i's input buffer on `stream`. */
+mptc_status mptc_batch_upload(mptc_batch *batch, int32_t i, const uint8_t *rgb, void *stream);
+/* Copies stream i's last outputs to host memory (synchronises `stream`);
+ * unique_host needs room for blocks entries; any pointer may be NULL. */
+mptc_status mptc_batch_fetch(mptc_batch *batch, int32_t i, uint64_t *final_host, uint8_t *motion_host,
+                             uint32_t *unique_host, uint32_t *n_unique_host, void *stream);
+/* Encodes the frame in every stream's input buffer; is_intra: host array, one
+ * flag per stream (a stream's first frame must be intra). Asynchronous on
+ * `stream`. */
+mptc_status mptc_batch_encode(mptc_batch *batch, const int32_t *is_intra, void *stream);
+/* Autotuner: times the candidate launch shapes on the current inputs and the
+ * given intra/inter pattern (without advancing the streams) and keeps the
+ * fastest: warps per CTA of the inter search (4, 8, 16) and the CTA count of
+ * each stream's intra search. Writes the chosen values (synchronises). */
+mptc_status mptc_batch_autotune(mptc_batch *batch, const int32_t *is_intra, int32_t *inter_warps,
+                                int32_t *intra_ctas, void *stream);
+
 /* Counters of the last frame reencoded on this context (synchronises `stream`). */
 mptc_status mptc_last_frame_stats(mptc_ctx *ctx, mptc_frame_stats *out, void *stream);
 

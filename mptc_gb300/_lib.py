@@ -19,7 +19,9 @@ EXPORTED = [
     "mptc_ctx_create", "mptc_ctx_destroy", "mptc_dxt1_encode", "mptc_reencode",
     "mptc_encode_frame", "mptc_encode_frame_host", "mptc_last_frame_stats", "mptc_last_error",
     "mptc_version", "mptc_built_arch", "mptc_set_kernel_timing", "mptc_kernel_times",
-    "mptc_alu_probe", "mptc_encode_frame_noalloc",
+    "mptc_alu_probe", "mptc_encode_frame_noalloc", "mptc_batch_create", "mptc_batch_destroy",
+    "mptc_batch_input", "mptc_batch_output", "mptc_batch_upload", "mptc_batch_fetch",
+    "mptc_batch_encode", "mptc_batch_autotune",
 ]
 
 NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
@@ -72,6 +74,15 @@ def lib() -> ctypes.CDLL:
         L.mptc_alu_probe.argtypes = [i32, i32, vp, ctypes.POINTER(ctypes.c_double), vp]
         L.mptc_encode_frame_noalloc.argtypes = [ctypes.POINTER(Config), i32, i32, vp, vp, vp, vp, vp,
                                                 vp, u32p, vp]
+        L.mptc_batch_create.argtypes = [ctypes.POINTER(Config), i32, vp, vp, ctypes.POINTER(vp)]
+        L.mptc_batch_destroy.argtypes = [vp]
+        L.mptc_batch_input.argtypes = [vp, i32, ctypes.POINTER(vp)]
+        L.mptc_batch_output.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                        ctypes.POINTER(vp), ctypes.POINTER(vp)]
+        L.mptc_batch_upload.argtypes = [vp, i32, vp, vp]
+        L.mptc_batch_fetch.argtypes = [vp, i32, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32), vp]
+        L.mptc_batch_encode.argtypes = [vp, vp, vp]
+        L.mptc_batch_autotune.argtypes = [vp, vp, ctypes.POINTER(i32), ctypes.POINTER(i32), vp]
         L.mptc_version.restype = i32
         L.mptc_built_arch.restype = i32
         for name in EXPORTED:

@@ -1,0 +1,89 @@
+"""Batched multi-stream encoding over the C ABI (mptc_batch_*).
+
+One call encodes one frame of every stream; the streams may have different
+resolutions. Frames enter through ``upload`` (host arrays or device tensors)
+and results leave through ``fetch``; between the two the work of all streams
+runs as one CUDA graph with a concurrent branch per stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import Config, check, lib
+
+
+class BatchEncoder:
+    def __init__(self, sizes: list[tuple[int, int]], search_area: int = 8, err_threshold: int = 5,
+                 intra_interval: int = 16):
+        self.sizes = list(sizes)
+        self.n = len(sizes)
+        self.intra_interval = intra_interval
+        w = (ctypes.c_int32 * self.n)(*[s[0] for s in sizes])
+        h = (ctypes.c_int32 * self.n)(*[s[1] for s in sizes])
+        cfg = Config(search_area, err_threshold, intra_interval, 0)
+        handle = ctypes.c_void_p()
+        check(lib().mptc_batch_create(ctypes.byref(cfg), self.n, w, h, ctypes.byref(handle)))
+        self._b = handle
+        self._num = [1] * self.n
+        self._next_intra = [True] * self.n
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            lib().mptc_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def nblk(self, i: int) -> int:
+        return (self.sizes[i][0] // 4) * (self.sizes[i][1] // 4)
+
+    def upload(self, i: int, frame, stream=None) -> None:
+        """frame: (H, W, 3) uint8 numpy array or CUDA tensor."""
+        ptr = frame.data_ptr() if hasattr(frame, "data_ptr") else np.ascontiguousarray(frame).ctypes.data
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_batch_upload(self._b, i, ptr, s))
+
+    def schedule(self) -> list[bool]:
+        """Intra flags of the next step: the reference's intra-interval rule per stream."""
+        out = []
+        for i in range(self.n):
+            out.append(self._next_intra[i])
+            if self._num[i] <= self.intra_interval:
+                self._next_intra[i] = False
+                if self._num[i] == self.intra_interval:
+                    self._next_intra[i] = True
+                    self._num[i] = 1
+                else:
+                    self._num[i] += 1
+        return out
+
+    def encode(self, is_intra: list[bool] | None = None, stream=None) -> list[bool]:
+        flags = self.schedule() if is_intra is None else list(is_intra)
+        arr = (ctypes.c_int32 * self.n)(*[int(bool(f)) for f in flags])
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_batch_encode(self._b, arr, s))
+        return flags
+
+    def autotune(self, is_intra: list[bool], stream=None) -> tuple[int, int]:
+        arr = (ctypes.c_int32 * self.n)(*[int(bool(f)) for f in is_intra])
+        w, c = ctypes.c_int32(0), ctypes.c_int32(0)
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_batch_autotune(self._b, arr, ctypes.byref(w), ctypes.byref(c), s))
+        return w.value, c.value
+
+    def fetch(self, i: int, stream=None):
+        n = self.nblk(i)
+        fin = np.empty(n, np.uint64)
+        mot = np.empty(2 * n, np.uint8)
+        uni = np.empty(n, np.uint32)
+        nu = ctypes.c_uint32(0)
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_batch_fetch(self._b, i, fin.ctypes.data, mot.ctypes.data, uni.ctypes.data,
+                                     ctypes.byref(nu), s))
+        return fin, mot, uni[: nu.value]

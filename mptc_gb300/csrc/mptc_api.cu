@@ -3,7 +3,9 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -24,6 +26,8 @@ struct mptc_ctx {
   mptc_config cfg{};
   int width = 0, height = 0, bw = 0, bh = 0, nblk = 0, ntiles = 0;
   int device = 0, sm_count = 0, intra_grid = 0;
+  // launch shapes (tunable): warps per CTA of the inter search, CTA cap of the intra search
+  int inter_warps = kSearchWarps, intra_cap = 0;
   // device scratch
   uint32_t *done = nullptr;        // per block
   uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count
@@ -332,10 +336,16 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   mptc::SearchParams P = make_params(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev);
   MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, 8 * sizeof(uint32_t), s));
   if (prev_final_dev) {
-    int grid = (ctx->nblk + kSearchWarps - 1) / kSearchWarps;
     KernelTimer t(ctx, K_INTER, s);
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
-    mptc::inter_search_kernel<kSearchWarps><<<grid, kSearchWarps * 32, 0, s>>>(P);
+    const int w = ctx->inter_warps;
+    const int grid = (ctx->nblk + w - 1) / w;
+    if (w == 4)
+      mptc::inter_search_kernel<4><<<grid, 4 * 32, 0, s>>>(P);
+    else if (w == 16)
+      mptc::inter_search_kernel<16><<<grid, 16 * 32, 0, s>>>(P);
+    else
+      mptc::inter_search_kernel<8><<<grid, 8 * 32, 0, s>>>(P);
     MPTC_CUDA(cudaGetLastError());
   } else {
     MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint32_t), s));
@@ -348,12 +358,11 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   }
   {
     KernelTimer t(ctx, prev_final_dev ? K_PENDING : K_INTRA, s);
+    const int ig = ctx->intra_cap > 0 ? std::min(ctx->intra_cap, ctx->intra_grid) : ctx->intra_grid;
     if (prev_final_dev)
-      mptc::intra_search_kernel<kIntraThreads><<<ctx->intra_grid, kIntraThreads, 0, s>>>(P, ctx->pending,
-                                                                                        ctx->work + 5, -1);
+      mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->pending, ctx->work + 5, -1);
     else
-      mptc::intra_search_kernel<kIntraThreads><<<ctx->intra_grid, kIntraThreads, 0, s>>>(P, ctx->order, nullptr,
-                                                                                        ctx->nblk);
+      mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
   }
   MPTC_CUDA(cudaGetLastError());
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
@@ -616,3 +625,247 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   noalloc_status_kernel<<<1, 32, 0, s>>>(work, n_unique_dev);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
+
+// ---------------------------------------------------------------------------
+// Batched multi-stream encoding: per-stream contexts on forked CUDA streams,
+// one CUDA graph per (intra/inter pattern, ping-pong parity).
+// ---------------------------------------------------------------------------
+struct mptc_batch {
+  int n = 0;
+  std::vector<mptc_ctx *> ctx;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> done_ev;
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<uint8_t *> rgb;
+  std::vector<uint64_t *> fin[2];
+  std::vector<uint8_t *> motion;
+  std::vector<uint32_t *> unique;
+  uint32_t *n_unique = nullptr;  // one per stream
+  std::vector<char> has_prev;
+  int parity = 0;                // final[parity] receives the next frame
+  std::map<std::string, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+void batch_clear_graphs(mptc_batch *b) {
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+// Launches one frame of every stream on the forked streams (capturable).
+mptc_status batch_launch(mptc_batch *b, const int32_t *is_intra, int parity, cudaStream_t s) {
+  if (cudaEventRecord(b->fork_ev, s) != cudaSuccess) return MPTC_ECUDA;
+  for (int i = 0; i < b->n; ++i) {
+    cudaStream_t si = b->streams[i];
+    if (cudaStreamWaitEvent(si, b->fork_ev, 0) != cudaSuccess) return MPTC_ECUDA;
+    const uint64_t *prev = is_intra[i] ? nullptr : b->fin[parity ^ 1][i];
+    mptc_status st = mptc_encode_frame(b->ctx[i], b->rgb[i], prev, nullptr, b->fin[parity][i], b->motion[i],
+                                       b->unique[i], b->n_unique + i, si);
+    if (st != MPTC_OK) return st;
+    if (cudaEventRecord(b->done_ev[i], si) != cudaSuccess) return MPTC_ECUDA;
+    if (cudaStreamWaitEvent(s, b->done_ev[i], 0) != cudaSuccess) return MPTC_ECUDA;
+  }
+  return MPTC_OK;
+}
+
+mptc_status batch_run(mptc_batch *b, const int32_t *is_intra, int parity, cudaStream_t s) {
+  std::string key(1, (char)('0' + parity));
+  for (int i = 0; i < b->n; ++i) key.push_back(is_intra[i] ? 'I' : 'P');
+  auto it = b->graphs.find(key);
+  if (it == b->graphs.end()) {
+    // capture on a private stream so the caller's stream is never in capture mode
+    cudaStream_t cs;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return MPTC_ECUDA;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    mptc_status st = MPTC_OK;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) st = MPTC_ECUDA;
+    if (st == MPTC_OK) st = batch_launch(b, is_intra, parity, cs);
+    cudaError_t e = cudaStreamEndCapture(cs, &g);
+    if (st == MPTC_OK && e != cudaSuccess) st = MPTC_ECUDA;
+    if (st == MPTC_OK && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) st = MPTC_ECUDA;
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (st != MPTC_OK) {
+      cudaGetLastError();
+      return st;
+    }
+    it = b->graphs.emplace(key, ge).first;
+  }
+  return cudaGraphLaunch(it->second, s) == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+mptc_status mptc_batch_create(const mptc_config *cfg, int32_t n_streams, const int32_t *widths,
+                              const int32_t *heights, mptc_batch **out_batch) {
+  if (!cfg || !widths || !heights || !out_batch || n_streams <= 0 || n_streams > 1024) return MPTC_EINVAL;
+  *out_batch = nullptr;
+  mptc_batch *b = new (std::nothrow) mptc_batch();
+  if (!b) return MPTC_ENOMEM;
+  b->n = n_streams;
+  auto bad = [&](mptc_status st) {
+    mptc_batch_destroy(b);
+    return st;
+  };
+  if (cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bad(MPTC_ECUDA);
+  if (dalloc(&b->n_unique, (size_t)n_streams)) return bad(MPTC_ENOMEM);
+  for (int i = 0; i < n_streams; ++i) {
+    mptc_ctx *c = nullptr;
+    mptc_status st = mptc_ctx_create(cfg, widths[i], heights[i], &c);
+    if (st != MPTC_OK) return bad(st);
+    b->ctx.push_back(c);
+    cudaStream_t si;
+    cudaEvent_t ev;
+    if (cudaStreamCreateWithFlags(&si, cudaStreamNonBlocking) != cudaSuccess) return bad(MPTC_ECUDA);
+    b->streams.push_back(si);
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return bad(MPTC_ECUDA);
+    b->done_ev.push_back(ev);
+    const size_t nb = (size_t)c->nblk;
+    uint8_t *rgb = nullptr, *mot = nullptr;
+    uint64_t *f0 = nullptr, *f1 = nullptr;
+    uint32_t *uni = nullptr;
+    if (dalloc(&rgb, nb * 48) || dalloc(&f0, nb) || dalloc(&f1, nb) || dalloc(&mot, 2 * nb) || dalloc(&uni, nb))
+      return bad(MPTC_ENOMEM);
+    b->rgb.push_back(rgb);
+    b->fin[0].push_back(f0);
+    b->fin[1].push_back(f1);
+    b->motion.push_back(mot);
+    b->unique.push_back(uni);
+    b->has_prev.push_back(0);
+  }
+  *out_batch = b;
+  return MPTC_OK;
+}
+
+mptc_status mptc_batch_destroy(mptc_batch *b) {
+  if (!b) return MPTC_EINVAL;
+  cudaDeviceSynchronize();
+  batch_clear_graphs(b);
+  for (auto c : b->ctx) mptc_ctx_destroy(c);
+  for (auto s : b->streams) cudaStreamDestroy(s);
+  for (auto e : b->done_ev) cudaEventDestroy(e);
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+  for (auto p : b->rgb) cudaFree(p);
+  for (int k = 0; k < 2; ++k)
+    for (auto p : b->fin[k]) cudaFree(p);
+  for (auto p : b->motion) cudaFree(p);
+  for (auto p : b->unique) cudaFree(p);
+  cudaFree(b->n_unique);
+  delete b;
+  return MPTC_OK;
+}
+
+mptc_status mptc_batch_input(mptc_batch *b, int32_t i, uint8_t **rgb_dev) {
+  if (!b || !rgb_dev || i < 0 || i >= b->n) return MPTC_EINVAL;
+  *rgb_dev = b->rgb[i];
+  return MPTC_OK;
+}
+
+mptc_status mptc_batch_output(mptc_batch *b, int32_t i, const uint64_t **final_dev, const uint8_t **motion_dev,
+                              const uint32_t **unique_dev, const uint32_t **n_unique_dev) {
+  if (!b || i < 0 || i >= b->n) return MPTC_EINVAL;
+  const int last = b->parity ^ 1;  // the buffer written by the last encode
+  if (final_dev) *final_dev = b->fin[last][i];
+  if (motion_dev) *motion_dev = b->motion[i];
+  if (unique_dev) *unique_dev = b->unique[i];
+  if (n_unique_dev) *n_unique_dev = b->n_unique + i;
+  return MPTC_OK;
+}
+
+mptc_status mptc_batch_upload(mptc_batch *b, int32_t i, const uint8_t *rgb, void *stream) {
+  if (!b || !rgb || i < 0 || i >= b->n) return MPTC_EINVAL;
+  const size_t bytes = (size_t)b->ctx[i]->nblk * 48;
+  return cudaMemcpyAsync(b->rgb[i], rgb, bytes, cudaMemcpyDefault, static_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? MPTC_OK
+             : MPTC_ECUDA;
+}
+
+mptc_status mptc_batch_fetch(mptc_batch *b, int32_t i, uint64_t *final_host, uint8_t *motion_host,
+                             uint32_t *unique_host, uint32_t *n_unique_host, void *stream) {
+  if (!b || i < 0 || i >= b->n) return MPTC_EINVAL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)b->ctx[i]->nblk;
+  const int last = b->parity ^ 1;
+  uint32_t nu = 0;
+  if (cudaMemcpyAsync(&nu, b->n_unique + i, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPTC_ECUDA;
+  if (final_host && cudaMemcpyAsync(final_host, b->fin[last][i], n * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return MPTC_ECUDA;
+  if (motion_host && cudaMemcpyAsync(motion_host, b->motion[i], n * 2, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return MPTC_ECUDA;
+  if (unique_host && cudaMemcpyAsync(unique_host, b->unique[i], n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return MPTC_ECUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MPTC_ECUDA;
+  uint32_t w[2];
+  if (cudaMemcpy(w, b->ctx[i]->work, sizeof(w), cudaMemcpyDeviceToHost) != cudaSuccess) return MPTC_ECUDA;
+  if (w[1] & mptc::kDevTimeout) return MPTC_ETIMEOUT;
+  if (n_unique_host) *n_unique_host = nu;
+  return MPTC_OK;
+}
+
+mptc_status mptc_batch_encode(mptc_batch *b, const int32_t *is_intra, void *stream) {
+  if (!b || !is_intra) return MPTC_EINVAL;
+  for (int i = 0; i < b->n; ++i)
+    if (!is_intra[i] && !b->has_prev[i]) return MPTC_ESTATE;
+  mptc_status st = batch_run(b, is_intra, b->parity, static_cast<cudaStream_t>(stream));
+  if (st != MPTC_OK) return st;
+  for (int i = 0; i < b->n; ++i) b->has_prev[i] = 1;
+  b->parity ^= 1;
+  return MPTC_OK;
+}
+
+mptc_status mptc_batch_autotune(mptc_batch *b, const int32_t *is_intra, int32_t *inter_warps, int32_t *intra_ctas,
+                                void *stream) {
+  if (!b || !is_intra) return MPTC_EINVAL;
+  for (int i = 0; i < b->n; ++i)
+    if (!is_intra[i] && !b->has_prev[i]) return MPTC_ESTATE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // trial steps re-encode the current inputs into the buffers of the next
+  // real step (same parity), so the streams do not advance
+  const int warps[3] = {4, 8, 16};
+  const int sms = b->ctx[0]->sm_count;
+  const int caps[5] = {0, 8 * sms, 4 * sms, 2 * sms, sms};
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return MPTC_ECUDA;
+  float best = 1e30f;
+  int bw = kSearchWarps, bc = 0;
+  mptc_status st = MPTC_OK;
+  for (int w : warps) {
+    for (int c : caps) {
+      for (auto cx : b->ctx) {
+        cx->inter_warps = w;
+        cx->intra_cap = c;
+      }
+      batch_clear_graphs(b);
+      st = batch_run(b, is_intra, b->parity, s);  // capture + warm-up
+      if (st != MPTC_OK) break;
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 3 && st == MPTC_OK; ++r) st = batch_run(b, is_intra, b->parity, s);
+      cudaEventRecord(e1, s);
+      if (st != MPTC_OK || cudaEventSynchronize(e1) != cudaSuccess) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        bw = w;
+        bc = c;
+      }
+    }
+    if (st != MPTC_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (auto cx : b->ctx) {
+    cx->inter_warps = bw;
+    cx->intra_cap = bc;
+  }
+  batch_clear_graphs(b);
+  if (inter_warps) *inter_warps = bw;
+  if (intra_ctas) *intra_ctas = bc;
+  return st;
+}
+
+}  // extern "C"
