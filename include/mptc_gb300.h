@@ -58,6 +58,7 @@ typedef struct mptc_ctx mptc_ctx;
 typedef struct mptc_frame_stats {
   uint32_t n_inter, n_intra, n_unique;
   uint32_t is_intra;
+  uint32_t n_fallback;  /* learned proposal: blocks that needed the exhaustive search */
 } mptc_frame_stats;
 
 /* Replaces the state the reference keeps in DXTImage statics and in the
@@ -174,6 +175,50 @@ mptc_status mptc_batch_encode(mptc_batch *batch, const int32_t *is_intra, void *
  * each stream's intra search. Writes the chosen values (synchronises). */
 mptc_status mptc_batch_autotune(mptc_batch *batch, const int32_t *is_intra, int32_t *inter_warps,
                                 int32_t *intra_ctas, void *stream);
+
+/* ---- Learned candidate proposal (no counterpart in the reference) -------
+ * A block MLP f (54 -> 256 -> 256 -> 64 over the 48 pixel bytes and the stb
+ * endpoints) and a candidate MLP g (32 -> 128 -> 64 over an index word's bits)
+ * score window candidates by f(block) . g(candidate). With a model attached,
+ * the inter search tests only the K best-scored window positions with the
+ * exact error (err_diff <= threshold) and falls back to the exhaustive search
+ * when none passes; the stream stays a valid MPTC stream but is no longer
+ * bit-identical to the reference's. BF16 tensor-core kernels, FP32 accumulate;
+ * trained on the GPU with AdamW on (block, accepted candidate) pairs. */
+typedef struct mptc_model mptc_model;
+int64_t mptc_model_num_params(void);
+mptc_status mptc_model_create(uint64_t seed, mptc_model **out_model);
+mptc_status mptc_model_destroy(mptc_model *model);
+/* Flat fp32 parameter vector (layer weights [in x out] then biases, for f1,
+ * f2, f3, g1, g2; f1's input padded to 64 rows). */
+mptc_status mptc_model_get_params(mptc_model *model, float *host);
+mptc_status mptc_model_set_params(mptc_model *model, const float *host);
+/* One AdamW step on a batch of B blocks of one frame (block indices
+ * blocks_dev) with C candidate index words each (cands_dev, B x C, the
+ * accepted candidate first): sampled softmax cross-entropy. */
+mptc_status mptc_model_train_step(mptc_model *model, const uint8_t *rgb_dev, int32_t width, const uint64_t *stb_dev,
+                                  const uint32_t *blocks_dev, const uint32_t *cands_dev, int32_t B, int32_t C,
+                                  float lr, float weight_decay, float *loss_host, void *stream);
+/* Loss and gradient (flat, like the parameters) of the same objective, no update. */
+mptc_status mptc_model_grads(mptc_model *model, const uint8_t *rgb_dev, int32_t width, const uint64_t *stb_dev,
+                             const uint32_t *blocks_dev, const uint32_t *cands_dev, int32_t B, int32_t C,
+                             float *grads_host, float *loss_host, void *stream);
+/* Embeddings: n_blocks rows of f (blocks_dev NULL = the first n_blocks blocks
+ * in raster order) and n_words rows of g (words_dev[i * word_stride]). */
+mptc_status mptc_model_embed(mptc_model *model, const uint8_t *rgb_dev, int32_t width, const uint64_t *stb_dev,
+                             const uint32_t *blocks_dev, int32_t n_blocks, float *emb_blocks_dev,
+                             const uint32_t *words_dev, int32_t word_stride, int32_t n_words,
+                             float *emb_words_dev, void *stream);
+/* Checkpoint / resume: parameters, AdamW moments and step count. */
+mptc_status mptc_model_save(mptc_model *model, const char *path);
+mptc_status mptc_model_load(mptc_model *model, const char *path);
+/* Attaches (k in 1..16) or detaches (model NULL or k <= 0) a model to a
+ * context's inter search. Needs search_area <= 12. */
+mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k);
+/* Squared error between a frame and the decoded DXT1 blocks (RGB565 endpoints
+ * expanded as a decoder does), into *sse_dev (device u64). */
+mptc_status mptc_decoded_sse(const uint8_t *rgb_dev, int32_t width, int32_t height, const uint64_t *blocks_dev,
+                             uint64_t *sse_dev, void *stream);
 
 /* Counters of the last frame reencoded on this context (synchronises `stream`). */
 mptc_status mptc_last_frame_stats(mptc_ctx *ctx, mptc_frame_stats *out, void *stream);

@@ -21,7 +21,10 @@ EXPORTED = [
     "mptc_version", "mptc_built_arch", "mptc_set_kernel_timing", "mptc_kernel_times",
     "mptc_alu_probe", "mptc_encode_frame_noalloc", "mptc_batch_create", "mptc_batch_destroy",
     "mptc_batch_input", "mptc_batch_output", "mptc_batch_upload", "mptc_batch_fetch",
-    "mptc_batch_encode", "mptc_batch_autotune",
+    "mptc_batch_encode", "mptc_batch_autotune", "mptc_model_num_params", "mptc_model_create",
+    "mptc_model_destroy", "mptc_model_get_params", "mptc_model_set_params", "mptc_model_train_step",
+    "mptc_model_grads", "mptc_model_embed", "mptc_model_save", "mptc_model_load",
+    "mptc_ctx_set_model", "mptc_decoded_sse",
 ]
 
 NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
@@ -34,7 +37,8 @@ class Config(ctypes.Structure):
 
 class FrameStats(ctypes.Structure):
     _fields_ = [("n_inter", ctypes.c_uint32), ("n_intra", ctypes.c_uint32),
-                ("n_unique", ctypes.c_uint32), ("is_intra", ctypes.c_uint32)]
+                ("n_unique", ctypes.c_uint32), ("is_intra", ctypes.c_uint32),
+                ("n_fallback", ctypes.c_uint32)]
 
 
 class KernelTime(ctypes.Structure):
@@ -83,10 +87,25 @@ def lib() -> ctypes.CDLL:
         L.mptc_batch_fetch.argtypes = [vp, i32, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32), vp]
         L.mptc_batch_encode.argtypes = [vp, vp, vp]
         L.mptc_batch_autotune.argtypes = [vp, vp, ctypes.POINTER(i32), ctypes.POINTER(i32), vp]
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.mptc_model_num_params.restype = ctypes.c_int64
+        L.mptc_model_create.argtypes = [ctypes.c_uint64, ctypes.POINTER(vp)]
+        L.mptc_model_destroy.argtypes = [vp]
+        L.mptc_model_get_params.argtypes = [vp, vp]
+        L.mptc_model_set_params.argtypes = [vp, vp]
+        L.mptc_model_train_step.argtypes = [vp, vp, i32, vp, vp, vp, i32, i32, ctypes.c_float,
+                                            ctypes.c_float, fp, vp]
+        L.mptc_model_grads.argtypes = [vp, vp, i32, vp, vp, vp, i32, i32, vp, fp, vp]
+        L.mptc_model_embed.argtypes = [vp, vp, i32, vp, vp, i32, vp, vp, i32, i32, vp, vp]
+        L.mptc_model_save.argtypes = [vp, ctypes.c_char_p]
+        L.mptc_model_load.argtypes = [vp, ctypes.c_char_p]
+        L.mptc_ctx_set_model.argtypes = [vp, vp, i32]
+        L.mptc_decoded_sse.argtypes = [vp, i32, i32, vp, vp, vp]
         L.mptc_version.restype = i32
         L.mptc_built_arch.restype = i32
         for name in EXPORTED:
-            if name not in ("mptc_last_error", "mptc_version", "mptc_built_arch"):
+            if name not in ("mptc_last_error", "mptc_version", "mptc_built_arch",
+                            "mptc_model_num_params"):
                 getattr(L, name).restype = ctypes.c_int
         _LIB = L
     return _LIB

@@ -14,6 +14,8 @@
 #include "../../include/mptc_gb300.h"
 #include "dxt1_encode.cuh"
 #include "search.cuh"
+#include "learned_search.cuh"
+#include "model_internal.h"
 
 namespace {
 
@@ -28,9 +30,15 @@ struct mptc_ctx {
   int device = 0, sm_count = 0, intra_grid = 0;
   // launch shapes (tunable): warps per CTA of the inter search, CTA cap of the intra search
   int inter_warps = kSearchWarps, intra_cap = 0;
+  // learned proposal (optional)
+  const mptc_model *model = nullptr;
+  int topk_k = 0;
+  float *femb = nullptr, *gemb = nullptr;
+  uint16_t *topk = nullptr;
+  mptc_internal::EmbedWorkspace ews;
   // device scratch
   uint32_t *done = nullptr;        // per block
-  uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count
+  uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats, [5] pending, [6] fallbacks, [5] pending count
   uint32_t *order = nullptr;       // blocks in wavefront order
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
   float4 *wdesc = nullptr;         // refit weight sums of the previous frame's blocks
@@ -297,6 +305,10 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->order);
   cudaFree(ctx->pending);
   cudaFree(ctx->wdesc);
+  cudaFree(ctx->femb);
+  cudaFree(ctx->gemb);
+  cudaFree(ctx->topk);
+  mptc_internal::embed_workspace_free(ctx->ews);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -340,7 +352,19 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
     const int w = ctx->inter_warps;
     const int grid = (ctx->nblk + w - 1) / w;
-    if (w == 4)
+    if (ctx->model) {
+      // learned proposal: embeddings, top-K window positions, exact test of the K
+      mptc_status es = mptc_internal::model_embed_frame(ctx->model, ctx->ews, rgb_dev, ctx->width, stb_dev, ctx->nblk,
+                                                        ctx->femb, reinterpret_cast<const uint32_t *>(prev_final_dev) + 1,
+                                                        2, ctx->gemb, s);
+      if (es != MPTC_OK) return fail(ctx, es, "learned proposal: embedding failed");
+      const int sa = ctx->cfg.search_area, uw = mptc::kTileW + 2 * sa - 1, uh = mptc::kTileH + 2 * sa - 1;
+      const int nu8 = (uw * uh + 7) & ~7;
+      const size_t smem = (size_t)nu8 * mptc::kEmb * 2 + 16 * mptc::kEmb * 2 + (size_t)16 * nu8 * 4;
+      dim3 tg((ctx->bw + mptc::kTileW - 1) / mptc::kTileW, (ctx->bh + mptc::kTileH - 1) / mptc::kTileH);
+      mptc::score_topk_kernel<<<tg, 128, smem, s>>>(ctx->femb, ctx->gemb, ctx->bw, ctx->bh, sa, ctx->topk_k, ctx->topk);
+      mptc::learned_inter_kernel<8><<<(ctx->nblk + 7) / 8, 256, 0, s>>>(P, ctx->topk, ctx->topk_k, ctx->work + 6);
+    } else if (w == 4)
       mptc::inter_search_kernel<4><<<grid, 4 * 32, 0, s>>>(P);
     else if (w == 16)
       mptc::inter_search_kernel<16><<<grid, 16 * 32, 0, s>>>(P);
@@ -394,13 +418,14 @@ mptc_status mptc_encode_frame(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint6
 
 mptc_status mptc_last_frame_stats(mptc_ctx *ctx, mptc_frame_stats *out, void *stream) {
   if (!ctx || !out) return MPTC_EINVAL;
-  uint32_t w[5];
+  uint32_t w[7];
   MPTC_CUDA(cudaMemcpyAsync(w, ctx->work, sizeof(w), cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream)));
   MPTC_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
   out->n_inter = w[2];
   out->n_intra = w[3];
   out->n_unique = w[4];
   out->is_intra = ctx->last_is_intra;
+  out->n_fallback = w[6];
   if (w[1] & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
   return MPTC_OK;
 }
@@ -452,6 +477,43 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
   ctx->cur = nxt;
   ctx->have_prev = true;
   return MPTC_OK;
+}
+
+mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k) {
+  if (!ctx) return MPTC_EINVAL;
+  if (!model || k <= 0) {
+    ctx->model = nullptr;
+    ctx->topk_k = 0;
+    return MPTC_OK;
+  }
+  if (k > mptc::kMaxK) return fail(ctx, MPTC_EINVAL, "learned proposal: k above 16");
+  if (ctx->cfg.search_area > 12) return fail(ctx, MPTC_EINVAL, "learned proposal: search area above 12");
+  const size_t n = (size_t)ctx->nblk;
+  if (!ctx->femb) {
+    if (dalloc(&ctx->femb, n * mptc::kEmb) || dalloc(&ctx->gemb, n * mptc::kEmb) || dalloc(&ctx->topk, n * mptc::kMaxK))
+      return fail(ctx, MPTC_ENOMEM, "learned proposal buffers");
+    if (mptc_internal::embed_workspace_alloc(ctx->ews, ctx->nblk) != MPTC_OK)
+      return fail(ctx, MPTC_ENOMEM, "learned proposal workspace");
+    const int sa = ctx->cfg.search_area, uw = mptc::kTileW + 2 * sa - 1, uh = mptc::kTileH + 2 * sa - 1;
+    const int nu8 = (uw * uh + 7) & ~7;
+    const int smem = nu8 * mptc::kEmb * 2 + 16 * mptc::kEmb * 2 + 16 * nu8 * 4;
+    MPTC_CUDA(cudaFuncSetAttribute(mptc::score_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  }
+  ctx->model = model;
+  ctx->topk_k = k;
+  return MPTC_OK;
+}
+
+mptc_status mptc_decoded_sse(const uint8_t *rgb_dev, int32_t width, int32_t height, const uint64_t *blocks_dev,
+                             uint64_t *sse_dev, void *stream) {
+  if (!rgb_dev || !blocks_dev || !sse_dev || width <= 0 || height <= 0 || (width & 3) || (height & 3))
+    return MPTC_EINVAL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int bw = width / 4, n = bw * (height / 4);
+  if (cudaMemsetAsync(sse_dev, 0, sizeof(uint64_t), s) != cudaSuccess) return MPTC_ECUDA;
+  mptc::decoded_sse_kernel<<<std::min((n + 255) / 256, 2048), 256, 0, s>>>(
+      rgb_dev, width, bw, n, blocks_dev, reinterpret_cast<unsigned long long *>(sse_dev));
+  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
 mptc_status mptc_set_kernel_timing(mptc_ctx *ctx, int32_t enable) {

@@ -84,6 +84,11 @@ class Encoder:
         check(lib().mptc_last_frame_stats(self._ctx, ctypes.byref(st), s), self._ctx)
         return st
 
+    def set_model(self, model, k: int = 8) -> None:
+        """Attach a ProposalModel to the inter search (k proposals), or detach (None)."""
+        check(lib().mptc_ctx_set_model(self._ctx, model.handle if model is not None else None,
+                                       int(k) if model is not None else 0), self._ctx)
+
     def set_kernel_timing(self, enable: bool) -> None:
         check(lib().mptc_set_kernel_timing(self._ctx, int(enable)), self._ctx)
 
