@@ -406,6 +406,186 @@ def run_batch(args, rank: int, world: int, dist) -> None:
     b.close()
 
 
+def adaptive_code_bits(symbols: np.ndarray, alphabet: int) -> float:
+    """Code length of an adaptive order-0 model whose counts start at 1:
+    log2(A (A+1) ... (A+N-1)) - sum_s log2(n_s!), in closed form."""
+    from math import lgamma, log
+    n = np.bincount(np.asarray(symbols, np.int64), minlength=alphabet).astype(np.float64)
+    N = float(n.sum())
+    nats = lgamma(alphabet + N) - lgamma(alphabet) - float(sum(lgamma(c + 1.0) for c in n if c > 0))
+    return nats / log(2.0)
+
+
+def encode_stream_quality(torch, enc, frames_dev, sched, W_, H_):
+    """Encodes a stream once (device API) and returns per-frame decoded SSE,
+    motion-code + palette adaptive code length (bits) and stats."""
+    import ctypes
+    from mptc_gb300._lib import check, lib
+    n = (W_ // 4) * (H_ // 4)
+    dev = frames_dev.device
+    fin = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(2)]
+    stb = torch.empty(n, dtype=torch.int64, device=dev)
+    mot = torch.empty(2 * n, dtype=torch.uint8, device=dev)
+    uni = torch.empty(n, dtype=torch.int32, device=dev)
+    nu = torch.zeros(1, dtype=torch.int32, device=dev)
+    sse = torch.zeros(1, dtype=torch.int64, device=dev)
+    out = dict(sse=[], bits=[], unique=[], fallback=0, inter=0)
+    for f in range(frames_dev.shape[0]):
+        prev = None if sched[f] else fin[(f - 1) % 2]
+        enc.encode_frame_device(frames_dev[f], prev, stb, fin[f % 2], mot, uni, nu)
+        check(lib().mptc_decoded_sse(frames_dev[f].data_ptr(), W_, H_, fin[f % 2].data_ptr(), sse.data_ptr(),
+                                     ctypes.c_void_p(0)))
+        st = enc.stats()
+        out["sse"].append(int(sse.item()))
+        m = mot.cpu().numpy()
+        k = int(nu.item())
+        pal = uni[:k].cpu().numpy().view(np.uint8)
+        out["bits"].append(adaptive_code_bits(m.astype(np.int64), 256) + adaptive_code_bits(pal.astype(np.int64), 256))
+        out["unique"].append(k)
+        out["fallback"] += st.n_fallback
+        out["inter"] += st.n_inter
+    return out
+
+
+def psnr_db(sse_list, W_, H_):
+    return float(np.mean([10.0 * np.log10(3.0 * 255.0 ** 2 / (s / (W_ * H_))) for s in sse_list]))
+
+
+def run_learned(args, rank: int, world: int, dist) -> None:
+    """Learned proposal vs exhaustive search on the 1080p stream: trains on 200
+    separate seeded frames with the library's kernels, then times both forms
+    (single stream, or --batch S concurrent streams) and compares decoded
+    PSNR and the motion/palette code length on the same 120 frames."""
+    import torch
+
+    from mptc_gb300.batch import BatchEncoder
+    from mptc_gb300.encoder import Encoder
+    from mptc_gb300.synth import FHD1080, FHD1080_TRAIN
+    from mptc_gb300.training import train_proposal
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t0 = time.time()
+    train_dev = torch.from_numpy(FHD1080_TRAIN.generate()).to(dev)
+    log(f"[rank {rank}] training frames in {time.time() - t0:.1f}s")
+    t0 = time.time()
+    model, losses = train_proposal(torch, train_dev, SA, THR, II, steps=args.train_steps, batch=4096, cands=16,
+                                   lr=1e-3, log=log if rank == 0 else None)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    del train_dev
+    nf = args.frames
+    frames_dev = torch.from_numpy(FHD1080.generate(0, nf)).to(dev)
+    sched = intra_schedule(nf, II)
+    # quality: the same stream through both forms
+    plain_enc = Encoder(W, H, SA, THR, II)
+    learned_enc = Encoder(W, H, SA, THR, II)
+    learned_enc.set_model(model, args.topk)
+    qp = encode_stream_quality(torch, plain_enc, frames_dev, sched, W, H)
+    ql = encode_stream_quality(torch, learned_enc, frames_dev, sched, W, H)
+    n = (W // 4) * (H // 4)
+    inter_blocks = sum(1 for f in sched if not f) * n
+
+    def time_single(enc):
+        fin = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(2)]
+        stb = torch.empty(n, dtype=torch.int64, device=dev)
+        mot = torch.empty(2 * n, dtype=torch.uint8, device=dev)
+        uni = torch.empty(n, dtype=torch.int32, device=dev)
+        nu = torch.zeros(1, dtype=torch.int32, device=dev)
+        s = torch.cuda.current_stream()
+
+        def step():
+            for f in range(nf):
+                prev = None if sched[f] else fin[(f - 1) % 2]
+                enc.encode_frame_device(frames_dev[f], prev, stb, fin[f % 2], mot, uni, nu, s)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(args.steps):
+            step()
+        e1.record(s)
+        torch.cuda.synchronize()
+        return nf * args.steps / (e0.elapsed_time(e1) * 1e-3)
+
+    def time_batch(S, with_model):
+        b = BatchEncoder([(W, H)] * S, SA, THR, II)
+        if with_model:
+            b.set_model(model, args.topk)
+        offsets = [(15 * k) % nf for k in range(S)]
+        phases = [(II * k) // S for k in range(S)]
+        s = torch.cuda.current_stream()
+
+        def flags(f):
+            return [f == 0 or (f - phases[k]) % II == 0 for k in range(S)]
+
+        def step():
+            for f in range(nf):
+                for k in range(S):
+                    b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
+                b.encode(flags(f), s)
+        for f in range(2):
+            for k in range(S):
+                b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
+            b.encode(flags(f), s)
+        b.autotune(flags(2), s)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(args.steps):
+            step()
+        e1.record(s)
+        torch.cuda.synchronize()
+        b.fetch(0)
+        b.close()
+        return S * nf * args.steps / (e0.elapsed_time(e1) * 1e-3)
+
+    clk = ClockSampler(local)
+    plain_fps = time_single(plain_enc)
+    learned_fps = time_single(learned_enc)
+    S = args.batch
+    plain_b = time_batch(S, False) if S > 0 else None
+    learned_b = time_batch(S, True) if S > 0 else None
+    clocks = clk.stop()
+    value = learned_b if S > 0 else learned_fps
+    base = plain_fps
+    bits_p, bits_l = sum(qp["bits"]), sum(ql["bits"])
+    if rank == 0:
+        cfg = workload_config()
+        cfg.update({"workload": ("learned proposal + batching" if S > 0 else "learned proposal") +
+                                f" on the 1080p stream ({S or 1} stream(s) x {nf} frames); top-K {args.topk}",
+                    "search": f"learned top-{args.topk} proposals, exact test, exhaustive fallback",
+                    "streams_per_gpu": S or 1,
+                    "train": {"frames": 200, "steps": args.train_steps, "batch_blocks": 4096,
+                              "candidates_per_block": 16, "optimizer": "AdamW lr 1e-3",
+                              "loss_first": round(losses[0], 4), "loss_last": round(losses[-1], 4),
+                              "seconds": round(train_s, 1)}})
+        line = dict(metric=METRIC, value=round(value, 3), unit="frames/s", n_gpus=world, steps=args.steps,
+                    warmup=args.warmup, ms_per_step=round(1000.0 * nf * (S or 1) / value, 3),
+                    higher_is_better=True, scaling="weak", vs_baseline=None, dtype="bf16+fp32+int32",
+                    data="synthetic", config=cfg, clocks=clocks,
+                    comparison={"plain_single_fps": round(plain_fps, 2), "learned_single_fps": round(learned_fps, 2),
+                                "plain_batched_fps": round(plain_b, 2) if plain_b else None,
+                                "learned_batched_fps": round(learned_b, 2) if learned_b else None,
+                                "speedup_vs_plain_single": round(value / base, 3),
+                                "psnr_plain_db": round(psnr_db(qp["sse"], W, H), 4),
+                                "psnr_learned_db": round(psnr_db(ql["sse"], W, H), 4),
+                                "psnr_delta_db": round(psnr_db(ql["sse"], W, H) - psnr_db(qp["sse"], W, H), 4),
+                                "motion_palette_bits_plain": int(bits_p), "motion_palette_bits_learned": int(bits_l),
+                                "motion_palette_bits_delta": round(bits_l / bits_p - 1.0, 5),
+                                "unique_blocks_plain": int(sum(qp["unique"])),
+                                "unique_blocks_learned": int(sum(ql["unique"])),
+                                "fallback_rate": round(ql["fallback"] / max(1, inter_blocks), 4)})
+        print(json.dumps(line), flush=True)
+    plain_enc.close()
+    learned_enc.close()
+    model.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -416,6 +596,10 @@ def main() -> None:
                     help="frames per step (profiling runs use a short prefix of the stream)")
     ap.add_argument("--batch", type=int, default=0,
                     help="S > 0: S concurrent 1080p streams per GPU through the batched encoder")
+    ap.add_argument("--learned", action="store_true",
+                    help="learned proposal: train on 200 separate seeded frames, then time plain vs learned")
+    ap.add_argument("--train-steps", type=int, default=600)
+    ap.add_argument("--topk", type=int, default=8)
     ap.add_argument("--quick", action="store_true",
                     help="device-timed region only: no e2e pass, CPU baseline or ALU probe (profiling)")
     args = ap.parse_args()
@@ -431,7 +615,9 @@ def main() -> None:
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         tdist.init_process_group("nccl")
         dist = tdist
-    if args.batch > 0:
+    if args.learned:
+        run_learned(args, rank, world, dist)
+    elif args.batch > 0:
         run_batch(args, rank, world, dist)
     else:
         run_gpu(args, rank, world, dist)

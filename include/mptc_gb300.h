@@ -215,6 +215,8 @@ mptc_status mptc_model_load(mptc_model *model, const char *path);
 /* Attaches (k in 1..16) or detaches (model NULL or k <= 0) a model to a
  * context's inter search. Needs search_area <= 12. */
 mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k);
+/* Attaches (or detaches) a model to every stream of a batch. */
+mptc_status mptc_batch_set_model(mptc_batch *batch, const mptc_model *model, int32_t k);
 /* Squared error between a frame and the decoded DXT1 blocks (RGB565 endpoints
  * expanded as a decoder does), into *sse_dev (device u64). */
 mptc_status mptc_decoded_sse(const uint8_t *rgb_dev, int32_t width, int32_t height, const uint64_t *blocks_dev,

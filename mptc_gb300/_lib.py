@@ -24,7 +24,7 @@ EXPORTED = [
     "mptc_batch_encode", "mptc_batch_autotune", "mptc_model_num_params", "mptc_model_create",
     "mptc_model_destroy", "mptc_model_get_params", "mptc_model_set_params", "mptc_model_train_step",
     "mptc_model_grads", "mptc_model_embed", "mptc_model_save", "mptc_model_load",
-    "mptc_ctx_set_model", "mptc_decoded_sse",
+    "mptc_ctx_set_model", "mptc_decoded_sse", "mptc_batch_set_model",
 ]
 
 NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
@@ -101,6 +101,7 @@ def lib() -> ctypes.CDLL:
         L.mptc_model_load.argtypes = [vp, ctypes.c_char_p]
         L.mptc_ctx_set_model.argtypes = [vp, vp, i32]
         L.mptc_decoded_sse.argtypes = [vp, i32, i32, vp, vp, vp]
+        L.mptc_batch_set_model.argtypes = [vp, vp, i32]
         L.mptc_version.restype = i32
         L.mptc_built_arch.restype = i32
         for name in EXPORTED:

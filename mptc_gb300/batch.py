@@ -40,6 +40,10 @@ class BatchEncoder:
         except Exception:
             pass
 
+    def set_model(self, model, k: int = 8) -> None:
+        check(lib().mptc_batch_set_model(self._b, model.handle if model is not None else None,
+                                         int(k) if model is not None else 0))
+
     def nblk(self, i: int) -> int:
         return (self.sizes[i][0] // 4) * (self.sizes[i][1] // 4)
 

@@ -18,8 +18,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
                                                         float *__restrict__ C, __nv_bfloat16 *__restrict__ Cb,
                                                         int ldc, const float *__restrict__ bias, int M, int N, int K,
                                                         int relu, int accumulate) {
-  __shared__ __nv_bfloat16 As[kGBM][kGBK + 8];
-  __shared__ __nv_bfloat16 Bs[kGBN][kGBK + 8];  // stored [n][k]
+  __shared__ __align__(16) __nv_bfloat16 As[kGBM][kGBK + 8];
+  __shared__ __align__(16) __nv_bfloat16 Bs[kGBN][kGBK + 8];  // stored [n][k]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = lane >> 2, t = lane & 3;
   const int m0 = blockIdx.y * kGBM, n0 = blockIdx.x * kGBN;
@@ -33,17 +33,38 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
       for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
   for (int k0 = 0; k0 < K; k0 += kGBK) {
-    for (int e = tid; e < kGBM * kGBK; e += 128) {
-      const int r = e / kGBK, c = e % kGBK, m = m0 + r, k = k0 + c;
-      __nv_bfloat16 v = zero;
-      if (m < M && k < K) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
-      As[r][c] = v;
+    // tiles with k contiguous in memory move as 16-byte vectors when aligned
+    const bool avec = !TA && (lda % 8 == 0) && (k0 + kGBK <= K) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+    const bool bvec = TB && (ldb % 8 == 0) && (k0 + kGBK <= K) && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
+    if (avec) {
+      for (int e = tid; e < kGBM * kGBK / 8; e += 128) {
+        const int r = e / (kGBK / 8), c = 8 * (e % (kGBK / 8)), m = m0 + r;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (m < M) v = *reinterpret_cast<const uint4 *>(A + (size_t)m * lda + k0 + c);
+        *reinterpret_cast<uint4 *>(&As[r][c]) = v;
+      }
+    } else {
+      for (int e = tid; e < kGBM * kGBK; e += 128) {
+        const int r = e / kGBK, c = e % kGBK, m = m0 + r, k = k0 + c;
+        __nv_bfloat16 v = zero;
+        if (m < M && k < K) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+        As[r][c] = v;
+      }
     }
-    for (int e = tid; e < kGBN * kGBK; e += 128) {
-      const int r = e / kGBK, c = e % kGBK, n = n0 + r, k = k0 + c;
-      __nv_bfloat16 v = zero;
-      if (n < N && k < K) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
-      Bs[r][c] = v;
+    if (bvec) {
+      for (int e = tid; e < kGBN * kGBK / 8; e += 128) {
+        const int r = e / (kGBK / 8), c = 8 * (e % (kGBK / 8)), n = n0 + r;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (n < N) v = *reinterpret_cast<const uint4 *>(B + (size_t)n * ldb + k0 + c);
+        *reinterpret_cast<uint4 *>(&Bs[r][c]) = v;
+      }
+    } else {
+      for (int e = tid; e < kGBN * kGBK; e += 128) {
+        const int r = e / kGBK, c = e % kGBK, n = n0 + r, k = k0 + c;
+        __nv_bfloat16 v = zero;
+        if (n < N && k < K) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
+        Bs[r][c] = v;
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -125,6 +146,14 @@ __global__ void cand_features_kernel(const uint32_t *__restrict__ words, int wor
 __global__ void relu_backward_kernel(float *__restrict__ d, const float *__restrict__ h, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     if (!(h[i] > 0.f)) d[i] = 0.f;
+}
+
+// Transposed bf16 copy: y[c][r] = bf16(x[r][c]) for an R x C fp32 matrix.
+__global__ void transpose_bf16_kernel(const float *__restrict__ x, int R, int C, __nv_bfloat16 *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < R * C; i += gridDim.x * blockDim.x) {
+    const int r = i / C, c = i - r * C;
+    y[(size_t)c * R + r] = __float2bfloat16(x[i]);
+  }
 }
 
 __global__ void to_bf16_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ y, int n) {

@@ -115,8 +115,8 @@ __global__ void __launch_bounds__(128) score_topk_kernel(const float *__restrict
 }
 
 // Learned inter search: one warp per block. Lanes 0..K-1 test the K proposed
-// window positions with the exact integer error; the passing proposal with the
-// smallest err_diff (ties: the better-scored) is accepted. When none passes,
+// window positions with the exact integer error; the proposal with the
+// smallest err_diff <= 0 (ties: the better-scored) is accepted. When none is,
 // the warp runs the exhaustive inter search with the reference's selection
 // rule. Accepted blocks become final; the others are left for the intra pass.
 template <int WARPS>
@@ -152,7 +152,10 @@ __global__ void __launch_bounds__(WARPS * 32) learned_inter_kernel(SearchParams 
         e = eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
       }
     }
-    const bool pass = e != kInvalid && e <= P.thr;
+    // A proposal is taken only when it is no worse than the block's own stb
+    // encoding (err_diff <= 0, the outcome the reference's search prefers); the
+    // others go to the exhaustive search, which keeps the decoded quality.
+    const bool pass = e != kInvalid && e <= 0 && e <= P.thr;
     const int key = pass ? ((e + 0x10000) << 8) | lane : 0x7fffffff;  // min err_diff, then best score
     const int best = __reduce_min_sync(kFull, key);
     int sel_pos, sel_refit;

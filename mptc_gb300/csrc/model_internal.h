@@ -14,6 +14,7 @@ struct EmbedWorkspace {
   int cap = 0;
   __nv_bfloat16 *x = nullptr, *h1b = nullptr, *h2b = nullptr;
   float *h1 = nullptr, *h2 = nullptr;
+  __nv_bfloat16 *wt = nullptr;  // transposed bf16 weights of the current model
 };
 
 mptc_status embed_workspace_alloc(EmbedWorkspace &ws, int rows);

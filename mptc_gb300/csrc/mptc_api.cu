@@ -879,6 +879,16 @@ mptc_status mptc_batch_encode(mptc_batch *b, const int32_t *is_intra, void *stre
   return MPTC_OK;
 }
 
+mptc_status mptc_batch_set_model(mptc_batch *b, const mptc_model *model, int32_t k) {
+  if (!b) return MPTC_EINVAL;
+  for (auto c : b->ctx) {
+    mptc_status st = mptc_ctx_set_model(c, model, k);
+    if (st != MPTC_OK) return st;
+  }
+  batch_clear_graphs(b);
+  return MPTC_OK;
+}
+
 mptc_status mptc_batch_autotune(mptc_batch *b, const int32_t *is_intra, int32_t *inter_warps, int32_t *intra_ctas,
                                 void *stream) {
   if (!b || !is_intra) return MPTC_EINVAL;

@@ -373,7 +373,7 @@ mptc_status embed_workspace_alloc(EmbedWorkspace &ws, int rows) {
   embed_workspace_free(ws);
   const size_t r = (size_t)rows;
   if (dmalloc(&ws.x, r * kFeatPad) || dmalloc(&ws.h1b, r * kH1) || dmalloc(&ws.h2b, r * kH2) ||
-      dmalloc(&ws.h1, r * kH1) || dmalloc(&ws.h2, r * kH2)) {
+      dmalloc(&ws.h1, r * kH1) || dmalloc(&ws.h2, r * kH2) || dmalloc(&ws.wt, kOff.total)) {
     embed_workspace_free(ws);
     return MPTC_ENOMEM;
   }
@@ -387,6 +387,7 @@ void embed_workspace_free(EmbedWorkspace &ws) {
   cudaFree(ws.h2b);
   cudaFree(ws.h1);
   cudaFree(ws.h2);
+  cudaFree(ws.wt);
   ws = EmbedWorkspace{};
 }
 
@@ -395,20 +396,30 @@ mptc_status model_embed_frame(const mptc_model *m, EmbedWorkspace &ws, const uin
                               float *G, cudaStream_t s) {
   using namespace mptc;
   if (!m || n > ws.cap) return MPTC_EINVAL;
-  const bf16 *W[5];
+  // transposed bf16 weights ([out x in]) so both GEMM operands load as
+  // contiguous 16-byte vectors along k
+  const bf16 *Wt[5];
   const float *b[5];
   for (int l = 0; l < 5; ++l) {
-    W[l] = m->wb + kOff.w[l];
+    const size_t cnt = (size_t)kLayers[l].in * kLayers[l].out;
+    transpose_bf16_kernel<<<blocks_for(cnt), 256, 0, s>>>(m->w + kOff.w[l], kLayers[l].in, kLayers[l].out,
+                                                          ws.wt + kOff.w[l]);
+    Wt[l] = ws.wt + kOff.w[l];
     b[l] = m->w + kOff.b[l];
   }
+  auto fwd = [&](const bf16 *x, int l, float *y, bf16 *yb, bool relu) {
+    const int K = kLayers[l].in, N = kLayers[l].out;
+    dim3 grid((N + kGBN - 1) / kGBN, (n + kGBM - 1) / kGBM);
+    gemm_bf16_kernel<false, true><<<grid, 128, 0, s>>>(x, K, Wt[l], K, y, yb, N, b[l], n, N, K, relu ? 1 : 0, 0);
+  };
   block_features_kernel<<<blocks_for((size_t)n * kFeatPad), 256, 0, s>>>(rgb, width, width / 4, stb, nullptr, n, ws.x);
-  gemm_fwd(ws.x, W[0], b[0], ws.h1, ws.h1b, n, kFeatPad, kH1, true, s);
-  gemm_fwd(ws.h1b, W[1], b[1], ws.h2, ws.h2b, n, kH1, kH2, true, s);
-  gemm_fwd(ws.h2b, W[2], b[2], F, nullptr, n, kH2, kEmb, false, s);
+  fwd(ws.x, 0, ws.h1, ws.h1b, true);
+  fwd(ws.h1b, 1, ws.h2, ws.h2b, true);
+  fwd(ws.h2b, 2, F, nullptr, false);
   // candidate MLP: reuse x (n x 32 fits in n x 64) and h1 (n x 128 fits in n x 256)
   cand_features_kernel<<<blocks_for((size_t)n * kCandIn), 256, 0, s>>>(words, word_stride, n, ws.x);
-  gemm_fwd(ws.x, W[3], b[3], ws.h1, ws.h1b, n, kCandIn, kCandH, true, s);
-  gemm_fwd(ws.h1b, W[4], b[4], G, nullptr, n, kCandH, kEmb, false, s);
+  fwd(ws.x, 3, ws.h1, ws.h1b, true);
+  fwd(ws.h1b, 4, G, nullptr, false);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
