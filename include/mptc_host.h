@@ -1,0 +1,65 @@
+/*
+ * mptc_host — host-side MPTC stream writer (no GPU): turns the arrays the
+ * encoder returns per frame (final DXT1 blocks, motion codes, unique index
+ * palette) into the MPTC container bytes, exactly as the reference encoder's
+ * CompressMultiUnique (codec/codec.cpp:1307-1532) writes them:
+ *
+ *   header (34 bytes): u32 height, u32 width, u8 unique_interval,
+ *     u8 search_area, u32 groups (= frames / unique_interval), then u32
+ *     max_unique_count, max_compressed_palette, max_compressed_motion_indices,
+ *     max_compressed_ep_Y, max_compressed_ep_C (patched when the stream ends);
+ *   per group of unique_interval frames: u32 palette_size, the arithmetic-coded
+ *     palette bytes of the group, u32 palette byte count, then every frame record;
+ *   frame record (EntropyEncode, codec/codec.cpp:1115-1158): u32 n_unique,
+ *     u32 motion_size, arithmetic-coded motion codes (x then y per block), then
+ *     the endpoint images (CompressEndpoint, :804-899): for ep1 then ep2,
+ *     RGB565 -> YCoCg-667, a 6-level integer 5/3 wavelet per 64x64 tile and
+ *     per plane, coefficients + 128, arithmetic coding of the Y plane and of
+ *     the Co plane followed by the Cg plane, each with a u32 size prefix.
+ *
+ * Like the reference, frames after the last complete group are coded (they
+ * count towards the maximum sizes) but not written, and the endpoint images
+ * must be multiples of 64 blocks in each direction (frame sizes multiples of
+ * 256 pixels): other sizes are rejected here, where the reference would write
+ * out of bounds.
+ */
+#ifndef MPTC_HOST_H_
+#define MPTC_HOST_H_
+
+#include <stdint.h>
+
+#include "mptc_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mptc_stream_writer mptc_stream_writer;
+
+/* `total_frames` is the number of frames the caller will add (it fixes the
+ * header's group count, codec/codec.cpp:1357). */
+mptc_status mptc_stream_writer_create(int32_t width, int32_t height, int32_t search_area,
+                                      int32_t unique_interval, int32_t total_frames,
+                                      mptc_stream_writer **out_writer);
+mptc_status mptc_stream_writer_destroy(mptc_stream_writer *writer);
+
+/* One encoded frame: blocks (width/4 * height/4 u64, the final physical
+ * blocks), motion (2 bytes per block), the unique palette and its length. */
+mptc_status mptc_stream_writer_add_frame(mptc_stream_writer *writer, const uint64_t *final_blocks,
+                                         const uint8_t *motion, const uint32_t *unique_palette,
+                                         uint32_t n_unique);
+
+/* Finishes the stream: *size receives its byte count; if `out` is not NULL
+ * (room for *size bytes when called with out == NULL first) the bytes are
+ * copied there. Frame record sizes of the last frame: optional. */
+mptc_status mptc_stream_writer_finish(mptc_stream_writer *writer, uint8_t *out, uint64_t *size);
+
+/* Sizes in bytes of the last added frame's coded parts: motion codes, the four
+ * endpoint streams (Y1, C1, Y2, C2). Any pointer may be NULL. */
+mptc_status mptc_stream_writer_frame_sizes(const mptc_stream_writer *writer, uint32_t *motion_bytes,
+                                           uint32_t *endpoint_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

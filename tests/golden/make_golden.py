@@ -9,7 +9,11 @@ synthetic streams and on adversarial block patterns, and records:
                        motion codes and unique palette, plus PSNR, for each
                        case (inputs are regenerated from the integer-exact
                        synthetic generator, so only hashes are stored);
-* ``adversarial.npz``  full input frames and outputs of the adversarial case.
+* ``adversarial.npz``  full input frames and outputs of the adversarial case;
+* ``golden.json["streams"]``  SHA-256 and size of whole MPTC streams written
+                       by the unmodified reference encoder (``CompressMultiUnique``
+                       via ``oracle/_ref/mptc_encoder``, fed PNG frames), which
+                       pin the host stream writer byte for byte.
 
 Usage (needs the reference sources; run from the repository root):
     make -C oracle/ref REF=<path to MPTC>
@@ -22,7 +26,9 @@ import json
 import os
 import subprocess
 import sys
+import struct
 import tempfile
+import zlib
 
 import numpy as np
 
@@ -32,6 +38,7 @@ sys.path.insert(0, ROOT)
 from mptc_gb300.synth import HD720, FHD1080, SMOKE_256, StreamSpec  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "hotpath_harness")
+ENCODER = os.path.join(ROOT, "oracle", "_ref", "mptc_encoder")
 OUT_DIR = os.path.dirname(os.path.abspath(__file__))
 
 # (name, spec, first frame, frame count, search_area, threshold, intra_interval)
@@ -47,6 +54,16 @@ CASES = [
     ("small200x52_sa3_thr2", StreamSpec(200, 52, 5, seed=12, square_size=24), 0, 5, 3, 2, 3),
     ("hd720_cut_sa8_thr5", HD720, 30, 4, 8, 5, 16),
     ("fhd1080_sa8_thr5", FHD1080, 0, 2, 8, 5, 16),
+]
+
+
+# (name, spec, first frame, frame count, search_area, threshold, intra_interval,
+#  unique_interval): whole streams; frame sizes are multiples of 256 pixels.
+STREAM_CASES = [
+    ("stream256_sa8_thr5_ii16_ui8", SMOKE_256, 0, 16, 8, 5, 16, 8),
+    ("stream256_sa4_thr0_ii4_ui3_tail", SMOKE_256, 0, 8, 4, 0, 4, 3),
+    ("stream512x256_sa2_thr20_ii2_ui1", StreamSpec(512, 256, 4, seed=21, n_squares=3), 0, 4, 2, 20, 2, 1),
+    ("stream256x512_sa16_thr5_ii8_ui4", StreamSpec(256, 512, 4, seed=22, cut_every=3), 0, 4, 16, 5, 8, 4),
 ]
 
 
@@ -133,6 +150,38 @@ def run_reference(frames: np.ndarray, sa: int, thr: int, ii: int):
     return res
 
 
+def write_png(path: str, rgb: np.ndarray) -> None:
+    """8-bit RGB PNG, filter 0 on every row (lossless; any decoder reads it back)."""
+    h, w, _ = rgb.shape
+    raw = b"".join(b"\x00" + rgb[y].tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data))
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
+
+
+def run_reference_stream(frames: np.ndarray, sa: int, thr: int, ii: int, ui: int) -> bytes:
+    """Stream bytes of the reference encoder (codec/encoder.cpp main ->
+    CompressMultiUnique) over PNG frames named in display order."""
+    with tempfile.TemporaryDirectory() as td:
+        fdir = os.path.join(td, "frames")
+        os.makedirs(fdir)
+        for i, f in enumerate(frames):
+            write_png(os.path.join(fdir, f"frame{i:05d}.png"), np.ascontiguousarray(f))
+        out = os.path.join(td, "stream.mptc")
+        os.makedirs(os.path.join(td, "dec"))
+        os.makedirs(os.path.join(td, "ep"))
+        subprocess.check_call([ENCODER, str(sa), str(ii), str(ui), str(thr), "1", fdir, out,
+                               os.path.join(td, "dec"), os.path.join(td, "ep")],
+                              cwd=td, stdout=subprocess.DEVNULL)
+        return open(out, "rb").read()
+
+
 def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
@@ -172,6 +221,16 @@ def main() -> None:
                             psnr=np.array([r["psnr"] for r in res]),
                             params=np.array([sa, thr, ii]))
         print(key, [r["unique"].size for r in res])
+    golden["streams"] = []
+    for name, spec, first, count, sa, thr, ii, ui in STREAM_CASES:
+        frames = spec.generate(first, count)
+        data = run_reference_stream(frames, sa, thr, ii, ui)
+        golden["streams"].append(dict(
+            name=name, spec=spec.__dict__, first=first, count=count, search_area=sa,
+            threshold=thr, intra_interval=ii, unique_interval=ui,
+            input_sha=[sha(f) for f in frames], size=len(data),
+            sha=hashlib.sha256(data).hexdigest(), header=data[:34].hex()))
+        print(name, len(data))
     with open(os.path.join(OUT_DIR, "golden.json"), "w") as f:
         json.dump(golden, f, indent=1)
 

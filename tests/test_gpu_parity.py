@@ -57,6 +57,24 @@ def test_gpu_matches_reference_golden(torch_cuda, case):
         assert sha(uni) == g["unique"], f"frame {k}: unique palette"
 
 
+STREAMS = json.load(open(os.path.join(GOLDEN, "golden.json")))["streams"]
+
+
+@pytest.mark.parametrize("case", STREAMS, ids=[c["name"] for c in STREAMS])
+def test_gpu_stream_bytes_match_reference(torch_cuda, case):
+    """CUDA encoder arrays -> host stream writer -> the reference encoder's
+    stream, byte for byte."""
+    from mptc_gb300.stream import write_stream
+    spec = StreamSpec(**case["spec"])
+    frames = spec.generate(case["first"], case["count"])
+    outs = gpu_stream(frames, case["search_area"], case["threshold"], case["intra_interval"],
+                      want_stb=False)
+    data = write_stream([o[1:] for o in outs], spec.width, spec.height, case["search_area"],
+                        case["unique_interval"])
+    assert len(data) == case["size"]
+    assert hashlib.sha256(data).hexdigest() == case["sha"]
+
+
 @pytest.mark.parametrize("key", ["adv_sa4_thr5_ii16", "adv_sa2_thr0_ii1"])
 def test_gpu_matches_reference_adversarial(torch_cuda, key):
     z = np.load(os.path.join(GOLDEN, f"{key}.npz"))

@@ -1,0 +1,107 @@
+"""Host stream writer (include/mptc_host.h) against whole MPTC streams written
+by the reference encoder (golden.json "streams": SHA-256 of the bytes of
+CompressMultiUnique, codec/codec.cpp:1307-1532, over the same frames).
+
+The frame arrays fed to the writer come from the oracle here; the GPU test in
+test_gpu_parity.py feeds the CUDA encoder's arrays to the same writer."""
+import hashlib
+import json
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import oracle
+from mptc_gb300.stream import StreamWriter, write_stream
+from mptc_gb300.synth import StreamSpec
+from mptc_gb300._lib import MptcError
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+STREAMS = json.load(open(os.path.join(GOLDEN, "golden.json")))["streams"]
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("case", STREAMS, ids=[c["name"] for c in STREAMS])
+def test_oracle_arrays_give_reference_stream(case):
+    spec = StreamSpec(**case["spec"])
+    frames = spec.generate(case["first"], case["count"])
+    assert [sha(f) for f in frames] == case["input_sha"]
+    res = oracle.encode_stream(frames, case["search_area"], case["threshold"],
+                               case["intra_interval"], threads=os.cpu_count() or 1, want_psnr=False)
+    data = write_stream(res, spec.width, spec.height, case["search_area"], case["unique_interval"])
+    assert data[:34].hex() == case["header"]
+    assert len(data) == case["size"]
+    assert hashlib.sha256(data).hexdigest() == case["sha"]
+
+
+def test_header_fields_and_group_layout():
+    """Header per codec/codec.cpp:1354-1367 and :1514-1520; one group record
+    per unique_interval frames, trailing frames left out."""
+    w, h, n = 256, 256, 5
+    nb = (w // 4) * (h // 4)
+    rng = np.random.default_rng(3)
+    final = rng.integers(0, 2**63, nb, dtype=np.uint64)
+    motion = np.full(2 * nb, 255, np.uint8)
+    uniq = np.arange(7, dtype=np.uint32)
+    sw = StreamWriter(w, h, 300 % 64, 2, n)  # search area fits a byte
+    for _ in range(n):
+        sw.add_frame(final, motion, uniq)
+    mb, ep = sw.frame_sizes()
+    data = sw.finish()
+    sw.close()
+    hh, ww, ui, sa, groups = struct.unpack_from("<IIBBI", data, 0)
+    assert (hh, ww, ui, sa, groups) == (h, w, 2, 300 % 64, n // 2)
+    max_unique, max_pal, max_mo, max_y, max_c = struct.unpack_from("<5I", data, 14)
+    assert max_unique == 2 * 4 * uniq.size  # palette BYTES of a group
+    assert max_mo == mb and max_y == max(ep[0], ep[2]) and max_c == max(ep[1], ep[3])
+    # walk the groups: [u32 palette size][palette][u32 count][2 frame records]
+    off = 34
+    for _ in range(groups):
+        (psz,) = struct.unpack_from("<I", data, off)
+        assert psz <= max_pal
+        off += 4 + psz
+        (cnt,) = struct.unpack_from("<I", data, off)
+        assert cnt == 2 * 4 * uniq.size
+        off += 4
+        for _ in range(2):
+            nu, msz = struct.unpack_from("<II", data, off)
+            assert nu == uniq.size and msz == mb
+            off += 8 + msz
+            for k in range(4):
+                (esz,) = struct.unpack_from("<I", data, off)
+                assert esz == ep[k]
+                off += 4 + esz
+    assert off == len(data)
+
+
+def test_constant_input_codes_small_and_deterministic():
+    w = h = 256
+    nb = (w // 4) * (h // 4)
+    final = np.full(nb, 0xAAAAAAAA_F800001F, np.uint64)
+    motion = np.zeros(2 * nb, np.uint8)
+    a = write_stream([(final, motion, np.zeros(0, np.uint32))] * 2, w, h, 8, 1)
+    b = write_stream([(final, motion, np.zeros(0, np.uint32))] * 2, w, h, 8, 1)
+    assert a == b
+    assert len(a) < 34 + 2 * 2000
+
+
+@pytest.mark.parametrize("w,h,sa,ui,n", [(255, 256, 8, 1, 1), (256, 320, 8, 1, 1), (256, 256, 0, 1, 1),
+                                          (256, 256, 64, 1, 1), (256, 256, 8, 0, 1),
+                                          (256, 256, 8, 256, 1), (256, 256, 8, 1, -1)])
+def test_writer_rejects_bad_parameters(w, h, sa, ui, n):
+    with pytest.raises(MptcError):
+        StreamWriter(w, h, sa, ui, n)
+
+
+def test_writer_rejects_mismatched_arrays():
+    sw = StreamWriter(256, 256, 8, 1, 1)
+    nb = 64 * 64
+    with pytest.raises(ValueError):
+        sw.add_frame(np.zeros(nb - 1, np.uint64), np.zeros(2 * nb, np.uint8), np.zeros(0, np.uint32))
+    with pytest.raises(MptcError):
+        sw.add_frame(np.zeros(nb, np.uint64), np.zeros(2 * nb, np.uint8), np.zeros(nb + 1, np.uint32))
+    sw.close()
