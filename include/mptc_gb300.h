@@ -244,6 +244,44 @@ mptc_status mptc_kernel_times(mptc_ctx *ctx, mptc_kernel_time *out, int32_t max_
  * per launch in *ops (2 ops per pair). */
 mptc_status mptc_alu_probe(int32_t blocks, int32_t iters, int32_t *sink_dev, double *ops, void *stream);
 
+/* ---- endpoint images and GPU decode (the stream's endpoint half) ----
+ * Frame sizes must be multiples of 256 pixels (64 blocks) in both directions:
+ * the reference transforms the endpoint images in 64x64-block tiles and
+ * writes out of bounds otherwise (codec/image_processing.h:293-294).
+ *
+ * Coefficient layout: 6 planes of blocks bytes each,
+ *   [Y1 | Co1 | Cg1 | Y2 | Co2 | Cg2]
+ * i.e. exactly the byte vectors CompressEndpoint arithmetic-codes
+ * (codec/codec.cpp:804-846: the Y plane of endpoint 1, its Co plane followed
+ * by its Cg plane, then the same for endpoint 2). */
+
+/* The transform half of CompressEndpoint (codec/codec.cpp:804-838: RGB565 ->
+ * YCoCg-667, ImageSplit, RunDXTEndpointPipeline = per-tile 6-level 5/3
+ * wavelet, int8 wrap, +128) for the final blocks of one frame. */
+mptc_status mptc_endpoint_coefficients(int32_t width, int32_t height, const uint64_t *blocks_dev,
+                                       uint8_t *coeff_dev, void *stream);
+
+/* GPU half of the reference's GetFrame (codec/decoder.cpp:256-414): from one
+ * frame's entropy-decoded parts (coefficients as above, motion codes, the
+ * frame's slice of the group palette) and the previous decoded frame, the
+ * frame's physical blocks: ReconstructDXTFrame (decoder.cpp:203-254) and
+ * ReconstructEndpoints with the inverse wavelet (decoder.cpp:68-201). */
+typedef struct mptc_decoder mptc_decoder;
+mptc_status mptc_decoder_create(int32_t width, int32_t height, int32_t search_area,
+                                mptc_decoder **out_decoder);
+mptc_status mptc_decoder_destroy(mptc_decoder *dec);
+/* prev_blocks_dev may be NULL for a frame without inter copies (the first).
+ * Asynchronous on `stream`; invalid references are recorded, see below. */
+mptc_status mptc_decode_frame(mptc_decoder *dec, const uint8_t *coeff_dev, const uint8_t *motion_dev,
+                              const uint32_t *unique_dev, uint32_t n_unique,
+                              const uint64_t *prev_blocks_dev, uint64_t *out_blocks_dev, void *stream);
+/* Synchronises `stream` and returns MPTC_EINVAL if any frame decoded since the
+ * last check held an invalid motion code (a copy from outside the previous
+ * frame or from a block not yet decoded) or a unique count that differs from
+ * n_unique; *flags (may be NULL) gets bit 0 / bit 1 for those. Clears them. */
+mptc_status mptc_decoder_check(mptc_decoder *dec, void *stream, uint32_t *flags);
+const char *mptc_decoder_last_error(const mptc_decoder *dec);
+
 /* Human-readable text of the last error on this context (never NULL). */
 const char *mptc_last_error(const mptc_ctx *ctx);
 

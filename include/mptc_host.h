@@ -1,6 +1,6 @@
 /*
- * mptc_host — host-side MPTC stream writer (no GPU): turns the arrays the
- * encoder returns per frame (final DXT1 blocks, motion codes, unique index
+ * mptc_host — host-side MPTC stream writer and reader (no GPU). The writer
+ * turns the arrays the encoder returns per frame (final DXT1 blocks, motion codes, unique index
  * palette) into the MPTC container bytes, exactly as the reference encoder's
  * CompressMultiUnique (codec/codec.cpp:1307-1532) writes them:
  *
@@ -21,7 +21,8 @@
  * count towards the maximum sizes) but not written, and the endpoint images
  * must be multiples of 64 blocks in each direction (frame sizes multiples of
  * 256 pixels): other sizes are rejected here, where the reference would write
- * out of bounds.
+ * out of bounds. A writer or reader object is not thread-safe; separate
+ * objects may be used from separate threads.
  */
 #ifndef MPTC_HOST_H_
 #define MPTC_HOST_H_
@@ -49,15 +50,54 @@ mptc_status mptc_stream_writer_add_frame(mptc_stream_writer *writer, const uint6
                                          const uint8_t *motion, const uint32_t *unique_palette,
                                          uint32_t n_unique);
 
+/* The same frame with its endpoint images already transformed (for instance by
+ * mptc_endpoint_coefficients on the GPU): `coeff` holds the six coefficient
+ * planes [Y1 | Co1 | Cg1 | Y2 | Co2 | Cg2] of blocks bytes each, the byte
+ * vectors that CompressEndpoint codes (codec/codec.cpp:838-846). */
+mptc_status mptc_stream_writer_add_frame_coefficients(mptc_stream_writer *writer, const uint8_t *coeff,
+                                                      const uint8_t *motion, const uint32_t *unique_palette,
+                                                      uint32_t n_unique);
+
 /* Finishes the stream: *size receives its byte count; if `out` is not NULL
  * (room for *size bytes when called with out == NULL first) the bytes are
- * copied there. Frame record sizes of the last frame: optional. */
+ * copied there. */
 mptc_status mptc_stream_writer_finish(mptc_stream_writer *writer, uint8_t *out, uint64_t *size);
 
 /* Sizes in bytes of the last added frame's coded parts: motion codes, the four
  * endpoint streams (Y1, C1, Y2, C2). Any pointer may be NULL. */
 mptc_status mptc_stream_writer_frame_sizes(const mptc_stream_writer *writer, uint32_t *motion_bytes,
                                            uint32_t *endpoint_bytes);
+
+/* ---- reader: the host half of the reference decoder's GetFrame
+ * (codec/decoder.cpp:256-414): header, group palettes and per-frame parts,
+ * arithmetic-decoded (EntropyDecode, decoder.cpp:44-65). The frame's blocks
+ * are then rebuilt by mptc_decode_frame (include/mptc_gb300.h).
+ *
+ * Unlike GetFrame, which rewinds to the first group as soon as it has read
+ * the last group's palette (decoder.cpp:404-409, so the later frames of that
+ * group are never returned), the reader returns every frame of every
+ * complete group, in order, then reports the end. */
+typedef struct mptc_stream_info {
+  int32_t width, height, search_area, unique_interval;
+  uint32_t groups, frames; /* frames = groups * unique_interval */
+  uint32_t max_unique_count, max_compressed_palette, max_compressed_motion_indices;
+  uint32_t max_compressed_ep_y, max_compressed_ep_c;
+} mptc_stream_info;
+
+typedef struct mptc_stream_reader mptc_stream_reader;
+
+/* Copies `size` bytes of stream; checks the header (sizes multiples of 256
+ * pixels, search area 1..63, unique interval >= 1). */
+mptc_status mptc_stream_reader_open(const uint8_t *data, uint64_t size, mptc_stream_reader **out_reader);
+mptc_status mptc_stream_reader_destroy(mptc_stream_reader *reader);
+mptc_status mptc_stream_reader_info(const mptc_stream_reader *reader, mptc_stream_info *info);
+
+/* Next frame's parts: motion (2 bytes per block), coeff (6 planes of blocks
+ * bytes, the layout mptc_decode_frame reads), its slice of the group palette
+ * (room for blocks entries) and the slice length. MPTC_ESTATE after the last
+ * frame; MPTC_EINVAL on a truncated or inconsistent stream. */
+mptc_status mptc_stream_reader_next(mptc_stream_reader *reader, uint8_t *motion, uint8_t *coeff,
+                                    uint32_t *unique_palette, uint32_t *n_unique);
 
 #ifdef __cplusplus
 }

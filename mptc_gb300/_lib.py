@@ -25,6 +25,8 @@ EXPORTED = [
     "mptc_model_destroy", "mptc_model_get_params", "mptc_model_set_params", "mptc_model_train_step",
     "mptc_model_grads", "mptc_model_embed", "mptc_model_save", "mptc_model_load",
     "mptc_ctx_set_model", "mptc_decoded_sse", "mptc_batch_set_model",
+    "mptc_endpoint_coefficients", "mptc_decoder_create", "mptc_decoder_destroy", "mptc_decode_frame",
+    "mptc_decoder_check", "mptc_decoder_last_error",
 ]
 
 NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
@@ -102,11 +104,18 @@ def lib() -> ctypes.CDLL:
         L.mptc_ctx_set_model.argtypes = [vp, vp, i32]
         L.mptc_decoded_sse.argtypes = [vp, i32, i32, vp, vp, vp]
         L.mptc_batch_set_model.argtypes = [vp, vp, i32]
+        L.mptc_endpoint_coefficients.argtypes = [i32, i32, vp, vp, vp]
+        L.mptc_decoder_create.argtypes = [i32, i32, i32, ctypes.POINTER(vp)]
+        L.mptc_decoder_destroy.argtypes = [vp]
+        L.mptc_decode_frame.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp, vp, vp]
+        L.mptc_decoder_check.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_uint32)]
+        L.mptc_decoder_last_error.argtypes = [vp]
+        L.mptc_decoder_last_error.restype = ctypes.c_char_p
         L.mptc_version.restype = i32
         L.mptc_built_arch.restype = i32
         for name in EXPORTED:
             if name not in ("mptc_last_error", "mptc_version", "mptc_built_arch",
-                            "mptc_model_num_params"):
+                            "mptc_model_num_params", "mptc_decoder_last_error"):
                 getattr(L, name).restype = ctypes.c_int
         _LIB = L
     return _LIB

@@ -1,0 +1,134 @@
+// Host-side MPTC stream reader (include/mptc_host.h): walks the container the
+// writer produces (codec/codec.cpp:1354-1505 layout) and arithmetic-decodes
+// each frame's parts, as the reference decoder's GetFrame does
+// (codec/decoder.cpp:256-414), without its rewind after the last group's
+// palette. The five parts of a frame decode concurrently on large frames.
+#include "../../include/mptc_host.h"
+#include "arith_coder.h"
+
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr size_t kParallelBlocks = 16384;
+
+uint32_t get_u32(const uint8_t *p) { return (uint32_t)p[0] | (uint32_t)p[1] << 8 | (uint32_t)p[2] << 16 | (uint32_t)p[3] << 24; }
+
+}  // namespace
+
+struct mptc_stream_reader {
+  std::vector<uint8_t> data;
+  mptc_stream_info info{};
+  size_t nblk = 0;
+  size_t pos = 34;               // next unread byte
+  uint32_t frame = 0;            // frames returned
+  std::vector<uint8_t> palette;  // decoded palette bytes of the current group
+  size_t palette_used = 0;
+
+  bool take(size_t n, const uint8_t **p) {
+    if (n > data.size() - pos) return false;
+    *p = data.data() + pos;
+    pos += n;
+    return true;
+  }
+  bool take_u32(uint32_t *v) {
+    const uint8_t *p;
+    if (!take(4, &p)) return false;
+    *v = get_u32(p);
+    return true;
+  }
+};
+
+extern "C" {
+
+mptc_status mptc_stream_reader_open(const uint8_t *data, uint64_t size, mptc_stream_reader **out) {
+  if (!out || (!data && size) || size < 34) return MPTC_EINVAL;
+  mptc_stream_info in{};
+  in.height = (int32_t)get_u32(data);
+  in.width = (int32_t)get_u32(data + 4);
+  in.unique_interval = data[8];
+  in.search_area = data[9];
+  in.groups = get_u32(data + 10);
+  in.max_unique_count = get_u32(data + 14);
+  in.max_compressed_palette = get_u32(data + 18);
+  in.max_compressed_motion_indices = get_u32(data + 22);
+  in.max_compressed_ep_y = get_u32(data + 26);
+  in.max_compressed_ep_c = get_u32(data + 30);
+  if (in.width <= 0 || in.height <= 0 || in.width % 256 || in.height % 256 || in.unique_interval < 1 ||
+      in.search_area < 1 || in.search_area > 63)
+    return MPTC_EINVAL;
+  in.frames = in.groups * (uint32_t)in.unique_interval;
+  mptc_stream_reader *r = new (std::nothrow) mptc_stream_reader();
+  if (!r) return MPTC_ENOMEM;
+  try {
+    r->data.assign(data, data + size);
+  } catch (...) {
+    delete r;
+    return MPTC_ENOMEM;
+  }
+  r->info = in;
+  r->nblk = (size_t)(in.width / 4) * (in.height / 4);
+  *out = r;
+  return MPTC_OK;
+}
+
+mptc_status mptc_stream_reader_destroy(mptc_stream_reader *r) {
+  if (!r) return MPTC_EINVAL;
+  delete r;
+  return MPTC_OK;
+}
+
+mptc_status mptc_stream_reader_info(const mptc_stream_reader *r, mptc_stream_info *info) {
+  if (!r || !info) return MPTC_EINVAL;
+  *info = r->info;
+  return MPTC_OK;
+}
+
+mptc_status mptc_stream_reader_next(mptc_stream_reader *r, uint8_t *motion, uint8_t *coeff, uint32_t *unique,
+                                    uint32_t *n_unique) {
+  if (!r || !motion || !coeff || !unique || !n_unique) return MPTC_EINVAL;
+  if (r->frame >= r->info.frames) return MPTC_ESTATE;
+  const size_t n = r->nblk;
+  if (r->frame % (uint32_t)r->info.unique_interval == 0) {
+    // group start: [u32 palette_size][palette code][u32 palette bytes] (decoder.cpp:341-357)
+    uint32_t psz, count;
+    const uint8_t *pc;
+    if (!r->take_u32(&psz) || !r->take(psz, &pc) || !r->take_u32(&count)) return MPTC_EINVAL;
+    if (count > 4 * n * (size_t)r->info.unique_interval) return MPTC_EINVAL;
+    r->palette.assign(count, 0);
+    if (!mptc_host::decode_bytes(pc, psz, r->palette.data(), count)) return MPTC_EINVAL;
+    r->palette_used = 0;
+  }
+  // frame record: [u32 n_unique][u32 size][motion] then 4 x [u32 size][part] (decoder.cpp:361-401)
+  uint32_t nu;
+  const uint8_t *code[5];
+  uint32_t csz[5];
+  if (!r->take_u32(&nu)) return MPTC_EINVAL;
+  for (int k = 0; k < 5; ++k)
+    if (!r->take_u32(&csz[k]) || !r->take(csz[k], &code[k])) return MPTC_EINVAL;
+  if (nu > n || 4 * (size_t)nu > r->palette.size() - r->palette_used) return MPTC_EINVAL;
+  uint8_t *dst[5] = {motion, coeff, coeff + n, coeff + 3 * n, coeff + 4 * n};
+  const size_t len[5] = {2 * n, n, 2 * n, n, 2 * n};
+  bool ok[5];
+  if (n >= kParallelBlocks) {
+    std::thread t[4];
+    for (int k = 1; k < 5; ++k)
+      t[k - 1] = std::thread([&, k] { ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]); });
+    ok[0] = mptc_host::decode_bytes(code[0], csz[0], dst[0], len[0]);
+    for (auto &th : t) th.join();
+  } else {
+    for (int k = 0; k < 5; ++k) ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]);
+  }
+  for (bool b : ok)
+    if (!b) return MPTC_EINVAL;
+  std::memcpy(unique, r->palette.data() + r->palette_used, 4 * (size_t)nu);
+  r->palette_used += 4 * (size_t)nu;
+  *n_unique = nu;
+  ++r->frame;
+  return MPTC_OK;
+}
+
+}  // extern "C"

@@ -1,133 +1,22 @@
-// Host-side MPTC stream writer (include/mptc_host.h): the container, the
-// adaptive arithmetic coder and the endpoint transform of the reference
-// encoder, restated so that a stream built from this library's per-frame
-// arrays is byte-identical to the reference encoder's stream.
-//
-// Arithmetic coder: the 32-bit multiplication-based coder with adaptive
-// multi-symbol models of A. Said's "FastAC" (as vendored in the reference,
-// entropy/arithmetic_codec.cpp:80-120, :360-388, :498-507, :547-573,
-// :781-826): interval [base, base + length), models that rescale a cumulative
-// distribution of 2^15 periodically from symbol counts, carry propagation into
-// the bytes already written.
+// Host-side MPTC stream writer (include/mptc_host.h): the container and the
+// endpoint transform of the reference encoder, restated so that a stream
+// built from this library's per-frame arrays is byte-identical to the
+// reference encoder's stream. The arithmetic coder is in arith_coder.h.
 #include "../../include/mptc_host.h"
+#include "arith_coder.h"
 
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <new>
+#include <thread>
 #include <vector>
 
 namespace {
 
-constexpr uint32_t kMinLength = 0x01000000u;  // renormalise below this length
-constexpr uint32_t kMaxLength = 0xFFFFFFFFu;
-constexpr uint32_t kLengthShift = 15;         // distribution resolution (bits)
-constexpr uint32_t kMaxCount = 1u << kLengthShift;
+using mptc_host::code_bytes;
 
-// Adaptive multi-symbol model: counts start at one; the cumulative
-// distribution is recomputed after `update_cycle` symbols, the cycle growing
-// by 5/4 up to 8 * (symbols + 6); counts are halved past kMaxCount.
-class AdaptiveModel {
- public:
-  explicit AdaptiveModel(uint32_t symbols) : n_(symbols), dist_(symbols), count_(symbols, 1u) {
-    total_ = 0;
-    cycle_ = n_;
-    rebuild();
-    until_ = cycle_ = (n_ + 6) >> 1;
-  }
-  uint32_t symbols() const { return n_; }
-  uint32_t lo(uint32_t s) const { return dist_[s]; }
-  uint32_t hi(uint32_t s) const { return dist_[s + 1]; }
-  void seen(uint32_t s) {
-    ++count_[s];
-    if (--until_ == 0) rebuild();
-  }
-
- private:
-  void rebuild() {
-    if ((total_ += cycle_) > kMaxCount) {
-      total_ = 0;
-      for (uint32_t k = 0; k < n_; ++k) total_ += (count_[k] = (count_[k] + 1) >> 1);
-    }
-    const uint32_t scale = 0x80000000u / total_;
-    uint32_t sum = 0;
-    for (uint32_t k = 0; k < n_; ++k) {
-      dist_[k] = (scale * sum) >> (31 - kLengthShift);
-      sum += count_[k];
-    }
-    cycle_ = (5 * cycle_) >> 2;
-    const uint32_t max_cycle = (n_ + 6) << 3;
-    if (cycle_ > max_cycle) cycle_ = max_cycle;
-    until_ = cycle_;
-  }
-
-  uint32_t n_;
-  std::vector<uint32_t> dist_, count_;
-  uint32_t total_ = 0, cycle_ = 0, until_ = 0;
-};
-
-class ArithmeticEncoder {
- public:
-  void encode(uint32_t s, AdaptiveModel &m) {
-    const uint32_t before = base_;
-    uint32_t x;
-    if (s == m.symbols() - 1) {  // last symbol: the interval's top end
-      x = m.lo(s) * (length_ >> kLengthShift);
-      base_ += x;
-      length_ -= x;
-    } else {
-      length_ >>= kLengthShift;
-      x = m.lo(s) * length_;
-      base_ += x;
-      length_ = m.hi(s) * length_ - x;
-    }
-    if (before > base_) carry();
-    if (length_ < kMinLength) renormalise();
-    m.seen(s);
-  }
-  // Final bytes; returns the code.
-  std::vector<uint8_t> &finish() {
-    const uint32_t before = base_;
-    if (length_ > 2 * kMinLength) {
-      base_ += kMinLength;
-      length_ = kMinLength >> 1;
-    } else {
-      base_ += kMinLength >> 1;
-      length_ = kMinLength >> 9;
-    }
-    if (before > base_) carry();
-    renormalise();
-    return out_;
-  }
-
- private:
-  void carry() {
-    for (size_t p = out_.size(); p-- > 0;) {
-      if (out_[p] != 0xFF) {
-        ++out_[p];
-        return;
-      }
-      out_[p] = 0;
-    }
-  }
-  void renormalise() {
-    do {
-      out_.push_back((uint8_t)(base_ >> 24));
-      base_ <<= 8;
-    } while ((length_ <<= 8) < kMinLength);
-  }
-
-  uint32_t base_ = 0, length_ = kMaxLength;
-  std::vector<uint8_t> out_;
-};
-
-// A byte sequence through a fresh 257-symbol adaptive model.
-std::vector<uint8_t> code_bytes(const uint8_t *data, size_t n) {
-  AdaptiveModel m(257);
-  ArithmeticEncoder enc;
-  for (size_t i = 0; i < n; ++i) enc.encode(data[i], m);
-  return enc.finish();
-}
+constexpr size_t kParallelBlocks = 16384;  // frames this large code their parts concurrently
 
 // --- endpoint transform (codec/image_processing.cpp:10-27, codec/wavelet.cpp:11-131) ---
 
@@ -210,6 +99,83 @@ struct mptc_stream_writer {
   uint32_t last_motion = 0, last_ep[4] = {0, 0, 0, 0};
 };
 
+namespace {
+
+// The six coefficient planes [Y1 | Co1 | Cg1 | Y2 | Co2 | Cg2] of a frame's
+// endpoint images (CompressEndpoint, codec/codec.cpp:804-838).
+std::vector<uint8_t> endpoint_coefficients(const uint64_t *blocks, int bw, int bh) {
+  const size_t n = (size_t)bw * bh;
+  std::vector<uint8_t> out(6 * n);
+  for (int e = 0; e < 2; ++e) {
+    std::vector<int16_t> Y(n), Co(n), Cg(n);
+    for (size_t i = 0; i < n; ++i) {
+      const uint32_t x = (uint32_t)((blocks[i] >> (16 * e)) & 0xFFFF);
+      const int r = (int)(x >> 11), g = (int)((x >> 5) & 63), b = (int)(x & 31);
+      // RGB565 -> YCoCg-667 (reversible): Co = r - b, t = r + b + b/16,
+      // Cg = g - t, Y = t + Cg/2 (C division)
+      const int co = r - b, t = r + b + (b >> 4), cg = g - t, y = t + cg / 2;
+      Y[i] = (int16_t)y;
+      Co[i] = (int16_t)co;
+      Cg[i] = (int16_t)cg;
+    }
+    const std::vector<int16_t> *planes[3] = {&Y, &Co, &Cg};
+    for (int p = 0; p < 3; ++p) {
+      const std::vector<uint8_t> c = plane_coefficients(*planes[p], bw, bh);
+      std::copy(c.begin(), c.end(), out.begin() + (3 * e + p) * n);
+    }
+  }
+  return out;
+}
+
+// Codes one frame's parts and appends its record to the open group; closes
+// the group after unique_interval frames (codec/codec.cpp:1115-1158, :1471-1505).
+// The five parts (motion codes, Y1, Co1|Cg1, Y2, Co2|Cg2) use independent
+// coders and are coded concurrently on large frames.
+void append_frame(mptc_stream_writer *w, const uint8_t *coeff, const uint8_t *motion, const uint32_t *unique,
+                  uint32_t n_unique) {
+  const size_t n = (size_t)w->bw * w->bh;
+  const uint8_t *src[5] = {motion, coeff, coeff + n, coeff + 3 * n, coeff + 4 * n};
+  const size_t len[5] = {2 * n, n, 2 * n, n, 2 * n};
+  std::vector<uint8_t> z[5];
+  if (n >= kParallelBlocks) {
+    std::thread t[4];
+    for (int k = 1; k < 5; ++k) t[k - 1] = std::thread([&, k] { z[k] = code_bytes(src[k], len[k]); });
+    z[0] = code_bytes(src[0], len[0]);
+    for (auto &th : t) th.join();
+  } else {
+    for (int k = 0; k < 5; ++k) z[k] = code_bytes(src[k], len[k]);
+  }
+  std::vector<uint8_t> &rec = w->group_records;
+  put_u32(rec, n_unique);
+  for (int k = 0; k < 5; ++k) {
+    put_u32(rec, (uint32_t)z[k].size());
+    rec.insert(rec.end(), z[k].begin(), z[k].end());
+  }
+  w->last_motion = (uint32_t)z[0].size();
+  w->max_motion = std::max(w->max_motion, w->last_motion);
+  for (int k = 0; k < 4; ++k) w->last_ep[k] = (uint32_t)z[k + 1].size();
+  w->max_ep_y = std::max({w->max_ep_y, w->last_ep[0], w->last_ep[2]});
+  w->max_ep_c = std::max({w->max_ep_c, w->last_ep[1], w->last_ep[3]});
+  // unique palette of the group: u32 entries as bytes
+  const uint8_t *pb = reinterpret_cast<const uint8_t *>(unique);
+  if (n_unique) w->group_palette.insert(w->group_palette.end(), pb, pb + 4 * (size_t)n_unique);
+  if (++w->group_frames == (uint32_t)w->unique_interval) {
+    const std::vector<uint8_t> zp = code_bytes(w->group_palette.data(), w->group_palette.size());
+    put_u32(w->stream, (uint32_t)zp.size());
+    w->max_palette = std::max(w->max_palette, (uint32_t)zp.size());
+    w->stream.insert(w->stream.end(), zp.begin(), zp.end());
+    const uint32_t count = (uint32_t)w->group_palette.size();  // bytes, as the reference counts them
+    put_u32(w->stream, count);
+    w->max_unique = std::max(w->max_unique, count);
+    w->stream.insert(w->stream.end(), w->group_records.begin(), w->group_records.end());
+    w->group_records.clear();
+    w->group_palette.clear();
+    w->group_frames = 0;
+  }
+}
+
+}  // namespace
+
 extern "C" {
 
 mptc_status mptc_stream_writer_create(int32_t width, int32_t height, int32_t search_area, int32_t unique_interval,
@@ -246,61 +212,18 @@ mptc_status mptc_stream_writer_destroy(mptc_stream_writer *w) {
 mptc_status mptc_stream_writer_add_frame(mptc_stream_writer *w, const uint64_t *blocks, const uint8_t *motion,
                                          const uint32_t *unique, uint32_t n_unique) {
   if (!w || !blocks || !motion || (n_unique && !unique)) return MPTC_EINVAL;
-  const size_t n = (size_t)w->bw * w->bh;
-  if (n_unique > n) return MPTC_EINVAL;
-  std::vector<uint8_t> rec;
-  // frame record: unique count, motion codes (codec/codec.cpp:1119-1153)
-  const std::vector<uint8_t> mo = code_bytes(motion, 2 * n);
-  put_u32(rec, n_unique);
-  put_u32(rec, (uint32_t)mo.size());
-  rec.insert(rec.end(), mo.begin(), mo.end());
-  w->max_motion = std::max(w->max_motion, (uint32_t)mo.size());
-  w->last_motion = (uint32_t)mo.size();
-  // endpoint images (CompressEndpoint, codec/codec.cpp:804-899)
-  for (int e = 0; e < 2; ++e) {
-    std::vector<int16_t> Y(n), Co(n), Cg(n);
-    for (size_t i = 0; i < n; ++i) {
-      const uint32_t x = (uint32_t)((blocks[i] >> (16 * e)) & 0xFFFF);
-      const int r = (int)(x >> 11), g = (int)((x >> 5) & 63), b = (int)(x & 31);
-      // RGB565 -> YCoCg-667 (reversible): Co = r - b, t = r + b + b/16,
-      // Cg = g - t, Y = t + Cg/2 (C division)
-      const int co = r - b, t = r + b + (b >> 4), cg = g - t, y = t + cg / 2;
-      Y[i] = (int16_t)y;
-      Co[i] = (int16_t)co;
-      Cg[i] = (int16_t)cg;
-    }
-    const std::vector<uint8_t> cy = plane_coefficients(Y, w->bw, w->bh);
-    std::vector<uint8_t> cc = plane_coefficients(Co, w->bw, w->bh);
-    const std::vector<uint8_t> ccg = plane_coefficients(Cg, w->bw, w->bh);
-    cc.insert(cc.end(), ccg.begin(), ccg.end());
-    const std::vector<uint8_t> zy = code_bytes(cy.data(), cy.size());
-    const std::vector<uint8_t> zc = code_bytes(cc.data(), cc.size());
-    put_u32(rec, (uint32_t)zy.size());
-    rec.insert(rec.end(), zy.begin(), zy.end());
-    put_u32(rec, (uint32_t)zc.size());
-    rec.insert(rec.end(), zc.begin(), zc.end());
-    w->max_ep_y = std::max(w->max_ep_y, (uint32_t)zy.size());
-    w->max_ep_c = std::max(w->max_ep_c, (uint32_t)zc.size());
-    w->last_ep[2 * e] = (uint32_t)zy.size();
-    w->last_ep[2 * e + 1] = (uint32_t)zc.size();
-  }
-  w->group_records.insert(w->group_records.end(), rec.begin(), rec.end());
-  // unique palette of the group (codec/codec.cpp:1471-1505): u32 entries as bytes
-  const uint8_t *pb = reinterpret_cast<const uint8_t *>(unique);
-  w->group_palette.insert(w->group_palette.end(), pb, pb + 4 * (size_t)n_unique);
-  if (++w->group_frames == (uint32_t)w->unique_interval) {
-    const std::vector<uint8_t> zp = code_bytes(w->group_palette.data(), w->group_palette.size());
-    put_u32(w->stream, (uint32_t)zp.size());
-    w->max_palette = std::max(w->max_palette, (uint32_t)zp.size());
-    w->stream.insert(w->stream.end(), zp.begin(), zp.end());
-    const uint32_t count = (uint32_t)w->group_palette.size();  // bytes, as the reference counts them
-    put_u32(w->stream, count);
-    w->max_unique = std::max(w->max_unique, count);
-    w->stream.insert(w->stream.end(), w->group_records.begin(), w->group_records.end());
-    w->group_records.clear();
-    w->group_palette.clear();
-    w->group_frames = 0;
-  }
+  if (n_unique > (size_t)w->bw * w->bh) return MPTC_EINVAL;
+  const std::vector<uint8_t> coeff = endpoint_coefficients(blocks, w->bw, w->bh);
+  append_frame(w, coeff.data(), motion, unique, n_unique);
+  return MPTC_OK;
+}
+
+mptc_status mptc_stream_writer_add_frame_coefficients(mptc_stream_writer *w, const uint8_t *coeff,
+                                                      const uint8_t *motion, const uint32_t *unique,
+                                                      uint32_t n_unique) {
+  if (!w || !coeff || !motion || (n_unique && !unique)) return MPTC_EINVAL;
+  if (n_unique > (size_t)w->bw * w->bh) return MPTC_EINVAL;
+  append_frame(w, coeff, motion, unique, n_unique);
   return MPTC_OK;
 }
 

@@ -1,9 +1,12 @@
-"""MPTC stream writer: ctypes binding of ``libmptc_host.so`` (include/mptc_host.h).
+"""MPTC stream writer and reader: ctypes binding of ``libmptc_host.so``
+(include/mptc_host.h).
 
-Turns the per-frame arrays the encoder returns (final blocks, motion codes,
-unique palette) into the bytes of an MPTC stream, identical to the stream the
-reference encoder's ``CompressMultiUnique`` (codec/codec.cpp:1307-1532) writes
-for the same frames. Host-only: no GPU is needed.
+The writer turns the per-frame arrays the encoder returns (final blocks,
+motion codes, unique palette) into the bytes of an MPTC stream, identical to
+the stream the reference encoder's ``CompressMultiUnique``
+(codec/codec.cpp:1307-1532) writes for the same frames. The reader walks a
+stream and entropy-decodes each frame's parts for the GPU decoder
+(``mptc_gb300.decoder``). Host-only: no GPU is needed.
 """
 from __future__ import annotations
 
@@ -19,8 +22,20 @@ HOST_LIB_PATH = os.path.join(_HERE, "libmptc_host.so")
 
 HOST_EXPORTED = [
     "mptc_stream_writer_create", "mptc_stream_writer_destroy", "mptc_stream_writer_add_frame",
-    "mptc_stream_writer_finish", "mptc_stream_writer_frame_sizes",
+    "mptc_stream_writer_add_frame_coefficients", "mptc_stream_writer_finish",
+    "mptc_stream_writer_frame_sizes", "mptc_stream_reader_open", "mptc_stream_reader_destroy",
+    "mptc_stream_reader_info", "mptc_stream_reader_next",
 ]
+
+
+class StreamInfo(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("search_area", ctypes.c_int32),
+                ("unique_interval", ctypes.c_int32), ("groups", ctypes.c_uint32),
+                ("frames", ctypes.c_uint32), ("max_unique_count", ctypes.c_uint32),
+                ("max_compressed_palette", ctypes.c_uint32),
+                ("max_compressed_motion_indices", ctypes.c_uint32),
+                ("max_compressed_ep_y", ctypes.c_uint32), ("max_compressed_ep_c", ctypes.c_uint32)]
+
 
 _HOST = None
 
@@ -37,6 +52,11 @@ def host_lib() -> ctypes.CDLL:
         L.mptc_stream_writer_add_frame.argtypes = [vp, vp, vp, vp, ctypes.c_uint32]
         L.mptc_stream_writer_finish.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_uint64)]
         L.mptc_stream_writer_frame_sizes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), vp]
+        L.mptc_stream_writer_add_frame_coefficients.argtypes = [vp, vp, vp, vp, ctypes.c_uint32]
+        L.mptc_stream_reader_open.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(vp)]
+        L.mptc_stream_reader_destroy.argtypes = [vp]
+        L.mptc_stream_reader_info.argtypes = [vp, ctypes.POINTER(StreamInfo)]
+        L.mptc_stream_reader_next.argtypes = [vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
         _HOST = L
     return _HOST
 
@@ -68,6 +88,18 @@ class StreamWriter:
         _check(host_lib().mptc_stream_writer_add_frame(self._h, final.ctypes.data, motion.ctypes.data,
                                                         unique.ctypes.data if unique.size else None,
                                                         unique.size), "add_frame")
+
+    def add_frame_coefficients(self, coeff: np.ndarray, motion: np.ndarray, unique: np.ndarray) -> None:
+        """A frame whose endpoint images are already transformed: ``coeff`` is
+        the six coefficient planes [Y1|Co1|Cg1|Y2|Co2|Cg2], blocks bytes each."""
+        coeff = np.ascontiguousarray(coeff, dtype=np.uint8).reshape(-1)
+        motion = np.ascontiguousarray(motion, dtype=np.uint8).reshape(-1)
+        unique = np.ascontiguousarray(unique, dtype=np.uint32).reshape(-1)
+        if coeff.size != 6 * self.blocks or motion.size != 2 * self.blocks:
+            raise ValueError(f"frame arrays do not match {self.blocks} blocks")
+        _check(host_lib().mptc_stream_writer_add_frame_coefficients(
+            self._h, coeff.ctypes.data, motion.ctypes.data, unique.ctypes.data if unique.size else None,
+            unique.size), "add_frame_coefficients")
 
     def frame_sizes(self) -> tuple[int, list[int]]:
         """(motion bytes, [Y1, C1, Y2, C2] endpoint bytes) of the last frame."""
@@ -110,3 +142,51 @@ def write_stream(frames, width: int, height: int, search_area: int, unique_inter
         return w.finish()
     finally:
         w.close()
+
+
+class StreamReader:
+    """Walks an MPTC stream and entropy-decodes each frame's parts (the host
+    half of the reference decoder's GetFrame, codec/decoder.cpp:256-414)."""
+
+    def __init__(self, data: bytes):
+        self._buf = np.frombuffer(data, np.uint8)
+        self._h = ctypes.c_void_p()
+        _check(host_lib().mptc_stream_reader_open(self._buf.ctypes.data if self._buf.size else None,
+                                                   self._buf.size, ctypes.byref(self._h)),
+               "stream header")
+        self.info = StreamInfo()
+        _check(host_lib().mptc_stream_reader_info(self._h, ctypes.byref(self.info)), "stream info")
+        self.blocks = (self.info.width // 4) * (self.info.height // 4)
+
+    def next_frame(self, motion=None, coeff=None, unique=None):
+        """(motion u8[2n], coeff u8[6n], unique u32[n_unique]) of the next frame,
+        or None after the last one. Output arrays may be passed in for reuse."""
+        n = self.blocks
+        motion = np.empty(2 * n, np.uint8) if motion is None else motion
+        coeff = np.empty(6 * n, np.uint8) if coeff is None else coeff
+        unique = np.empty(n, np.uint32) if unique is None else unique
+        nu = ctypes.c_uint32()
+        rc = host_lib().mptc_stream_reader_next(self._h, motion.ctypes.data, coeff.ctypes.data,
+                                                unique.ctypes.data, ctypes.byref(nu))
+        if rc == 5:  # MPTC_ESTATE: no frames left
+            return None
+        _check(rc, "stream frame")
+        return motion, coeff, unique[: nu.value]
+
+    def __iter__(self):
+        while True:
+            f = self.next_frame()
+            if f is None:
+                return
+            yield f
+
+    def close(self) -> None:
+        if self._h:
+            host_lib().mptc_stream_reader_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

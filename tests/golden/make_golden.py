@@ -13,7 +13,10 @@ synthetic streams and on adversarial block patterns, and records:
 * ``golden.json["streams"]``  SHA-256 and size of whole MPTC streams written
                        by the unmodified reference encoder (``CompressMultiUnique``
                        via ``oracle/_ref/mptc_encoder``, fed PNG frames), which
-                       pin the host stream writer byte for byte.
+                       pin the host stream writer byte for byte, and SHA-256 per
+                       frame of the blocks the unmodified reference decoder
+                       (``GetFrame`` via ``oracle/_ref/decoder_harness``)
+                       rebuilds from each stream, which pin the GPU decoder.
 
 Usage (needs the reference sources; run from the repository root):
     make -C oracle/ref REF=<path to MPTC>
@@ -39,6 +42,7 @@ from mptc_gb300.synth import HD720, FHD1080, SMOKE_256, StreamSpec  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "hotpath_harness")
 ENCODER = os.path.join(ROOT, "oracle", "_ref", "mptc_encoder")
+DECODER = os.path.join(ROOT, "oracle", "_ref", "decoder_harness")
 OUT_DIR = os.path.dirname(os.path.abspath(__file__))
 
 # (name, spec, first frame, frame count, search_area, threshold, intra_interval)
@@ -63,7 +67,7 @@ STREAM_CASES = [
     ("stream256_sa8_thr5_ii16_ui8", SMOKE_256, 0, 16, 8, 5, 16, 8),
     ("stream256_sa4_thr0_ii4_ui3_tail", SMOKE_256, 0, 8, 4, 0, 4, 3),
     ("stream512x256_sa2_thr20_ii2_ui1", StreamSpec(512, 256, 4, seed=21, n_squares=3), 0, 4, 2, 20, 2, 1),
-    ("stream256x512_sa16_thr5_ii8_ui4", StreamSpec(256, 512, 4, seed=22, cut_every=3), 0, 4, 16, 5, 8, 4),
+    ("stream256x512_sa16_thr5_ii8_ui4", StreamSpec(256, 512, 8, seed=22, cut_every=3), 0, 8, 16, 5, 8, 4),
 ]
 
 
@@ -182,6 +186,20 @@ def run_reference_stream(frames: np.ndarray, sa: int, thr: int, ii: int, ui: int
         return open(out, "rb").read()
 
 
+def run_reference_decoder(data: bytes, n_frames: int) -> list[np.ndarray]:
+    """Physical blocks of the first n_frames frames as the reference decoder's
+    GetFrame (codec/decoder.cpp:256-414) rebuilds them."""
+    h, w = struct.unpack_from("<II", data, 0)
+    nblk = (w // 4) * (h // 4)
+    with tempfile.TemporaryDirectory() as td:
+        sp = os.path.join(td, "stream.mptc")
+        op = os.path.join(td, "blocks.bin")
+        open(sp, "wb").write(data)
+        subprocess.check_call([DECODER, sp, str(n_frames), op], cwd=td, stdout=subprocess.DEVNULL)
+        raw = np.fromfile(op, np.uint64)
+    return list(raw.reshape(n_frames, nblk))
+
+
 def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
@@ -225,12 +243,17 @@ def main() -> None:
     for name, spec, first, count, sa, thr, ii, ui in STREAM_CASES:
         frames = spec.generate(first, count)
         data = run_reference_stream(frames, sa, thr, ii, ui)
+        # GetFrame rewinds after the first frame of the last group
+        groups = count // ui
+        n_dec = (groups - 1) * ui + 1
+        decoded = run_reference_decoder(data, n_dec)
         golden["streams"].append(dict(
             name=name, spec=spec.__dict__, first=first, count=count, search_area=sa,
             threshold=thr, intra_interval=ii, unique_interval=ui,
             input_sha=[sha(f) for f in frames], size=len(data),
-            sha=hashlib.sha256(data).hexdigest(), header=data[:34].hex()))
-        print(name, len(data))
+            sha=hashlib.sha256(data).hexdigest(), header=data[:34].hex(),
+            decoded=[sha(b) for b in decoded]))
+        print(name, len(data), "decoded", n_dec)
     with open(os.path.join(OUT_DIR, "golden.json"), "w") as f:
         json.dump(golden, f, indent=1)
 

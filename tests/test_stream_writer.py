@@ -105,3 +105,88 @@ def test_writer_rejects_mismatched_arrays():
     with pytest.raises(MptcError):
         sw.add_frame(np.zeros(nb, np.uint64), np.zeros(2 * nb, np.uint8), np.zeros(nb + 1, np.uint32))
     sw.close()
+
+
+# ---- reader -------------------------------------------------------------------
+
+def _oracle_stream(case):
+    spec = StreamSpec(**case["spec"])
+    frames = spec.generate(case["first"], case["count"])
+    res = oracle.encode_stream(frames, case["search_area"], case["threshold"], case["intra_interval"],
+                               threads=os.cpu_count() or 1, want_psnr=False)
+    return spec, res, write_stream(res, spec.width, spec.height, case["search_area"],
+                                   case["unique_interval"])
+
+
+@pytest.mark.parametrize("case", STREAMS, ids=[c["name"] for c in STREAMS])
+def test_reader_recovers_frames_and_rewrites_identical_stream(case):
+    """Reader -> (motion, coefficients, palette) -> writer from coefficients
+    reproduces the reference stream; motion codes and palettes are the
+    encoder's (only complete groups are in the stream)."""
+    from mptc_gb300.stream import StreamReader
+    spec, res, data = _oracle_stream(case)
+    assert hashlib.sha256(data).hexdigest() == case["sha"]
+    rd = StreamReader(data)
+    ui = case["unique_interval"]
+    assert (rd.info.width, rd.info.height, rd.info.search_area, rd.info.unique_interval) == \
+        (spec.width, spec.height, case["search_area"], ui)
+    assert rd.info.frames == (case["count"] // ui) * ui
+    sw = StreamWriter(spec.width, spec.height, case["search_area"], ui, case["count"])
+    got = 0
+    for k, (motion, coeff, unique) in enumerate(rd):
+        np.testing.assert_array_equal(motion, res[k].motion)
+        np.testing.assert_array_equal(unique, res[k].unique)
+        sw.add_frame_coefficients(coeff, motion, unique)
+        got += 1
+    assert got == rd.info.frames
+    # frames after the last complete group are coded but not written
+    for r in res[got:]:
+        sw.add_frame(r.final, r.motion, r.unique)
+    assert hashlib.sha256(sw.finish()).hexdigest() == case["sha"]
+    sw.close()
+    rd.close()
+
+
+def test_reader_rejects_truncated_and_bad_streams():
+    from mptc_gb300.stream import StreamReader
+    case = STREAMS[2]
+    _, _, data = _oracle_stream(case)
+    with pytest.raises(MptcError):
+        StreamReader(data[:20])
+    bad = bytearray(data)
+    bad[9] = 0  # search area 0
+    with pytest.raises(MptcError):
+        StreamReader(bytes(bad))
+    rd = StreamReader(data[: len(data) // 2])
+    with pytest.raises(MptcError):
+        for _ in rd:
+            pass
+    rd.close()
+
+
+def test_arithmetic_coder_round_trip_on_skewed_and_uniform_bytes():
+    """Writer and reader coders are inverse on long runs, skewed and uniform
+    symbol statistics (model rescaling, carries, renormalisation)."""
+    from mptc_gb300.stream import StreamReader
+    w = h = 256
+    nb = (w // 4) * (h // 4)
+    rng = np.random.default_rng(11)
+    frames = []
+    for k in range(3):
+        motion = (rng.geometric(0.3 + 0.3 * k, 2 * nb) % 256).astype(np.uint8)
+        if k == 2:
+            motion = rng.integers(0, 256, 2 * nb, dtype=np.uint8)
+        coeff = rng.integers(0, 256, 6 * nb, dtype=np.uint8) if k else np.full(6 * nb, 128, np.uint8)
+        unique = rng.integers(0, 2**32, 17 * k, dtype=np.uint32)
+        frames.append((motion, coeff, unique))
+    sw = StreamWriter(w, h, 8, 1, 3)
+    for m, c, u in frames:
+        sw.add_frame_coefficients(c, m, u)
+    data = sw.finish()
+    sw.close()
+    rd = StreamReader(data)
+    for (m, c, u), (m2, c2, u2) in zip(frames, rd):
+        np.testing.assert_array_equal(m, m2)
+        np.testing.assert_array_equal(c, c2)
+        np.testing.assert_array_equal(u, u2)
+    rd.close()
