@@ -447,6 +447,55 @@ def encode_stream_quality(torch, enc, frames_dev, sched, W_, H_):
     return out
 
 
+def pad_to_tiles(torch, frames_dev):
+    """Edge-replicates frames to multiples of 256 pixels, the sizes the MPTC
+    stream's endpoint wavelet accepts (1920x1080 -> 2048x1280)."""
+    n, h, w, _ = frames_dev.shape
+    H2, W2 = -(-h // 256) * 256, -(-w // 256) * 256
+    out = torch.empty((n, H2, W2, 3), dtype=torch.uint8, device=frames_dev.device)
+    out[:, :h, :w] = frames_dev
+    out[:, h:, :w] = frames_dev[:, h - 1:h, :]
+    out[:, :, w:] = out[:, :, w - 1:w]
+    return out
+
+
+def stream_size(torch, enc, frames_dev, sched, ui):
+    """Encodes the frames (device API), writes the MPTC stream (GPU endpoint
+    transform + host arithmetic coder) and decodes it with the GPU decoder.
+    Returns (stream bytes, every frame decoded bit-exactly)."""
+    from mptc_gb300.decoder import Decoder, endpoint_coefficients
+    from mptc_gb300.stream import StreamReader, StreamWriter
+    nf, H_, W_, _ = frames_dev.shape
+    n = (W_ // 4) * (H_ // 4)
+    dev = frames_dev.device
+    fin = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(2)]
+    stb = torch.empty(n, dtype=torch.int64, device=dev)
+    mot = torch.empty(2 * n, dtype=torch.uint8, device=dev)
+    uni = torch.empty(n, dtype=torch.int32, device=dev)
+    nu = torch.zeros(1, dtype=torch.int32, device=dev)
+    coeff = torch.empty(6 * n, dtype=torch.uint8, device=dev)
+    sw = StreamWriter(W_, H_, SA, ui, nf)
+    finals = []
+    for f in range(nf):
+        prev = None if sched[f] else fin[(f - 1) % 2]
+        enc.encode_frame_device(frames_dev[f], prev, stb, fin[f % 2], mot, uni, nu)
+        endpoint_coefficients(W_, H_, fin[f % 2], coeff)
+        k = int(nu.item())
+        sw.add_frame_coefficients(coeff.cpu().numpy(), mot.cpu().numpy(), uni[:k].cpu().numpy().view(np.uint32))
+        finals.append(fin[f % 2].cpu().numpy().view(np.uint64).copy())
+    data = sw.finish()
+    sw.close()
+    rd = StreamReader(data)
+    dec = Decoder(W_, H_, SA)
+    exact = True
+    for k, (m, c, u) in enumerate(rd):
+        exact &= bool((dec.decode_frame(m, c, u).cpu().numpy().view(np.uint64) == finals[k]).all())
+    dec.check()
+    dec.close()
+    rd.close()
+    return len(data), exact
+
+
 def psnr_db(sse_list, W_, H_):
     return float(np.mean([10.0 * np.log10(3.0 * 255.0 ** 2 / (s / (W_ * H_))) for s in sse_list]))
 
@@ -455,7 +504,9 @@ def run_learned(args, rank: int, world: int, dist) -> None:
     """Learned proposal vs exhaustive search on the 1080p stream: trains on 200
     separate seeded frames with the library's kernels, then times both forms
     (single stream, or --batch S concurrent streams) and compares decoded
-    PSNR and the motion/palette code length on the same 120 frames."""
+    PSNR and the motion/palette code length on the same 120 frames, and the
+    bytes of whole MPTC streams of the first 32 frames (edge-padded to
+    256-pixel multiples, decoded back bit-exactly on the GPU)."""
     import torch
 
     from mptc_gb300.batch import BatchEncoder
@@ -484,6 +535,16 @@ def run_learned(args, rank: int, world: int, dist) -> None:
     learned_enc.set_model(model, args.topk)
     qp = encode_stream_quality(torch, plain_enc, frames_dev, sched, W, H)
     ql = encode_stream_quality(torch, learned_enc, frames_dev, sched, W, H)
+    # bitrate: whole MPTC streams of the first frames, padded to 256-pixel multiples
+    ns, UI = min(nf, 32), 8
+    padded = pad_to_tiles(torch, frames_dev[:ns])
+    pw, ph = padded.shape[2], padded.shape[1]
+    enc_p = Encoder(pw, ph, SA, THR, II)
+    bytes_p, exact_p = stream_size(torch, enc_p, padded, sched, UI)
+    enc_p.set_model(model, args.topk)
+    bytes_l, exact_l = stream_size(torch, enc_p, padded, sched, UI)
+    enc_p.close()
+    del padded
     n = (W // 4) * (H // 4)
     inter_blocks = sum(1 for f in sched if not f) * n
 
@@ -577,6 +638,10 @@ def run_learned(args, rank: int, world: int, dist) -> None:
                                 "psnr_delta_db": round(psnr_db(ql["sse"], W, H) - psnr_db(qp["sse"], W, H), 4),
                                 "motion_palette_bits_plain": int(bits_p), "motion_palette_bits_learned": int(bits_l),
                                 "motion_palette_bits_delta": round(bits_l / bits_p - 1.0, 5),
+                                "stream_frames": ns, "stream_padding": f"{W}x{H} edge-replicated to {pw}x{ph}",
+                                "stream_bytes_plain": bytes_p, "stream_bytes_learned": bytes_l,
+                                "stream_bytes_delta": round(bytes_l / bytes_p - 1.0, 5),
+                                "streams_decode_exactly": bool(exact_p and exact_l),
                                 "unique_blocks_plain": int(sum(qp["unique"])),
                                 "unique_blocks_learned": int(sum(ql["unique"])),
                                 "fallback_rate": round(ql["fallback"] / max(1, inter_blocks), 4)})

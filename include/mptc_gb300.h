@@ -122,7 +122,7 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
  * stb error of each block, the wavefront order and pending list of the intra
  * search, the refit weight sums of the previous frame's blocks, work counters,
  * tile counts) lives in one
- * file-scope device array of about 5 MiB inside the library, which every GPU
+ * file-scope device array of about 5.5 MiB inside the library, which every GPU
  * that loads the library holds until the process exits.
  *
  * Frames larger than MPTC_NOALLOC_MAX_BLOCKS blocks are rejected with

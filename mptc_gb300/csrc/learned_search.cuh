@@ -194,12 +194,15 @@ __global__ void __launch_bounds__(WARPS * 32) learned_inter_kernel(SearchParams 
       sel_refit = st.sel_refit;
     }
     if (lane == 0) {
+      uint64_t word = 0;
       if (accept) {
         const int row = sel_pos / w2, col = sel_pos - (sel_pos / w2) * w2;
-        P.final_blk[idx] = sel_refit ? ((uint64_t)sel_eps | ((uint64_t)sel_cand << 32)) : stb;
+        const uint64_t blk = sel_refit ? ((uint64_t)sel_eps | ((uint64_t)sel_cand << 32)) : stb;
+        P.final_blk[idx] = blk;
         P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
+        word = done_word(blk);
       }
-      P.done[idx] = accept ? 1u : 0u;
+      P.done[idx] = word;
     }
     __syncwarp();
   }

@@ -37,7 +37,7 @@ struct mptc_ctx {
   uint16_t *topk = nullptr;
   mptc_internal::EmbedWorkspace ews;
   // device scratch
-  uint32_t *done = nullptr;        // per block
+  uint64_t *done = nullptr;        // per block completion words
   uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats, [5] pending, [6] fallbacks, [5] pending count
   uint32_t *order = nullptr;       // blocks in wavefront order
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
@@ -372,7 +372,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
       mptc::inter_search_kernel<8><<<grid, 8 * 32, 0, s>>>(P);
     MPTC_CUDA(cudaGetLastError());
   } else {
-    MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint32_t), s));
+    MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint64_t), s));
   }
   if (prev_final_dev) {
     // pending = blocks the inter pass left open, in wavefront order
@@ -566,8 +566,8 @@ namespace {
 constexpr size_t kNaMaxBlocks = MPTC_NOALLOC_MAX_BLOCKS;
 constexpr size_t kNaTiles = (kNaMaxBlocks + mptc::kUniqTile - 1) / mptc::kUniqTile;
 // byte offsets inside the scratch array (each 256-byte aligned)
-constexpr size_t kNaDone = 0;                                   // u32 per block
-constexpr size_t kNaStb = kNaDone + kNaMaxBlocks * 4;           // u64 per block
+constexpr size_t kNaDone = 0;                                   // u64 per block
+constexpr size_t kNaStb = kNaDone + kNaMaxBlocks * 8;           // u64 per block
 constexpr size_t kNaOrig = kNaStb + kNaMaxBlocks * 8;           // i32 per block
 constexpr size_t kNaOrder = kNaOrig + kNaMaxBlocks * 4;         // u32 per block
 constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
@@ -639,7 +639,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   if (st != MPTC_OK) return st;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  uint32_t *done = reinterpret_cast<uint32_t *>(d->scratch + kNaDone);
+  uint64_t *done = reinterpret_cast<uint64_t *>(d->scratch + kNaDone);
   uint64_t *stb = stb_dev ? stb_dev : reinterpret_cast<uint64_t *>(d->scratch + kNaStb);
   int32_t *orig = reinterpret_cast<int32_t *>(d->scratch + kNaOrig);
   uint32_t *work = reinterpret_cast<uint32_t *>(d->scratch + kNaWork);
@@ -653,7 +653,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   // The scratch keeps the previous call's contents: clear the counters, and
   // the completion flags when no inter pass will write them.
   if (cudaMemsetAsync(work, 0, 8 * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
-  if (!prev_final_dev && cudaMemsetAsync(done, 0, nblk * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
+  if (!prev_final_dev && cudaMemsetAsync(done, 0, nblk * sizeof(uint64_t), s) != cudaSuccess) return MPTC_ECUDA;
   mptc::wavefront_order_kernel<<<(n + 255) / 256, 256, 0, s>>>(bw, bh, cfg->search_area, order);
   mptc::dxt1_encode_kernel<<<(n + 127) / 128, 128, 0, s>>>(rgb_dev, width, bw, n, stb, orig);
   mptc::SearchParams P;

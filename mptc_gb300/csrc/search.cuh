@@ -307,6 +307,10 @@ __device__ __forceinline__ int eval_candidate(const BlockTab &t, const PixelGrou
   return (int)((uint32_t)sse / 48u) - orig_err;
 }
 
+// Completion word of a final block: bit 32 set, the low half the block's
+// index word, which is all a waiting block reads of it.
+__device__ __forceinline__ uint64_t done_word(uint64_t blk) { return (1ull << 32) | (blk >> 32); }
+
 struct SearchParams {
   const uint8_t *rgb;
   const float4 *wdesc;    // weight sums of the previous frame's final blocks (inter)
@@ -315,7 +319,7 @@ struct SearchParams {
   const uint64_t *prev;   // previous frame's final blocks (inter)
   uint64_t *final_blk;
   uint16_t *motion;       // (x | y << 8) per block
-  uint32_t *done;         // per block: 1 once final (release/acquire)
+  uint64_t *done;         // per block: 0 while open, done_word(final block) once final
   uint32_t *work;         // dataflow work counter
   uint32_t *status;       // device status bits
   int width, bw, bh, sa, thr;
@@ -362,12 +366,15 @@ __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P
     }
     if (lane == 0) {
       const bool accept = st.min_e <= P.thr;
+      uint64_t word = 0;
       if (accept) {
         const int row = st.sel_pos / w2, col = st.sel_pos - (st.sel_pos / w2) * w2;
-        P.final_blk[idx] = st.sel_refit ? ((uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32)) : stb;
+        const uint64_t blk = st.sel_refit ? ((uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32)) : stb;
+        P.final_blk[idx] = blk;
         P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
+        word = done_word(blk);
       }
-      P.done[idx] = accept ? 1u : 0u;
+      P.done[idx] = word;
     }
     __syncwarp();
   }
@@ -392,31 +399,41 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
 
-// Waits until done[idx] != 0. Gives up after ~1 s, or at once when another
-// wait of this launch already gave up (sets kDevTimeout and returns false), so
-// a broken dependency can never hang the GPU: every later wait falls through.
-__device__ __forceinline__ bool wait_done(const uint32_t *done, size_t idx, uint32_t *status) {
-  if (ld_acquire(done + idx)) return true;
+// Completion words are read and written as single 64-bit words, so
+// publishing needs no fence and a waiter needs no second load.
+__device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(uint64_t *p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Waits until done[idx] != 0 and returns the word. Gives up after ~1 s, or at
+// once when another wait of this launch already gave up (sets kDevTimeout and
+// returns 0), so a broken dependency can never hang the GPU: every later wait
+// falls through.
+__device__ __forceinline__ uint64_t wait_done(const uint64_t *done, size_t idx, uint32_t *status) {
+  uint64_t w = ld_relaxed(done + idx);
+  if (w) return w;
   const uint64_t t0 = global_ns();
   for (uint32_t it = 0; it < (1u << 24); ++it) {
     __nanosleep(32);
-    if (ld_acquire(done + idx)) return true;
+    if ((w = ld_relaxed(done + idx)) != 0) return w;
     if ((it & 63u) == 63u) {
-      if (ld_acquire(status) & kDevTimeout) return false;
+      if (ld_acquire(status) & kDevTimeout) return 0;
       if (global_ns() - t0 > 1000000000ull) break;
     }
   }
   atomicOr(status, kDevTimeout);
-  return false;
+  return 0;
 }
 
 // Wavefront order of the intra dataflow. Block (x, y) reads, in this frame,
@@ -549,7 +566,6 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
   const int tid = threadIdx.x, lane = tid & 31;
   const int n_pend = n_pending_host >= 0 ? n_pending_host : (int)__ldcg(n_pending_dev);
   const int w2 = 2 * P.sa, npos = w2 * w2;
-  const uint32_t *fin_hi = reinterpret_cast<const uint32_t *>(P.final_blk) + 1;
   while (true) {
     if (tid == 0) s_claim = (int)atomicAdd(P.work, 1u);
     __syncthreads();
@@ -583,8 +599,9 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
       uint32_t cand = 0, eps = 0;
       if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
         const size_t nidx = (size_t)j * P.bw + i;
-        if (wait_done(P.done, nidx, P.status)) {
-          cand = __ldcg(fin_hi + 2 * nidx);
+        const uint64_t w = wait_done(P.done, nidx, P.status);
+        if (w) {
+          cand = (uint32_t)w;
           const WeightSums ws = weight_sums(cand, s_wk);
           e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
         }
@@ -603,7 +620,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
       }
       P.final_blk[idx] = blk;
       P.motion[idx] = m;
-      st_release(P.done + idx, 1u);  // orders the two stores above before the flag
+      st_relaxed(P.done + idx, done_word(blk));  // waiters read only this word
     }
     __syncthreads();
   }
@@ -615,11 +632,11 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
 constexpr int kPendTile = 4096;
 
 __global__ void __launch_bounds__(256) pending_count_kernel(const uint32_t *__restrict__ order,
-                                                            const uint32_t *__restrict__ done, int n,
+                                                            const uint64_t *__restrict__ done, int n,
                                                             uint32_t *__restrict__ tile_counts) {
   const int t0 = blockIdx.x * kPendTile;
   int c = 0;
-  for (int i = t0 + threadIdx.x; i < min(n, t0 + kPendTile); i += blockDim.x) c += __ldg(done + order[i]) == 0u;
+  for (int i = t0 + threadIdx.x; i < min(n, t0 + kPendTile); i += blockDim.x) c += __ldg(done + order[i]) == 0ull;
   c = __reduce_add_sync(kFull, c);
   __shared__ int s[8];
   if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
@@ -632,7 +649,7 @@ __global__ void __launch_bounds__(256) pending_count_kernel(const uint32_t *__re
 }
 
 __global__ void __launch_bounds__(256) pending_scatter_kernel(const uint32_t *__restrict__ order,
-                                                              const uint32_t *__restrict__ done, int n,
+                                                              const uint64_t *__restrict__ done, int n,
                                                               const uint32_t *__restrict__ tile_counts, int ntiles,
                                                               uint32_t *__restrict__ pending,
                                                               uint32_t *__restrict__ n_pending) {
@@ -653,7 +670,7 @@ __global__ void __launch_bounds__(256) pending_scatter_kernel(const uint32_t *__
   for (int c0 = t0; c0 < t1; c0 += 256) {
     const int i = c0 + threadIdx.x;
     const uint32_t blk = i < t1 ? order[i] : 0u;
-    const bool u = i < t1 && __ldg(done + blk) == 0u;
+    const bool u = i < t1 && __ldg(done + blk) == 0ull;
     const unsigned bal = __ballot_sync(kFull, u);
     if (lane == 0) s_warp[warp] = __popc(bal);
     __syncthreads();

@@ -224,3 +224,46 @@ def test_learned_stream_is_valid(torch_cuda):
         prev = fin
     enc.close()
     m.close()
+
+
+def test_learned_stream_decodes_bit_exactly(torch_cuda):
+    """The learned path's output is an MPTC stream like any other: written by
+    the host writer (pinned to the reference encoder's bytes) and rebuilt by
+    the decoder (pinned to the reference decoder), it gives back the learned
+    path's final blocks frame for frame."""
+    torch = torch_cuda
+    from mptc_gb300.decoder import decode_stream
+    from mptc_gb300.encoder import Encoder
+    from mptc_gb300.model import ProposalModel, sample_examples
+    from mptc_gb300.stream import write_stream
+    w, h, sa, thr, ui = 256, 256, 8, 5, 4
+    frames = StreamSpec(w, h, 8, seed=41).generate()
+    bw, bh = w // 4, h // 4
+    plain = Encoder(w, h, sa, thr, 16)
+    outs = [plain.encode_frame_host(f, want_stb=True) for f in frames]
+    outs = [(o.stb.copy(), o.final.copy(), o.motion.copy()) for o in outs]
+    plain.close()
+    m = ProposalModel(seed=3)
+    rng = np.random.default_rng(1)
+    dev = torch.device("cuda")
+    for step in range(30):
+        t = 1 + step % (len(frames) - 1)
+        ex = sample_examples(rng, bw, bh, sa, outs[t][2], outs[t - 1][1], 256, 16)
+        if ex is None:
+            continue
+        m.train_step(torch.from_numpy(frames[t].copy()).to(dev), w,
+                     torch.from_numpy(outs[t][0].view(np.int64)).to(dev),
+                     torch.from_numpy(ex.blocks).to(dev), torch.from_numpy(ex.cands.view(np.int32)).to(dev))
+    enc = Encoder(w, h, sa, thr, 16)
+    enc.set_model(m, 8)
+    learned = []
+    for f in frames:
+        o = enc.encode_frame_host(f)
+        learned.append((o.final.copy(), o.motion.copy(), o.unique.copy()))
+    enc.close()
+    m.close()
+    data = write_stream(learned, w, h, sa, ui)
+    dec = decode_stream(data)
+    assert len(dec) == len(frames)
+    for k, d in enumerate(dec):
+        np.testing.assert_array_equal(d, learned[k][0], err_msg=f"frame {k}")
