@@ -36,6 +36,10 @@ W, H, FRAMES, SA, THR, II = 1920, 1080, 120, 8, 5, 16
 # pixel sums + 3 mul + 3 add for the weight sums), 2x2 solve, rounding and
 # 5/6-bit snap, palette, 16-pixel squared error) and per stb block encode.
 C_CAND, C_DXT = 600, 1500
+# DRAM bytes (read + write) per launch of the search kernels on the 1080p
+# stream, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum);
+# the summaries under profiles/ give the commands.
+NCU_TRAFFIC: dict = {}
 
 
 def algo_bytes(kernel: str, n: int) -> int:
@@ -88,7 +92,29 @@ def cpu_sample(threads: int):
     t_intra, t_inter = t1 - t0, t2 - t1
     fps = FRAMES / (n_intra * t_intra + (FRAMES - n_intra) * t_inter)
     return fps, dict(t_intra=t_intra, t_inter=t_inter, intra_visited=r0.stats.intra_visited,
-                     inter_visited=r1.stats.inter_visited, inter_frame_intra_visited=r1.stats.intra_visited)
+                     inter_visited=r1.stats.inter_visited, inter_frame_intra_visited=r1.stats.intra_visited,
+                     inter_distinct=window_distinct(r0.final, stb1, W // 4, H // 4, SA))
+
+
+def window_distinct(prev_final: np.ndarray, stb: np.ndarray, bw: int, bh: int, sa: int) -> int:
+    """Sum over blocks of the distinct index words, other than the block's own,
+    among the in-bounds positions of its inter window: the candidate
+    evaluations a search that evaluates each distinct word once performs."""
+    from numpy.lib.stride_tricks import sliding_window_view
+    prev = (prev_final >> np.uint64(32)).astype(np.int64).reshape(bh, bw)
+    own = (stb >> np.uint64(32)).astype(np.int64).reshape(bh, bw)
+    pad = np.full((bh + 2 * sa, bw + 2 * sa), -1, np.int64)
+    pad[sa:sa + bh, sa:sa + bw] = prev
+    win = sliding_window_view(pad, (2 * sa, 2 * sa))[:bh, :bw]
+    total = 0
+    for y0 in range(0, bh, 16):
+        w = win[y0:y0 + 16].reshape(-1, 4 * sa * sa).copy()
+        o = own[y0:y0 + 16].reshape(-1, 1)
+        w[w == o] = -1
+        w.sort(axis=1)
+        d = (np.diff(w, axis=1) != 0).sum(axis=1) + 1 - (w[:, 0] == -1)
+        total += int(d.sum())
+    return total
 
 
 def run_reference(args, rank: int) -> None:
@@ -316,17 +342,23 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
         avg_s = tot / nl * 1e-3
         units = None
         if info is not None:
-            units = {"inter_search_kernel": info["inter_visited"],
-                     "intra_search_kernel": info["intra_visited"],
+            units = {"inter_dedup_kernel": info["inter_visited"],
+                     "intra_rows_kernel": info["intra_visited"],
                      "intra_search_kernel/inter_frame": info["inter_frame_intra_visited"],
                      "dxt1_encode_kernel": n}.get(name)
         if units is not None:
             per = C_DXT if name == "dxt1_encode_kernel" else C_CAND
+            ref_units = units
+            if name == "inter_dedup_kernel":
+                # the kernel evaluates each distinct index word of a window once
+                units = info["inter_distinct"]
             ach = units * per / avg_s / 1e9
             line["roofline"] = dict(bound="alu", achieved=round(ach, 1), peak=round(peak, 1), unit="Gop/s",
                                     frac=round(ach / peak, 4), kernel=name,
                                     units_per_launch=int(units), ops_per_unit=per,
-                                    traffic=None,
+                                    reference_units_per_launch=int(ref_units),
+                                    reference_frac=round(ref_units * per / avg_s / 1e9 / peak, 4),
+                                    traffic=NCU_TRAFFIC.get(name),
                                     hbm=dict(achieved_gbs=round(algo_bytes(name, n) / avg_s / 1e9, 2),
                                              peak_gbs=6782.1, bytes_per_launch=algo_bytes(name, n)),
                                     peak_note="measured fp32 add probe (libmptc_gb300 mptc_alu_probe), "

@@ -19,7 +19,7 @@
 
 namespace {
 
-constexpr int kSearchWarps = 8;     // inter search: warps per CTA, one block per warp
+constexpr int kSearchWarps = 4;     // inter search: warps per CTA, one block per warp
 constexpr int kIntraThreads = 256;  // intra search: one block per CTA
 
 }  // namespace
@@ -167,8 +167,8 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
 }
 
 enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_STATS, K_COUNT };
-const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_search_kernel",
-                                     "intra_search_kernel",     "intra_search_kernel/inter_frame",
+const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_dedup_kernel",
+                                     "intra_rows_kernel",       "intra_search_kernel/inter_frame",
                                      "unique_kernels",          "frame_stats_kernel"};
 
 cudaEvent_t pool_event(mptc_ctx *ctx) {
@@ -364,12 +364,10 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
       dim3 tg((ctx->bw + mptc::kTileW - 1) / mptc::kTileW, (ctx->bh + mptc::kTileH - 1) / mptc::kTileH);
       mptc::score_topk_kernel<<<tg, 128, smem, s>>>(ctx->femb, ctx->gemb, ctx->bw, ctx->bh, sa, ctx->topk_k, ctx->topk);
       mptc::learned_inter_kernel<8><<<(ctx->nblk + 7) / 8, 256, 0, s>>>(P, ctx->topk, ctx->topk_k, ctx->work + 6);
-    } else if (w == 4)
-      mptc::inter_search_kernel<4><<<grid, 4 * 32, 0, s>>>(P);
-    else if (w == 16)
-      mptc::inter_search_kernel<16><<<grid, 16 * 32, 0, s>>>(P);
+    } else if (w == 2)
+      mptc::inter_dedup_kernel<2><<<grid, 2 * 32, 0, s>>>(P);
     else
-      mptc::inter_search_kernel<8><<<grid, 8 * 32, 0, s>>>(P);
+      mptc::inter_dedup_kernel<4><<<(ctx->nblk + 3) / 4, 4 * 32, 0, s>>>(P);
     MPTC_CUDA(cudaGetLastError());
   } else {
     MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint64_t), s));
@@ -386,7 +384,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     if (prev_final_dev)
       mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->pending, ctx->work + 5, -1);
     else
-      mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
+      mptc::intra_rows_kernel<kIntraThreads><<<std::min(ig, ctx->bh), kIntraThreads, 0, s>>>(P);
   }
   MPTC_CUDA(cudaGetLastError());
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
@@ -674,12 +672,12 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   P.thr = cfg->err_threshold;
   if (prev_final_dev) {
     mptc::weight_desc_kernel<<<(n + 255) / 256, 256, 0, s>>>(prev_final_dev, n, wdesc);
-    mptc::inter_search_kernel<kSearchWarps><<<(n + kSearchWarps - 1) / kSearchWarps, kSearchWarps * 32, 0, s>>>(P);
+    mptc::inter_dedup_kernel<4><<<(n + 3) / 4, 4 * 32, 0, s>>>(P);
     mptc::pending_count_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles);
     mptc::pending_scatter_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles, ntiles, pend, work + 5);
     mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, pend, work + 5, -1);
   } else {
-    mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, order, nullptr, n);
+    mptc::intra_rows_kernel<kIntraThreads><<<std::min(d->intra_grid, bh), kIntraThreads, 0, s>>>(P);
   }
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
   mptc::unique_count_kernel<<<ntiles, 256, 0, s>>>(m16, n, tiles);
@@ -897,7 +895,7 @@ mptc_status mptc_batch_autotune(mptc_batch *b, const int32_t *is_intra, int32_t 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // trial steps re-encode the current inputs into the buffers of the next
   // real step (same parity), so the streams do not advance
-  const int warps[3] = {4, 8, 16};
+  const int warps[2] = {2, 4};
   const int sms = b->ctx[0]->sm_count;
   const int caps[5] = {0, 8 * sms, 4 * sms, 2 * sms, sms};
   cudaEvent_t e0, e1;

@@ -380,6 +380,149 @@ __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P
   }
 }
 
+// The same search with each distinct index word of the window evaluated once.
+// Refit, validity and error depend only on the block and the candidate index
+// word, so positions holding equal words get equal results; on smooth content
+// a 16x16 window holds few distinct words (about 15% of the positions on the
+// 1080p test stream). Per span of up to 256 positions (the whole window for
+// sa <= 8): the warp loads the candidates, inserts the distinct words other
+// than the block's own into a shared hash table (own word = empty marker: the
+// identity candidate needs no refit), evaluates the distinct words 32 at a
+// time, then runs the reference's selection over the positions in scan order
+// with the looked-up results, exactly as inter_search_kernel does.
+constexpr int kDedupSpan = 256;     // positions per dedup span (8 chunks)
+constexpr int kDedupBuckets = 512;  // hash buckets (load <= 1/2)
+
+struct DedupTab {
+  uint32_t key[kDedupBuckets];  // index word, or the block's own word when empty
+  uint16_t slot[kDedupBuckets];
+  uint32_t nidx[kDedupSpan];    // a window block holding each distinct word
+  int e[kDedupSpan];
+  uint32_t eps[kDedupSpan];
+};
+
+__device__ __forceinline__ uint32_t dedup_hash(uint32_t v) { return (v * 2654435761u) >> 23; }
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) inter_dedup_kernel(SearchParams P) {
+  __shared__ BlockTab s_tab[WARPS];
+  __shared__ DedupTab s_dd[WARPS];
+  __shared__ uint8_t s_snap5[256], s_snap6[256];
+  build_snap_tables(s_snap5, s_snap6);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  BlockTab &tab = s_tab[warp];
+  DedupTab &dd = s_dd[warp];
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
+  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
+  for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
+    const int by = idx / P.bw, bx = idx - by * P.bw;
+    const int sumsq = stage_block(tab, P.rgb, P.width, bx, by, lane);
+    const PixelGroups pg = load_groups(tab);
+    const uint64_t stb = P.stb[idx];
+    const uint32_t own = (uint32_t)(stb >> 32);
+    const int orig = P.orig_err[idx];
+    SelState st;
+    sel_init(st);
+    for (int span = 0; span < npos; span += kDedupSpan) {
+      for (int b = lane; b < kDedupBuckets; b += 32) dd.key[b] = own;
+      __syncwarp();
+      uint32_t lc[8];
+      int ls[8];
+      unsigned valid = 0;
+      int nuniq = 0;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int pos = span + 32 * c + lane;
+        const int row = pos / w2, col = pos - row * w2;
+        const int j = by - P.sa + row, i = bx - P.sa + col;
+        uint32_t cand = own, nidx = 0;
+        if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
+          nidx = (uint32_t)(j * P.bw + i);
+          cand = __ldg(prev_hi + 2 * (size_t)nidx);
+          valid |= 1u << c;
+        }
+        lc[c] = cand;
+        const bool need = cand != own;  // invalid positions hold `own` too
+        const unsigned peers = __match_any_sync(kFull, cand);
+        const int leader = __ffs(peers) - 1;
+        uint32_t b = dedup_hash(cand);
+        bool is_new = false, found = false;
+        if (need && lane == leader) {
+          for (int probe = 0; probe < kDedupBuckets; ++probe) {
+            const uint32_t old = atomicCAS(&dd.key[b], own, cand);
+            if (old == own) {
+              is_new = true;
+              break;
+            }
+            if (old == cand) {
+              found = true;
+              break;
+            }
+            b = (b + 1) & (kDedupBuckets - 1);
+          }
+        }
+        const unsigned newm = __ballot_sync(kFull, is_new);
+        int slot = -1;
+        if (is_new) {
+          slot = nuniq + __popc(newm & lt_mask);
+          dd.slot[b] = (uint16_t)slot;
+          dd.nidx[slot] = nidx;
+        } else if (found) {
+          slot = dd.slot[b];  // inserted by an earlier chunk of this span
+        }
+        ls[c] = __shfl_sync(kFull, slot, leader);
+        nuniq += __popc(newm);
+        __syncwarp();  // this chunk's slot writes land before later chunks read them
+      }
+      __syncwarp();
+      for (int k = lane; k < nuniq; k += 32) {
+        const uint32_t nidx = dd.nidx[k];
+        const uint32_t cand = __ldg(prev_hi + 2 * (size_t)nidx);
+        const float4 d = __ldg(P.wdesc + nidx);
+        const WeightSums ws{d.x, d.y, d.z, d.w};
+        uint32_t eps = 0;
+        int refit = 0;
+        dd.e[k] = eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+        dd.eps[k] = eps;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int pos = span + 32 * c + lane;
+        const int row = pos / w2;
+        int e = kInvalid, refit = 0;
+        uint32_t eps = 0;
+        if ((valid >> c) & 1u) {
+          if (lc[c] == own) {
+            e = 0;
+          } else {
+            e = dd.e[ls[c]];
+            eps = dd.eps[ls[c]];
+            refit = 1;
+          }
+        }
+        sel_chunk(st, lane, row, e, pos, lc[c], eps, refit);
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const bool accept = st.min_e <= P.thr;
+      uint64_t word = 0;
+      if (accept) {
+        const int row = st.sel_pos / w2, col = st.sel_pos - (st.sel_pos / w2) * w2;
+        const uint64_t blk = st.sel_refit ? ((uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32)) : stb;
+        P.final_blk[idx] = blk;
+        P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
+        word = done_word(blk);
+      }
+      P.done[idx] = word;
+    }
+    __syncwarp();
+  }
+}
+
 // Weight sums of the refit for every block's index word (the candidates the
 // next inter search reads), one thread per block.
 __global__ void __launch_bounds__(256) weight_desc_kernel(const uint64_t *__restrict__ blocks, int n,
@@ -623,6 +766,99 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
       st_relaxed(P.done + idx, done_word(blk));  // waiters read only this word
     }
     __syncthreads();
+  }
+}
+
+// Intra frames (every block open): the same search with one CTA per block
+// row. Rows are claimed in order and a CTA walks its row left to right, so the
+// window blocks of its own row (columns bx-sa .. bx-1) are the CTA's own
+// earlier results, kept in shared memory: the in-row dependency costs a
+// barrier instead of a trip through L2. Blocks of the rows above come from
+// their completion words, which each thread polls for its window position.
+// Before the first block of a row, thread 0 alone waits for block
+// (min(bw-1, sa-1), by-1), which is final only after row by-1 up to that
+// column and rows by-2 .. by-2sa+1 further right are, so a row that starts
+// early does not flood L2 with the polls of all its threads. A row only waits
+// on rows claimed earlier by running CTAs, so the dataflow cannot deadlock.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) intra_rows_kernel(SearchParams P) {
+  __shared__ BlockTab s_tab;
+  __shared__ uint8_t s_snap5[256], s_snap6[256];
+  __shared__ float4 s_wk[4];
+  __shared__ int s_red[2 * (THREADS / 32)];
+  __shared__ CtaSel s_sel;
+  __shared__ int s_claim, s_sumsq;
+  __shared__ uint32_t s_row[128];  // final index words of this row, column & 127 (sa <= 63)
+  build_snap_tables(s_snap5, s_snap6);
+  build_weight_table(s_wk);
+  CtaReduce<THREADS> red{s_red, 0};
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w2 = 2 * P.sa, npos = w2 * w2;
+  while (true) {
+    if (tid == 0) s_claim = (int)atomicAdd(P.work, 1u);
+    __syncthreads();
+    const int by = s_claim;
+    if (by >= P.bh) break;
+    for (int bx = 0; bx < P.bw; ++bx) {
+      const int idx = by * P.bw + bx;
+      if (tid < 32) {
+        const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
+        if (tid == 0) {
+          s_sumsq = sq;
+          s_sel.min_e = kInvalid;
+          s_sel.broken_row = -1;
+          s_sel.sel_pos = -1;
+          s_sel.sel_cand = 0;
+          s_sel.sel_eps = 0;
+          s_sel.sel_refit = 0;
+          if (by > 0 && bx == 0) wait_done(P.done, (size_t)(by - 1) * P.bw + min(P.bw - 1, P.sa - 1), P.status);
+        }
+      }
+      __syncthreads();
+      const uint64_t stb = __ldg(P.stb + idx);
+      const uint32_t own = (uint32_t)(stb >> 32);
+      const int orig = __ldg(P.orig_err + idx);
+      const int sumsq = s_sumsq;
+      const PixelGroups pg = load_groups(s_tab);
+      for (int base = 0; base < npos; base += THREADS) {
+        const int pos = base + tid;
+        const int row = pos / w2, col = pos - row * w2;
+        const int j = by - row, i = bx + P.sa - 1 - col;
+        int e = kInvalid, refit = 0;
+        uint32_t cand = 0, eps = 0;
+        if (pos < npos && i >= 0 && j >= 0 && i < P.bw && !(j == by && i >= bx)) {
+          bool ok = true;
+          if (j == by) {
+            cand = s_row[i & 127];
+          } else {
+            const uint64_t w = wait_done(P.done, (size_t)j * P.bw + i, P.status);
+            ok = w != 0;
+            cand = (uint32_t)w;
+          }
+          if (ok) {
+            const WeightSums ws = weight_sums(cand, s_wk);
+            e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+          }
+        }
+        cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
+      }
+      if (tid == 0) {
+        uint16_t m;
+        uint64_t blk = stb;
+        if (s_sel.min_e <= P.thr) {
+          const int row = s_sel.sel_pos / w2, col = s_sel.sel_pos - (s_sel.sel_pos / w2) * w2;
+          m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
+          if (s_sel.sel_refit) blk = (uint64_t)s_sel.sel_eps | ((uint64_t)s_sel.sel_cand << 32);
+        } else {
+          m = 0xFFFFu;
+        }
+        P.final_blk[idx] = blk;
+        P.motion[idx] = m;
+        s_row[bx & 127] = (uint32_t)(blk >> 32);
+        st_relaxed(P.done + idx, done_word(blk));
+      }
+      __syncthreads();
+    }
   }
 }
 
