@@ -17,8 +17,10 @@
 // are resolved by pointer jumping (log2(blocks) rounds) instead of the
 // reference's raster loop.
 //
-// One CTA per (64x64 tile, endpoint): the three planes sit in shared memory
-// as int16 (2 x 24 KiB, source and destination of each lifting pass).
+// Forward: one CTA per (64x64 tile, plane), two int16 tiles in shared memory
+// (source and destination of each lifting pass). Inverse: one CTA per
+// (tile, endpoint) with its three planes (2 x 24 KiB), which the RGB565
+// conversion needs together.
 #pragma once
 
 #include <cstdint>
@@ -32,12 +34,14 @@ constexpr int kCodecThreads = 256;
 // Mirror index into [0, len) for the indices the lifting uses (-1 and len).
 __device__ __forceinline__ int lift_mirror(int i, int len) { return i < 0 ? -i : (i >= len ? 2 * len - 2 - i : i); }
 
-// One forward lifting pass over `lines` lines of length `len` (power of two),
-// all three planes: element k of line l is at base + l*lstride + k*estride.
-// src -> dst, details in the upper half (codec/wavelet.cpp:30-66).
-__device__ __forceinline__ void forward_pass(const int16_t *src, int16_t *dst, int len, int lstride, int estride) {
+// One forward lifting pass over `lines` lines of length `len` (power of two)
+// of `planes` planes: element k of line l of plane p is at
+// p*kTileElems + l*lstride + k*estride. src -> dst, details in the upper half
+// (codec/wavelet.cpp:30-66).
+__device__ __forceinline__ void forward_pass(const int16_t *src, int16_t *dst, int planes, int len, int lstride,
+                                             int estride) {
   const int half = len >> 1;  // len is even: mid point == half
-  const int work = 3 * len * half;
+  const int work = planes * len * half;
   for (int w = threadIdx.x; w < work; w += blockDim.x) {
     const int p = w / (len * half), r = w - p * len * half;
     const int l = r / half, k = r - l * half;
@@ -84,31 +88,32 @@ __device__ __forceinline__ void inverse_pass(const int16_t *src, int16_t *dst, i
   __syncthreads();
 }
 
-// grid (bw/64, bh/64, 2 endpoints). coeff: 6 planes of bw*bh bytes,
+// grid (bw/64, bh/64, 6 planes: Y, Co, Cg of endpoint 1, then of endpoint 2),
+// one plane of one tile per CTA. coeff: 6 planes of bw*bh bytes,
 // [Y1 | Co1 | Cg1 | Y2 | Co2 | Cg2], each plane raster order over the image.
 __global__ void __launch_bounds__(kCodecThreads) endpoint_forward_kernel(const uint64_t *__restrict__ blocks, int bw,
                                                                          int bh, uint8_t *__restrict__ coeff) {
-  __shared__ int16_t a[3 * kTileElems], b[3 * kTileElems];
-  const int tx = blockIdx.x * kTile, ty = blockIdx.y * kTile, ep = blockIdx.z;
+  __shared__ int16_t a[kTileElems], b[kTileElems];
+  const int tx = blockIdx.x * kTile, ty = blockIdx.y * kTile, plane = blockIdx.z;
+  const int ep = plane / 3, channel = plane - 3 * ep;
   const size_t n = (size_t)bw * bh;
   for (int e = threadIdx.x; e < kTileElems; e += blockDim.x) {
     const int y = e >> 6, x = e & 63;
     const uint32_t lo = (uint32_t)blocks[(size_t)(ty + y) * bw + tx + x];
     const int c = (int)(ep ? (lo >> 16) : (lo & 0xFFFFu));
     const int r5 = c >> 11, g6 = (c >> 5) & 63, b5 = c & 31;
-    const int co = r5 - b5, t = r5 + b5 + (b5 >> 4), cg = g6 - t, yy = t + cg / 2;
-    a[e] = (int16_t)yy;
-    a[kTileElems + e] = (int16_t)co;
-    a[2 * kTileElems + e] = (int16_t)cg;
+    const int co = r5 - b5, t = r5 + b5 + (b5 >> 4), cg = g6 - t;
+    a[e] = (int16_t)(channel == 0 ? t + cg / 2 : (channel == 1 ? co : cg));
   }
   __syncthreads();
   for (int dim = kTile; dim > 1; dim >>= 1) {
-    forward_pass(a, b, dim, 1, kTile);      // columns: line = column, element stride = row
-    forward_pass(b, a, dim, kTile, 1);      // rows
+    forward_pass(a, b, 1, dim, 1, kTile);   // columns: line = column, element stride = row
+    forward_pass(b, a, 1, dim, kTile, 1);   // rows
   }
-  for (int e = threadIdx.x; e < 3 * kTileElems; e += blockDim.x) {
-    const int p = e >> 12, q = e & (kTileElems - 1), y = q >> 6, x = q & 63;
-    coeff[(size_t)(3 * ep + p) * n + (size_t)(ty + y) * bw + tx + x] = (uint8_t)((int)(int8_t)a[e] + 128);
+  uint8_t *out = coeff + (size_t)plane * n;
+  for (int e = threadIdx.x; e < kTileElems; e += blockDim.x) {
+    const int y = e >> 6, x = e & 63;
+    out[(size_t)(ty + y) * bw + tx + x] = (uint8_t)((int)(int8_t)a[e] + 128);
   }
 }
 

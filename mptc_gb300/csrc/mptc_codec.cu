@@ -51,7 +51,7 @@ mptc_status mptc_endpoint_coefficients(int32_t width, int32_t height, const uint
                                        uint8_t *coeff_dev, void *stream) {
   if (!tiled_size(width, height) || !blocks_dev || !coeff_dev) return MPTC_EINVAL;
   const int bw = width / 4, bh = height / 4;
-  const dim3 grid(bw / mptc::kTile, bh / mptc::kTile, 2);
+  const dim3 grid(bw / mptc::kTile, bh / mptc::kTile, 6);
   mptc::endpoint_forward_kernel<<<grid, mptc::kCodecThreads, 0, (cudaStream_t)stream>>>(blocks_dev, bw, bh,
                                                                                         coeff_dev);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;

@@ -62,7 +62,7 @@ def test_batch_autotune_keeps_results(torch_cuda):
             b.upload(k, streams[k][f])
         if f == 1:
             warps, ctas = b.autotune([False, False])
-            assert warps in (4, 8, 16) and ctas >= 0
+            assert warps in (2, 4) and ctas >= 0
         b.encode([flags[f]] * 2)
         for k in range(2):
             fin, mot, uni = b.fetch(k)
