@@ -386,12 +386,13 @@ __global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P
 // a 16x16 window holds few distinct words (about 15% of the positions on the
 // 1080p test stream). Per span of up to 256 positions (the whole window for
 // sa <= 8): the warp loads the candidates, inserts the distinct words other
-// than the block's own into a shared hash table (own word = empty marker: the
+// than the block's own into a shared hash table (open addressing with as many
+// buckets as positions, so an insertion always ends; own word = empty marker: the
 // identity candidate needs no refit), evaluates the distinct words 32 at a
 // time, then runs the reference's selection over the positions in scan order
 // with the looked-up results, exactly as inter_search_kernel does.
 constexpr int kDedupSpan = 256;     // positions per dedup span (8 chunks)
-constexpr int kDedupBuckets = 512;  // hash buckets (load <= 1/2)
+constexpr int kDedupBuckets = 256;  // hash buckets (a span has <= 256 distinct words)
 
 struct DedupTab {
   uint32_t key[kDedupBuckets];  // index word, or the block's own word when empty
@@ -401,10 +402,10 @@ struct DedupTab {
   uint32_t eps[kDedupSpan];
 };
 
-__device__ __forceinline__ uint32_t dedup_hash(uint32_t v) { return (v * 2654435761u) >> 23; }
+__device__ __forceinline__ uint32_t dedup_hash(uint32_t v) { return (v * 2654435761u) >> 24; }
 
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) inter_dedup_kernel(SearchParams P) {
+__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) inter_dedup_kernel(SearchParams P) {
   __shared__ BlockTab s_tab[WARPS];
   __shared__ DedupTab s_dd[WARPS];
   __shared__ uint8_t s_snap5[256], s_snap6[256];
@@ -428,22 +429,38 @@ __global__ void __launch_bounds__(WARPS * 32) inter_dedup_kernel(SearchParams P)
     for (int span = 0; span < npos; span += kDedupSpan) {
       for (int b = lane; b < kDedupBuckets; b += 32) dd.key[b] = own;
       __syncwarp();
-      uint32_t lc[8];
+      uint32_t lc[8], ln[8];
       int ls[8];
       unsigned valid = 0;
       int nuniq = 0;
+      // all candidate loads of the span first, so their latencies overlap
+      {
+        const int pos0 = span + lane;
+        int row = pos0 / w2, col = pos0 - row * w2;
+        const int drow = 32 / w2, dcol = 32 - drow * w2;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int pos = pos0 + 32 * c;
+          const int j = by - P.sa + row, i = bx - P.sa + col;
+          uint32_t cand = own, nidx = 0;
+          if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
+            nidx = (uint32_t)(j * P.bw + i);
+            cand = __ldg(prev_hi + 2 * (size_t)nidx);
+            valid |= 1u << c;
+          }
+          lc[c] = cand;
+          ln[c] = nidx;
+          row += drow;
+          col += dcol;
+          if (col >= w2) {
+            col -= w2;
+            ++row;
+          }
+        }
+      }
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const int pos = span + 32 * c + lane;
-        const int row = pos / w2, col = pos - row * w2;
-        const int j = by - P.sa + row, i = bx - P.sa + col;
-        uint32_t cand = own, nidx = 0;
-        if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
-          nidx = (uint32_t)(j * P.bw + i);
-          cand = __ldg(prev_hi + 2 * (size_t)nidx);
-          valid |= 1u << c;
-        }
-        lc[c] = cand;
+        const uint32_t cand = lc[c], nidx = ln[c];
         const bool need = cand != own;  // invalid positions hold `own` too
         const unsigned peers = __match_any_sync(kFull, cand);
         const int leader = __ffs(peers) - 1;
@@ -603,9 +620,19 @@ __global__ void __launch_bounds__(256) wavefront_order_kernel(int bw, int bh, in
   }
 }
 
+// Barrier over the THREADS threads that search: the whole CTA (BAR == 0) or
+// named barrier BAR when the CTA also holds a producer warp.
+template <int BAR, int THREADS>
+__device__ __forceinline__ void cta_barrier() {
+  if constexpr (BAR == 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(THREADS) : "memory");
+}
+
 // Block-wide reductions for the intra CTA (THREADS/32 warps). `buf` holds two
 // alternating rows of per-warp partials so one barrier per reduction suffices.
-template <int THREADS>
+template <int THREADS, int BAR = 0>
 struct CtaReduce {
   int *buf;  // [2][THREADS/32]
   int phase;
@@ -614,7 +641,7 @@ struct CtaReduce {
     int *b = buf + phase * (THREADS / 32);
     phase ^= 1;
     if ((threadIdx.x & 31) == 0) b[threadIdx.x >> 5] = w;
-    __syncthreads();
+    cta_barrier<BAR, THREADS>();
     int r = b[0];
 #pragma unroll
     for (int k = 1; k < THREADS / 32; ++k) r = r < b[k] ? r : b[k];
@@ -631,8 +658,8 @@ struct CtaSel {
 
 // The selection rule of the reference loop (as in sel_chunk) over one round
 // of THREADS consecutive scan positions, thread k holding position base + k.
-template <int THREADS>
-__device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red, int row, int e, int pos,
+template <int THREADS, int BAR = 0>
+__device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS, BAR> &red, int row, int e, int pos,
                                               uint32_t cand, uint32_t eps, int refit) {
   const int tid = threadIdx.x;
   const int min_e = s.min_e, broken = s.broken_row;
@@ -653,7 +680,7 @@ __device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red
       }
     }
     if (first != 0x7fffffff) {
-      __syncthreads();  // the update above lands before the first-e<=0 one
+      cta_barrier<BAR, THREADS>();  // the update above lands before the first-e<=0 one
       if (tid == first) {
         s.min_e = 0;
         s.sel_pos = pos;
@@ -662,14 +689,14 @@ __device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red
         s.sel_refit = refit;
         s.broken_row = row;
       }
-      __syncthreads();
+      cta_barrier<BAR, THREADS>();
       active = active && tid > first && row != s.broken_row;
     } else {
       active = false;  // min stays positive: no position of this round is <= 0
     }
   }
   if (min_e > 0 && first == 0x7fffffff) {
-    __syncthreads();
+    cta_barrier<BAR, THREADS>();
     return;
   }
   // min is 0: the first err_diff < 0 of the last row that has one wins.
@@ -682,7 +709,7 @@ __device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red
     s.sel_refit = refit;
     s.broken_row = row;
   }
-  __syncthreads();
+  cta_barrier<BAR, THREADS>();
 }
 
 // IntraSearch, codec/dxt_image.cpp:652-713, as a dataflow over the blocks
@@ -770,56 +797,96 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
 }
 
 // Intra frames (every block open): the same search with one CTA per block
-// row. Rows are claimed in order and a CTA walks its row left to right, so the
-// window blocks of its own row (columns bx-sa .. bx-1) are the CTA's own
-// earlier results, kept in shared memory: the in-row dependency costs a
-// barrier instead of a trip through L2. Blocks of the rows above come from
-// their completion words, which each thread polls for its window position.
+// row. Rows are claimed in order and a CTA walks its row left to right:
+// - the window blocks of its own row (columns bx-sa .. bx-1) are the CTA's own
+//   earlier results, kept in shared memory, so the in-row dependency costs a
+//   barrier instead of a trip through L2;
+// - blocks of the rows above come from their completion words; between two
+//   consecutive blocks the window moves by one column, so the words are cached
+//   in shared memory and only the new column is polled (sa <= 16);
+// - a producer warp stages the next block (pixel table, stb block and error)
+//   into the other half of a double buffer while the THREADS search threads
+//   work on the current one (named barriers: FULL when staged, EMPTY when
+//   consumed; the search threads reduce on their own named barrier).
 // Before the first block of a row, thread 0 alone waits for block
 // (min(bw-1, sa-1), by-1), which is final only after row by-1 up to that
 // column and rows by-2 .. by-2sa+1 further right are, so a row that starts
 // early does not flood L2 with the polls of all its threads. A row only waits
 // on rows claimed earlier by running CTAs, so the dataflow cannot deadlock.
+constexpr int kRowBarSearch = 1;   // search threads' reductions
+constexpr int kRowBarFull = 2;     // + buffer: staged (2, 3)
+constexpr int kRowBarEmpty = 4;    // + buffer: consumed (4, 5)
+constexpr int kRowCacheSa = 16;    // window-word cache for sa <= 16
+
+template <int N>
+__device__ __forceinline__ void named_sync(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(N) : "memory");
+}
+template <int N>
+__device__ __forceinline__ void named_arrive(int id) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "n"(N) : "memory");
+}
+
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) intra_rows_kernel(SearchParams P) {
-  __shared__ BlockTab s_tab;
+__global__ void __launch_bounds__(THREADS + 32) intra_rows_kernel(SearchParams P) {
+  constexpr int ALL = THREADS + 32;
+  __shared__ BlockTab s_tab[2];
+  __shared__ int s_sumsq[2], s_orig[2];
+  __shared__ uint64_t s_stb[2];
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
   __shared__ int s_red[2 * (THREADS / 32)];
   __shared__ CtaSel s_sel;
-  __shared__ int s_claim, s_sumsq;
-  __shared__ uint32_t s_row[128];  // final index words of this row, column & 127 (sa <= 63)
+  __shared__ int s_claim;
+  __shared__ uint32_t s_row[128];                        // this row's final words, column & 127
+  __shared__ uint32_t s_cache[2 * kRowCacheSa][32];      // rows above: [row][column & 31]
   build_snap_tables(s_snap5, s_snap6);
   build_weight_table(s_wk);
-  CtaReduce<THREADS> red{s_red, 0};
+  CtaReduce<THREADS, kRowBarSearch> red{s_red, 0};
   const int tid = threadIdx.x, lane = tid & 31;
+  const bool producer = tid >= THREADS;
   const int w2 = 2 * P.sa, npos = w2 * w2;
+  const bool cached = P.sa <= kRowCacheSa;
   while (true) {
     if (tid == 0) s_claim = (int)atomicAdd(P.work, 1u);
     __syncthreads();
     const int by = s_claim;
+    __syncthreads();  // everyone has read s_claim before it is rewritten
     if (by >= P.bh) break;
-    for (int bx = 0; bx < P.bw; ++bx) {
-      const int idx = by * P.bw + bx;
-      if (tid < 32) {
-        const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
-        if (tid == 0) {
-          s_sumsq = sq;
-          s_sel.min_e = kInvalid;
-          s_sel.broken_row = -1;
-          s_sel.sel_pos = -1;
-          s_sel.sel_cand = 0;
-          s_sel.sel_eps = 0;
-          s_sel.sel_refit = 0;
-          if (by > 0 && bx == 0) wait_done(P.done, (size_t)(by - 1) * P.bw + min(P.bw - 1, P.sa - 1), P.status);
+    if (producer) {
+      for (int bx = 0; bx < P.bw; ++bx) {
+        const int b = bx & 1;
+        if (bx >= 2) named_sync<ALL>(kRowBarEmpty + b);
+        const int idx = by * P.bw + bx;
+        const int sq = stage_block(s_tab[b], P.rgb, P.width, bx, by, lane);
+        if (lane == 0) {
+          s_sumsq[b] = sq;
+          s_stb[b] = __ldg(P.stb + idx);
+          s_orig[b] = __ldg(P.orig_err + idx);
         }
+        __syncwarp();
+        named_arrive<ALL>(kRowBarFull + b);
       }
-      __syncthreads();
-      const uint64_t stb = __ldg(P.stb + idx);
+      continue;
+    }
+    if (tid == 0 && by > 0) wait_done(P.done, (size_t)(by - 1) * P.bw + min(P.bw - 1, P.sa - 1), P.status);
+    for (int bx = 0; bx < P.bw; ++bx) {
+      const int b = bx & 1;
+      const int idx = by * P.bw + bx;
+      named_sync<ALL>(kRowBarFull + b);
+      if (tid == 0) {
+        s_sel.min_e = kInvalid;
+        s_sel.broken_row = -1;
+        s_sel.sel_pos = -1;
+        s_sel.sel_cand = 0;
+        s_sel.sel_eps = 0;
+        s_sel.sel_refit = 0;
+      }
+      const uint64_t stb = s_stb[b];
       const uint32_t own = (uint32_t)(stb >> 32);
-      const int orig = __ldg(P.orig_err + idx);
-      const int sumsq = s_sumsq;
-      const PixelGroups pg = load_groups(s_tab);
+      const int orig = s_orig[b], sumsq = s_sumsq[b];
+      const PixelGroups pg = load_groups(s_tab[b]);
+      cta_barrier<kRowBarSearch, THREADS>();  // s_sel initialised
       for (int base = 0; base < npos; base += THREADS) {
         const int pos = base + tid;
         const int row = pos / w2, col = pos - row * w2;
@@ -830,17 +897,20 @@ __global__ void __launch_bounds__(THREADS) intra_rows_kernel(SearchParams P) {
           bool ok = true;
           if (j == by) {
             cand = s_row[i & 127];
+          } else if (cached && col > 0 && bx > 0) {
+            cand = s_cache[row][i & 31];  // polled at an earlier block of this row
           } else {
             const uint64_t w = wait_done(P.done, (size_t)j * P.bw + i, P.status);
             ok = w != 0;
             cand = (uint32_t)w;
+            if (cached) s_cache[row][i & 31] = cand;
           }
           if (ok) {
             const WeightSums ws = weight_sums(cand, s_wk);
-            e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+            e = eval_candidate(s_tab[b], pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
           }
         }
-        cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
+        cta_sel_round<THREADS, kRowBarSearch>(s_sel, red, row, e, pos, cand, eps, refit);
       }
       if (tid == 0) {
         uint16_t m;
@@ -857,7 +927,8 @@ __global__ void __launch_bounds__(THREADS) intra_rows_kernel(SearchParams P) {
         s_row[bx & 127] = (uint32_t)(blk >> 32);
         st_relaxed(P.done + idx, done_word(blk));
       }
-      __syncthreads();
+      if (bx + 2 < P.bw) named_arrive<ALL>(kRowBarEmpty + b);
+      cta_barrier<kRowBarSearch, THREADS>();  // s_row / s_cache writes before the next block
     }
   }
 }
