@@ -585,7 +585,7 @@ __device__ __forceinline__ uint64_t wait_done(const uint64_t *done, size_t idx, 
   if (w) return w;
   const uint64_t t0 = global_ns();
   for (uint32_t it = 0; it < (1u << 24); ++it) {
-    __nanosleep(32);
+    if (it >= 256) __nanosleep(64);  // spin first: the awaited block is usually close
     if ((w = ld_relaxed(done + idx)) != 0) return w;
     if ((it & 63u) == 63u) {
       if (ld_acquire(status) & kDevTimeout) return 0;
