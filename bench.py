@@ -343,7 +343,7 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
         units = None
         if info is not None:
             units = {"inter_dedup_kernel": info["inter_visited"],
-                     "intra_rows_kernel": info["intra_visited"],
+                     "intra_search_kernel": info["intra_visited"],
                      "intra_search_kernel/inter_frame": info["inter_frame_intra_visited"],
                      "dxt1_encode_kernel": n}.get(name)
         if units is not None:

@@ -168,7 +168,7 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
 
 enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_STATS, K_COUNT };
 const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_dedup_kernel",
-                                     "intra_rows_kernel",       "intra_search_kernel/inter_frame",
+                                     "intra_search_kernel",     "intra_search_kernel/inter_frame",
                                      "unique_kernels",          "frame_stats_kernel"};
 
 cudaEvent_t pool_event(mptc_ctx *ctx) {
@@ -384,7 +384,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     if (prev_final_dev)
       mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->pending, ctx->work + 5, -1);
     else
-      mptc::intra_rows_kernel<kIntraThreads><<<std::min(ig, ctx->bh), kIntraThreads + 32, 0, s>>>(P);
+      mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
   }
   MPTC_CUDA(cudaGetLastError());
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
@@ -677,7 +677,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
     mptc::pending_scatter_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles, ntiles, pend, work + 5);
     mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, pend, work + 5, -1);
   } else {
-    mptc::intra_rows_kernel<kIntraThreads><<<std::min(d->intra_grid, bh), kIntraThreads + 32, 0, s>>>(P);
+    mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, order, nullptr, n);
   }
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
   mptc::unique_count_kernel<<<ntiles, 256, 0, s>>>(m16, n, tiles);

@@ -307,6 +307,87 @@ __device__ __forceinline__ int eval_candidate(const BlockTab &t, const PixelGrou
   return (int)((uint32_t)sse / 48u) - orig_err;
 }
 
+// The selection rule in closed form, for a warp that holds all positions of
+// a window spread over its lanes (each lane visits its positions in scan
+// order). The reference loop (if e < m { m = e; sel = pos; if e <= 0 { m = 0;
+// break the row } }) selects:
+// - if some valid position has e <= 0: let P0 be the first (scan order) and
+//   r0 its row. Later rows replace the selection with their first e < 0 (e < 0
+//   beats m = 0, then the row breaks), so the last row after r0 holding an
+//   e < 0 gives its first e < 0; without one the selection stays P0. Rows
+//   before r0 hold no e <= 0, and row r0 breaks at P0. m = 0.
+// - otherwise the first position of the minimum e (strict improvement), m = it.
+// Each lane keeps three candidates (first e <= 0; last-row-first e < 0 as the
+// key row << 16 | (0xFFFF - pos); first minimum) with their data; five warp
+// reductions give the result.
+struct SelPick {
+  uint32_t cand = 0, eps = 0;
+  int refit = 0;
+};
+struct LaneSel {
+  int le0_pos = 0x7fffffff;  // first position with e <= 0
+  SelPick le0;
+  int neg_key = -1;          // max over e < 0 of (row << 16 | (0xFFFF - pos))
+  SelPick neg;
+  int min_e = kInvalid, min_pos = 0x7fffffff;
+  SelPick mn;
+  __device__ __forceinline__ void add(int pos, int row, int e, uint32_t cand, uint32_t eps, int refit) {
+    if (e == kInvalid) return;
+    if (e <= 0 && pos < le0_pos) {
+      le0_pos = pos;
+      le0 = SelPick{cand, eps, refit};
+    }
+    if (e < 0) {
+      const int key = (row << 16) | (0xFFFF - pos);
+      if (key > neg_key) {
+        neg_key = key;
+        neg = SelPick{cand, eps, refit};
+      }
+    }
+    if (e < min_e) {  // positions arrive in increasing order: keeps the first minimum
+      min_e = e;
+      min_pos = pos;
+      mn = SelPick{cand, eps, refit};
+    }
+  }
+};
+struct SelResult {
+  int min_e, sel_pos, sel_refit;
+  uint32_t sel_cand, sel_eps;
+};
+
+__device__ __forceinline__ SelResult warp_select(const LaneSel &l, int lane, int w2) {
+  SelResult r;
+  const int p0 = __reduce_min_sync(kFull, l.le0_pos);
+  int owner, which;
+  if (p0 != 0x7fffffff) {
+    const int key = __reduce_max_sync(kFull, l.neg_key);
+    r.min_e = 0;
+    if (key >= 0 && (key >> 16) > p0 / w2) {
+      r.sel_pos = 0xFFFF - (key & 0xFFFF);
+      owner = __ffs(__ballot_sync(kFull, l.neg_key == key)) - 1;
+      which = 1;
+    } else {
+      r.sel_pos = p0;
+      owner = __ffs(__ballot_sync(kFull, l.le0_pos == p0)) - 1;
+      which = 0;
+    }
+  } else {
+    const int m = __reduce_min_sync(kFull, l.min_e);
+    r.min_e = m;
+    const int p = __reduce_min_sync(kFull, l.min_e == m ? l.min_pos : 0x7fffffff);
+    r.sel_pos = p == 0x7fffffff ? -1 : p;
+    owner = __ffs(__ballot_sync(kFull, l.min_e == m && l.min_pos == p)) - 1;
+    which = 2;
+  }
+  const SelPick &pk = which == 0 ? l.le0 : (which == 1 ? l.neg : l.mn);
+  r.sel_cand = __shfl_sync(kFull, pk.cand, owner);
+  r.sel_eps = __shfl_sync(kFull, pk.eps, owner);
+  r.sel_refit = __shfl_sync(kFull, pk.refit, owner);
+  (void)lane;
+  return r;
+}
+
 // Completion word of a final block: bit 32 set, the low half the block's
 // index word, which is all a waiting block reads of it.
 __device__ __forceinline__ uint64_t done_word(uint64_t blk) { return (1ull << 32) | (blk >> 32); }
@@ -329,68 +410,18 @@ struct SearchParams {
 // InterBlockSearch, codec/dxt_image.cpp:715-774: rows j = by-sa .. by+sa-1,
 // columns i = bx-sa .. bx+sa-1 (both ascending); motion (i-bx+sa)|0x80,
 // (j-by+sa)|0x80. Accepted blocks become final here; the others are left for
-// the intra pass (done = 0).
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) inter_search_kernel(SearchParams P) {
-  __shared__ BlockTab s_tab[WARPS];
-  __shared__ uint8_t s_snap5[256], s_snap6[256];
-  build_snap_tables(s_snap5, s_snap6);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  BlockTab &tab = s_tab[warp];
-  const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
-  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
-  for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
-    const int by = idx / P.bw, bx = idx - by * P.bw;
-    const int sumsq = stage_block(tab, P.rgb, P.width, bx, by, lane);
-    const PixelGroups pg = load_groups(tab);
-    const uint64_t stb = P.stb[idx];
-    const uint32_t own = (uint32_t)(stb >> 32);
-    const int orig = P.orig_err[idx];
-    SelState st;
-    sel_init(st);
-    for (int base = 0; base < npos; base += 32) {
-      const int pos = base + lane;
-      const int row = pos / w2, col = pos - row * w2;
-      const int j = by - P.sa + row, i = bx - P.sa + col;
-      int e = kInvalid, refit = 0;
-      uint32_t cand = 0, eps = 0;
-      if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
-        const size_t nidx = (size_t)j * P.bw + i;
-        cand = __ldg(prev_hi + 2 * nidx);
-        const float4 d = __ldg(P.wdesc + nidx);
-        const WeightSums ws{d.x, d.y, d.z, d.w};
-        e = eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
-      }
-      sel_chunk(st, lane, row, e, pos, cand, eps, refit);
-    }
-    if (lane == 0) {
-      const bool accept = st.min_e <= P.thr;
-      uint64_t word = 0;
-      if (accept) {
-        const int row = st.sel_pos / w2, col = st.sel_pos - (st.sel_pos / w2) * w2;
-        const uint64_t blk = st.sel_refit ? ((uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32)) : stb;
-        P.final_blk[idx] = blk;
-        P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
-        word = done_word(blk);
-      }
-      P.done[idx] = word;
-    }
-    __syncwarp();
-  }
-}
-
-// The same search with each distinct index word of the window evaluated once.
+// the intra pass (done = 0). One warp per block.
 // Refit, validity and error depend only on the block and the candidate index
-// word, so positions holding equal words get equal results; on smooth content
-// a 16x16 window holds few distinct words (about 15% of the positions on the
-// 1080p test stream). Per span of up to 256 positions (the whole window for
-// sa <= 8): the warp loads the candidates, inserts the distinct words other
-// than the block's own into a shared hash table (open addressing with as many
-// buckets as positions, so an insertion always ends; own word = empty marker: the
-// identity candidate needs no refit), evaluates the distinct words 32 at a
-// time, then runs the reference's selection over the positions in scan order
-// with the looked-up results, exactly as inter_search_kernel does.
+// word, so positions holding equal words get equal results, and each distinct
+// word of the window is evaluated once: on smooth content a 16x16 window holds
+// few distinct words (about 15% of the positions on the 1080p test stream).
+// Per span of up to 256 positions (the whole window for sa <= 8): the warp
+// loads the candidates, inserts the distinct words other than the block's own
+// into a shared hash table (open addressing with as many buckets as positions,
+// so an insertion always ends; own word = empty marker: the identity
+// candidate needs no refit), evaluates the distinct words 32 at a time and
+// records each position's result in the lane's selection statistics
+// (LaneSel); warp_select then applies the reference's selection rule.
 constexpr int kDedupSpan = 256;     // positions per dedup span (8 chunks)
 constexpr int kDedupBuckets = 256;  // hash buckets (a span has <= 256 distinct words)
 
@@ -424,8 +455,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) inter_dedup_kernel(Sea
     const uint64_t stb = P.stb[idx];
     const uint32_t own = (uint32_t)(stb >> 32);
     const int orig = P.orig_err[idx];
-    SelState st;
-    sel_init(st);
+    LaneSel ls_;
     for (int span = 0; span < npos; span += kDedupSpan) {
       for (int b = lane; b < kDedupBuckets; b += 32) dd.key[b] = own;
       __syncwarp();
@@ -507,23 +537,17 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) inter_dedup_kernel(Sea
       __syncwarp();
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const int pos = span + 32 * c + lane;
-        const int row = pos / w2;
-        int e = kInvalid, refit = 0;
-        uint32_t eps = 0;
         if ((valid >> c) & 1u) {
-          if (lc[c] == own) {
-            e = 0;
-          } else {
-            e = dd.e[ls[c]];
-            eps = dd.eps[ls[c]];
-            refit = 1;
-          }
+          const int pos = span + 32 * c + lane;
+          if (lc[c] == own)
+            ls_.add(pos, pos / w2, 0, own, 0u, 0);
+          else
+            ls_.add(pos, pos / w2, dd.e[ls[c]], lc[c], dd.eps[ls[c]], 1);
         }
-        sel_chunk(st, lane, row, e, pos, lc[c], eps, refit);
       }
       __syncwarp();
     }
+    const SelResult st = warp_select(ls_, lane, w2);
     if (lane == 0) {
       const bool accept = st.min_e <= P.thr;
       uint64_t word = 0;
@@ -620,19 +644,9 @@ __global__ void __launch_bounds__(256) wavefront_order_kernel(int bw, int bh, in
   }
 }
 
-// Barrier over the THREADS threads that search: the whole CTA (BAR == 0) or
-// named barrier BAR when the CTA also holds a producer warp.
-template <int BAR, int THREADS>
-__device__ __forceinline__ void cta_barrier() {
-  if constexpr (BAR == 0)
-    __syncthreads();
-  else
-    asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(THREADS) : "memory");
-}
-
 // Block-wide reductions for the intra CTA (THREADS/32 warps). `buf` holds two
 // alternating rows of per-warp partials so one barrier per reduction suffices.
-template <int THREADS, int BAR = 0>
+template <int THREADS>
 struct CtaReduce {
   int *buf;  // [2][THREADS/32]
   int phase;
@@ -641,7 +655,7 @@ struct CtaReduce {
     int *b = buf + phase * (THREADS / 32);
     phase ^= 1;
     if ((threadIdx.x & 31) == 0) b[threadIdx.x >> 5] = w;
-    cta_barrier<BAR, THREADS>();
+    __syncthreads();
     int r = b[0];
 #pragma unroll
     for (int k = 1; k < THREADS / 32; ++k) r = r < b[k] ? r : b[k];
@@ -658,8 +672,8 @@ struct CtaSel {
 
 // The selection rule of the reference loop (as in sel_chunk) over one round
 // of THREADS consecutive scan positions, thread k holding position base + k.
-template <int THREADS, int BAR = 0>
-__device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS, BAR> &red, int row, int e, int pos,
+template <int THREADS>
+__device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red, int row, int e, int pos,
                                               uint32_t cand, uint32_t eps, int refit) {
   const int tid = threadIdx.x;
   const int min_e = s.min_e, broken = s.broken_row;
@@ -680,7 +694,7 @@ __device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS, BAR>
       }
     }
     if (first != 0x7fffffff) {
-      cta_barrier<BAR, THREADS>();  // the update above lands before the first-e<=0 one
+      __syncthreads();  // the update above lands before the first-e<=0 one
       if (tid == first) {
         s.min_e = 0;
         s.sel_pos = pos;
@@ -689,14 +703,14 @@ __device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS, BAR>
         s.sel_refit = refit;
         s.broken_row = row;
       }
-      cta_barrier<BAR, THREADS>();
+      __syncthreads();
       active = active && tid > first && row != s.broken_row;
     } else {
       active = false;  // min stays positive: no position of this round is <= 0
     }
   }
   if (min_e > 0 && first == 0x7fffffff) {
-    cta_barrier<BAR, THREADS>();
+    __syncthreads();
     return;
   }
   // min is 0: the first err_diff < 0 of the last row that has one wins.
@@ -709,7 +723,7 @@ __device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS, BAR>
     s.sel_refit = refit;
     s.broken_row = row;
   }
-  cta_barrier<BAR, THREADS>();
+  __syncthreads();
 }
 
 // IntraSearch, codec/dxt_image.cpp:652-713, as a dataflow over the blocks
@@ -793,143 +807,6 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
       st_relaxed(P.done + idx, done_word(blk));  // waiters read only this word
     }
     __syncthreads();
-  }
-}
-
-// Intra frames (every block open): the same search with one CTA per block
-// row. Rows are claimed in order and a CTA walks its row left to right:
-// - the window blocks of its own row (columns bx-sa .. bx-1) are the CTA's own
-//   earlier results, kept in shared memory, so the in-row dependency costs a
-//   barrier instead of a trip through L2;
-// - blocks of the rows above come from their completion words; between two
-//   consecutive blocks the window moves by one column, so the words are cached
-//   in shared memory and only the new column is polled (sa <= 16);
-// - a producer warp stages the next block (pixel table, stb block and error)
-//   into the other half of a double buffer while the THREADS search threads
-//   work on the current one (named barriers: FULL when staged, EMPTY when
-//   consumed; the search threads reduce on their own named barrier).
-// Before the first block of a row, thread 0 alone waits for block
-// (min(bw-1, sa-1), by-1), which is final only after row by-1 up to that
-// column and rows by-2 .. by-2sa+1 further right are, so a row that starts
-// early does not flood L2 with the polls of all its threads. A row only waits
-// on rows claimed earlier by running CTAs, so the dataflow cannot deadlock.
-constexpr int kRowBarSearch = 1;   // search threads' reductions
-constexpr int kRowBarFull = 2;     // + buffer: staged (2, 3)
-constexpr int kRowBarEmpty = 4;    // + buffer: consumed (4, 5)
-constexpr int kRowCacheSa = 16;    // window-word cache for sa <= 16
-
-template <int N>
-__device__ __forceinline__ void named_sync(int id) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(N) : "memory");
-}
-template <int N>
-__device__ __forceinline__ void named_arrive(int id) {
-  asm volatile("bar.arrive %0, %1;" ::"r"(id), "n"(N) : "memory");
-}
-
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS + 32) intra_rows_kernel(SearchParams P) {
-  constexpr int ALL = THREADS + 32;
-  __shared__ BlockTab s_tab[2];
-  __shared__ int s_sumsq[2], s_orig[2];
-  __shared__ uint64_t s_stb[2];
-  __shared__ uint8_t s_snap5[256], s_snap6[256];
-  __shared__ float4 s_wk[4];
-  __shared__ int s_red[2 * (THREADS / 32)];
-  __shared__ CtaSel s_sel;
-  __shared__ int s_claim;
-  __shared__ uint32_t s_row[128];                        // this row's final words, column & 127
-  __shared__ uint32_t s_cache[2 * kRowCacheSa][32];      // rows above: [row][column & 31]
-  build_snap_tables(s_snap5, s_snap6);
-  build_weight_table(s_wk);
-  CtaReduce<THREADS, kRowBarSearch> red{s_red, 0};
-  const int tid = threadIdx.x, lane = tid & 31;
-  const bool producer = tid >= THREADS;
-  const int w2 = 2 * P.sa, npos = w2 * w2;
-  const bool cached = P.sa <= kRowCacheSa;
-  while (true) {
-    if (tid == 0) s_claim = (int)atomicAdd(P.work, 1u);
-    __syncthreads();
-    const int by = s_claim;
-    __syncthreads();  // everyone has read s_claim before it is rewritten
-    if (by >= P.bh) break;
-    if (producer) {
-      for (int bx = 0; bx < P.bw; ++bx) {
-        const int b = bx & 1;
-        if (bx >= 2) named_sync<ALL>(kRowBarEmpty + b);
-        const int idx = by * P.bw + bx;
-        const int sq = stage_block(s_tab[b], P.rgb, P.width, bx, by, lane);
-        if (lane == 0) {
-          s_sumsq[b] = sq;
-          s_stb[b] = __ldg(P.stb + idx);
-          s_orig[b] = __ldg(P.orig_err + idx);
-        }
-        __syncwarp();
-        named_arrive<ALL>(kRowBarFull + b);
-      }
-      continue;
-    }
-    if (tid == 0 && by > 0) wait_done(P.done, (size_t)(by - 1) * P.bw + min(P.bw - 1, P.sa - 1), P.status);
-    for (int bx = 0; bx < P.bw; ++bx) {
-      const int b = bx & 1;
-      const int idx = by * P.bw + bx;
-      named_sync<ALL>(kRowBarFull + b);
-      if (tid == 0) {
-        s_sel.min_e = kInvalid;
-        s_sel.broken_row = -1;
-        s_sel.sel_pos = -1;
-        s_sel.sel_cand = 0;
-        s_sel.sel_eps = 0;
-        s_sel.sel_refit = 0;
-      }
-      const uint64_t stb = s_stb[b];
-      const uint32_t own = (uint32_t)(stb >> 32);
-      const int orig = s_orig[b], sumsq = s_sumsq[b];
-      const PixelGroups pg = load_groups(s_tab[b]);
-      cta_barrier<kRowBarSearch, THREADS>();  // s_sel initialised
-      for (int base = 0; base < npos; base += THREADS) {
-        const int pos = base + tid;
-        const int row = pos / w2, col = pos - row * w2;
-        const int j = by - row, i = bx + P.sa - 1 - col;
-        int e = kInvalid, refit = 0;
-        uint32_t cand = 0, eps = 0;
-        if (pos < npos && i >= 0 && j >= 0 && i < P.bw && !(j == by && i >= bx)) {
-          bool ok = true;
-          if (j == by) {
-            cand = s_row[i & 127];
-          } else if (cached && col > 0 && bx > 0) {
-            cand = s_cache[row][i & 31];  // polled at an earlier block of this row
-          } else {
-            const uint64_t w = wait_done(P.done, (size_t)j * P.bw + i, P.status);
-            ok = w != 0;
-            cand = (uint32_t)w;
-            if (cached) s_cache[row][i & 31] = cand;
-          }
-          if (ok) {
-            const WeightSums ws = weight_sums(cand, s_wk);
-            e = eval_candidate(s_tab[b], pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
-          }
-        }
-        cta_sel_round<THREADS, kRowBarSearch>(s_sel, red, row, e, pos, cand, eps, refit);
-      }
-      if (tid == 0) {
-        uint16_t m;
-        uint64_t blk = stb;
-        if (s_sel.min_e <= P.thr) {
-          const int row = s_sel.sel_pos / w2, col = s_sel.sel_pos - (s_sel.sel_pos / w2) * w2;
-          m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
-          if (s_sel.sel_refit) blk = (uint64_t)s_sel.sel_eps | ((uint64_t)s_sel.sel_cand << 32);
-        } else {
-          m = 0xFFFFu;
-        }
-        P.final_blk[idx] = blk;
-        P.motion[idx] = m;
-        s_row[bx & 127] = (uint32_t)(blk >> 32);
-        st_relaxed(P.done + idx, done_word(blk));
-      }
-      if (bx + 2 < P.bw) named_arrive<ALL>(kRowBarEmpty + b);
-      cta_barrier<kRowBarSearch, THREADS>();  // s_row / s_cache writes before the next block
-    }
   }
 }
 
