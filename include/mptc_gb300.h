@@ -118,11 +118,11 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
  * calling cudaMalloc, and frame loops with a latency budget that cannot absorb
  * the allocator (cudaFree synchronises the whole device). It takes no context:
  * the caller passes the configuration, the frame size, the input frame and
- * every output buffer; the kernels' scratch (per-block completion flags, the
- * stb error of each block, the wavefront order and pending list of the intra
- * search, the refit weight sums of the previous frame's blocks, work counters,
- * tile counts) lives in one
- * file-scope device array of about 5.5 MiB inside the library, which every GPU
+ * every output buffer; the kernels' scratch (per-block completion words, the
+ * stb error of each block, the wavefront order, pending list and sweep
+ * estimates of the intra search, the refit weight sums of the previous frame's
+ * blocks, work counters, tile counts) lives in one
+ * file-scope device array of about 6.5 MiB inside the library, which every GPU
  * that loads the library holds until the process exits.
  *
  * Frames larger than MPTC_NOALLOC_MAX_BLOCKS blocks are rejected with

@@ -737,7 +737,9 @@ __device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, const uint32_t *__restrict__ pending,
                                                                const uint32_t *__restrict__ n_pending_dev,
-                                                               int n_pending_host) {
+                                                               int n_pending_host,
+                                                               const uint32_t *__restrict__ run_flag = nullptr) {
+  if (run_flag && __ldcg(run_flag) == 0u) return;  // the sweeps below converged
   __shared__ BlockTab s_tab;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
@@ -808,6 +810,108 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
     }
     __syncthreads();
   }
+}
+
+// Inter frames: the intra search of the blocks the inter pass left open, as
+// a fixed-point iteration instead of a dataflow. Each open block's result
+// depends only on the final index words of earlier blocks (causal order), so
+// the system x_b = F_b(x_earlier) has exactly one solution, and it is the only
+// fixed point. Sweep k evaluates every open block from the estimates of sweep
+// k-1 (cur; open blocks start at their stb word, i.e. as if unique, which most
+// open blocks on inter frames end up as) and writes its result (final block,
+// motion code, next estimate); when no estimate changed, the outputs of that
+// sweep are the reference's. A sweep runs only while the previous one changed
+// something (changed[k] != 0); if the last sweep still changed something, the
+// dataflow kernel recomputes the open blocks exactly. Sweeps have no waits:
+// every open block is independent within a sweep.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, const uint32_t *__restrict__ pending,
+                                                              const uint32_t *__restrict__ n_pending_dev,
+                                                              const uint32_t *__restrict__ cur,
+                                                              uint32_t *__restrict__ next,
+                                                              const uint32_t *__restrict__ changed_in,
+                                                              uint32_t *__restrict__ changed_out) {
+  if (__ldcg(changed_in) == 0u) return;
+  __shared__ BlockTab s_tab;
+  __shared__ uint8_t s_snap5[256], s_snap6[256];
+  __shared__ float4 s_wk[4];
+  __shared__ int s_red[2 * (THREADS / 32)];
+  __shared__ CtaSel s_sel;
+  __shared__ int s_sumsq;
+  build_snap_tables(s_snap5, s_snap6);
+  build_weight_table(s_wk);
+  CtaReduce<THREADS> red{s_red, 0};
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int n_pend = (int)__ldcg(n_pending_dev);
+  const int w2 = 2 * P.sa, npos = w2 * w2;
+  for (int k = blockIdx.x; k < n_pend; k += gridDim.x) {
+    const int idx = (int)__ldcg(pending + k);
+    const int by = idx / P.bw, bx = idx - by * P.bw;
+    if (tid < 32) {
+      const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
+      if (tid == 0) {
+        s_sumsq = sq;
+        s_sel.min_e = kInvalid;
+        s_sel.broken_row = -1;
+        s_sel.sel_pos = -1;
+        s_sel.sel_cand = 0;
+        s_sel.sel_eps = 0;
+        s_sel.sel_refit = 0;
+      }
+    }
+    __syncthreads();
+    const uint64_t stb = __ldg(P.stb + idx);
+    const uint32_t own = (uint32_t)(stb >> 32);
+    const int orig = __ldg(P.orig_err + idx);
+    const int sumsq = s_sumsq;
+    const PixelGroups pg = load_groups(s_tab);
+    for (int base = 0; base < npos; base += THREADS) {
+      const int pos = base + tid;
+      const int row = pos / w2, col = pos - row * w2;
+      const int j = by - row, i = bx + P.sa - 1 - col;
+      int e = kInvalid, refit = 0;
+      uint32_t cand = 0, eps = 0;
+      if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
+        const size_t nidx = (size_t)j * P.bw + i;
+        const uint64_t w = __ldcg(P.done + nidx);
+        cand = w ? (uint32_t)w : __ldcg(cur + nidx);
+        const WeightSums ws = weight_sums(cand, s_wk);
+        e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+      }
+      cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
+    }
+    if (tid == 0) {
+      uint16_t m;
+      uint64_t blk = stb;
+      if (s_sel.min_e <= P.thr) {
+        const int row = s_sel.sel_pos / w2, col = s_sel.sel_pos - (s_sel.sel_pos / w2) * w2;
+        m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
+        if (s_sel.sel_refit) blk = (uint64_t)s_sel.sel_eps | ((uint64_t)s_sel.sel_cand << 32);
+      } else {
+        m = 0xFFFFu;
+      }
+      P.final_blk[idx] = blk;
+      P.motion[idx] = m;
+      const uint32_t x = (uint32_t)(blk >> 32);
+      next[idx] = x;
+      if (x != __ldcg(cur + idx)) atomicOr(changed_out, 1u);
+    }
+    __syncthreads();
+  }
+}
+
+// Start of the sweeps: open blocks' estimates = their stb words; changed[0] = 1.
+__global__ void __launch_bounds__(256) sweep_init_kernel(const uint32_t *__restrict__ pending,
+                                                         const uint32_t *__restrict__ n_pending_dev,
+                                                         const uint64_t *__restrict__ stb, uint32_t *__restrict__ cur,
+                                                         uint32_t *__restrict__ changed, int n_flags) {
+  const int n_pend = (int)__ldcg(n_pending_dev);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_pend; k += gridDim.x * blockDim.x) {
+    const uint32_t idx = pending[k];
+    cur[idx] = (uint32_t)(stb[idx] >> 32);
+  }
+  if (blockIdx.x == 0)
+    for (int f = threadIdx.x; f < n_flags; f += blockDim.x) changed[f] = f == 0 ? 1u : 0u;
 }
 
 // Order-preserving compaction of the pending blocks (done == 0) of the
