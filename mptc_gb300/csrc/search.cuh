@@ -317,75 +317,36 @@ __device__ __forceinline__ int eval_candidate(const BlockTab &t, const PixelGrou
 //   e < 0 gives its first e < 0; without one the selection stays P0. Rows
 //   before r0 hold no e <= 0, and row r0 breaks at P0. m = 0.
 // - otherwise the first position of the minimum e (strict improvement), m = it.
-// Each lane keeps three candidates (first e <= 0; last-row-first e < 0 as the
-// key row << 16 | (0xFFFF - pos); first minimum) with their data; five warp
-// reductions give the result.
-struct SelPick {
-  uint32_t cand = 0, eps = 0;
-  int refit = 0;
-};
+// Each lane keeps the three positions (first e <= 0; the key
+// row << 16 | (0xFFFF - pos) of its e < 0 positions; first minimum); four warp
+// reductions give the selected position, whose candidate data the caller
+// recovers.
 struct LaneSel {
   int le0_pos = 0x7fffffff;  // first position with e <= 0
-  SelPick le0;
   int neg_key = -1;          // max over e < 0 of (row << 16 | (0xFFFF - pos))
-  SelPick neg;
   int min_e = kInvalid, min_pos = 0x7fffffff;
-  SelPick mn;
-  __device__ __forceinline__ void add(int pos, int row, int e, uint32_t cand, uint32_t eps, int refit) {
+  __device__ __forceinline__ void add(int pos, int row, int e) {
     if (e == kInvalid) return;
-    if (e <= 0 && pos < le0_pos) {
-      le0_pos = pos;
-      le0 = SelPick{cand, eps, refit};
-    }
-    if (e < 0) {
-      const int key = (row << 16) | (0xFFFF - pos);
-      if (key > neg_key) {
-        neg_key = key;
-        neg = SelPick{cand, eps, refit};
-      }
-    }
+    if (e <= 0 && pos < le0_pos) le0_pos = pos;
+    if (e < 0) neg_key = max(neg_key, (row << 16) | (0xFFFF - pos));
     if (e < min_e) {  // positions arrive in increasing order: keeps the first minimum
       min_e = e;
       min_pos = pos;
-      mn = SelPick{cand, eps, refit};
     }
   }
-};
-struct SelResult {
-  int min_e, sel_pos, sel_refit;
-  uint32_t sel_cand, sel_eps;
 };
 
-__device__ __forceinline__ SelResult warp_select(const LaneSel &l, int lane, int w2) {
-  SelResult r;
+// Returns the selected position (-1 when no position is valid) and its m.
+__device__ __forceinline__ int warp_select(const LaneSel &l, int w2, int &m) {
   const int p0 = __reduce_min_sync(kFull, l.le0_pos);
-  int owner, which;
   if (p0 != 0x7fffffff) {
+    m = 0;
     const int key = __reduce_max_sync(kFull, l.neg_key);
-    r.min_e = 0;
-    if (key >= 0 && (key >> 16) > p0 / w2) {
-      r.sel_pos = 0xFFFF - (key & 0xFFFF);
-      owner = __ffs(__ballot_sync(kFull, l.neg_key == key)) - 1;
-      which = 1;
-    } else {
-      r.sel_pos = p0;
-      owner = __ffs(__ballot_sync(kFull, l.le0_pos == p0)) - 1;
-      which = 0;
-    }
-  } else {
-    const int m = __reduce_min_sync(kFull, l.min_e);
-    r.min_e = m;
-    const int p = __reduce_min_sync(kFull, l.min_e == m ? l.min_pos : 0x7fffffff);
-    r.sel_pos = p == 0x7fffffff ? -1 : p;
-    owner = __ffs(__ballot_sync(kFull, l.min_e == m && l.min_pos == p)) - 1;
-    which = 2;
+    return (key >= 0 && (key >> 16) > p0 / w2) ? 0xFFFF - (key & 0xFFFF) : p0;
   }
-  const SelPick &pk = which == 0 ? l.le0 : (which == 1 ? l.neg : l.mn);
-  r.sel_cand = __shfl_sync(kFull, pk.cand, owner);
-  r.sel_eps = __shfl_sync(kFull, pk.eps, owner);
-  r.sel_refit = __shfl_sync(kFull, pk.refit, owner);
-  (void)lane;
-  return r;
+  m = __reduce_min_sync(kFull, l.min_e);
+  const int p = __reduce_min_sync(kFull, l.min_e == m ? l.min_pos : 0x7fffffff);
+  return p == 0x7fffffff ? -1 : p;
 }
 
 // Completion word of a final block: bit 32 set, the low half the block's
@@ -456,11 +417,11 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) inter_dedup_kernel(Sea
     const uint32_t own = (uint32_t)(stb >> 32);
     const int orig = P.orig_err[idx];
     LaneSel ls_;
+    int ls[8];  // slot of each of the lane's positions in the current span
     for (int span = 0; span < npos; span += kDedupSpan) {
       for (int b = lane; b < kDedupBuckets; b += 32) dd.key[b] = own;
       __syncwarp();
       uint32_t lc[8], ln[8];
-      int ls[8];
       unsigned valid = 0;
       int nuniq = 0;
       // all candidate loads of the span first, so their latencies overlap
@@ -539,27 +500,48 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) inter_dedup_kernel(Sea
       for (int c = 0; c < 8; ++c) {
         if ((valid >> c) & 1u) {
           const int pos = span + 32 * c + lane;
-          if (lc[c] == own)
-            ls_.add(pos, pos / w2, 0, own, 0u, 0);
-          else
-            ls_.add(pos, pos / w2, dd.e[ls[c]], lc[c], dd.eps[ls[c]], 1);
+          ls_.add(pos, pos / w2, lc[c] == own ? 0 : dd.e[ls[c]]);
         }
       }
       __syncwarp();
     }
-    const SelResult st = warp_select(ls_, lane, w2);
-    if (lane == 0) {
-      const bool accept = st.min_e <= P.thr;
-      uint64_t word = 0;
-      if (accept) {
-        const int row = st.sel_pos / w2, col = st.sel_pos - (st.sel_pos / w2) * w2;
-        const uint64_t blk = st.sel_refit ? ((uint64_t)st.sel_eps | ((uint64_t)st.sel_cand << 32)) : stb;
+    int m;
+    const int sel = warp_select(ls_, w2, m);
+    const bool accept = sel >= 0 && m <= P.thr;  // warp-uniform
+    uint64_t word = 0;
+    if (accept) {
+      // the selected position's index word and refit: the owning lane looks
+      // them up (one span) or evaluates the word again (several spans)
+      const int owner = sel & 31;
+      uint64_t blk = 0;
+      if (lane == owner) {
+        const int i = bx - P.sa + sel % w2, j = by - P.sa + sel / w2;
+        const uint32_t cand = __ldg(prev_hi + 2 * (size_t)(j * P.bw + i));
+        if (cand == own) {
+          blk = stb;
+        } else if (npos <= kDedupSpan) {
+          const int c = sel >> 5;
+          int slot = 0;
+#pragma unroll
+          for (int cc = 0; cc < 8; ++cc)
+            if (cc == c) slot = ls[cc];
+          blk = (uint64_t)dd.eps[slot] | ((uint64_t)cand << 32);
+        } else {
+          const float4 d = __ldg(P.wdesc + (size_t)(j * P.bw + i));
+          const WeightSums ws{d.x, d.y, d.z, d.w};
+          uint32_t eps = 0;
+          int refit = 0;
+          eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+          blk = (uint64_t)eps | ((uint64_t)cand << 32);
+        }
+        const int row = sel / w2, col = sel - row * w2;
         P.final_blk[idx] = blk;
         P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
         word = done_word(blk);
       }
-      P.done[idx] = word;
+      word = __shfl_sync(kFull, word, owner);
     }
+    if (lane == 0) P.done[idx] = word;
     __syncwarp();
   }
 }
