@@ -238,6 +238,10 @@ mptc_status mptc_set_kernel_timing(mptc_ctx *ctx, int32_t enable);
 mptc_status mptc_kernel_times(mptc_ctx *ctx, mptc_kernel_time *out, int32_t max_entries,
                               int32_t *n_entries);
 
+/* Number of kernels the library launched for this context since the last
+ * call (or since creation); clears the count. */
+mptc_status mptc_kernel_launches(mptc_ctx *ctx, uint64_t *count);
+
 /* Scalar-ALU throughput probe: `threads` x `iters` x 32 dependent-chain-free
  * fp32 add/int32 add pairs. Writes a checksum to *sink_dev (device int32) so
  * nothing is optimised away; the caller times the launch. Returns the op count

@@ -26,7 +26,7 @@ EXPORTED = [
     "mptc_model_grads", "mptc_model_embed", "mptc_model_save", "mptc_model_load",
     "mptc_ctx_set_model", "mptc_decoded_sse", "mptc_batch_set_model",
     "mptc_endpoint_coefficients", "mptc_decoder_create", "mptc_decoder_destroy", "mptc_decode_frame",
-    "mptc_decoder_check", "mptc_decoder_last_error",
+    "mptc_decoder_check", "mptc_decoder_last_error", "mptc_kernel_launches",
 ]
 
 NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
@@ -111,6 +111,7 @@ def lib() -> ctypes.CDLL:
         L.mptc_decoder_check.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_uint32)]
         L.mptc_decoder_last_error.argtypes = [vp]
         L.mptc_decoder_last_error.restype = ctypes.c_char_p
+        L.mptc_kernel_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
         L.mptc_version.restype = i32
         L.mptc_built_arch.restype = i32
         for name in EXPORTED:

@@ -21,6 +21,9 @@ mptc_status embed_workspace_alloc(EmbedWorkspace &ws, int rows);
 void embed_workspace_free(EmbedWorkspace &ws);
 
 // F[n x 64] = f(features of blocks 0..n-1 of a frame); G[n x 64] = g(words).
+// Kernels model_embed_frame launches per call (5 weight transposes, block
+// and candidate features, 5 GEMMs).
+constexpr int kEmbedLaunches = 12;
 mptc_status model_embed_frame(const mptc_model *m, EmbedWorkspace &ws, const uint8_t *rgb, int width,
                               const uint64_t *stb, int n, float *F, const uint32_t *words, int word_stride,
                               float *G, cudaStream_t s);

@@ -60,6 +60,7 @@ struct mptc_ctx {
   uint32_t last_is_intra = 0;
   std::string err;
   // opt-in per-kernel event timing
+  uint64_t launches = 0;       // kernels launched on this context (mptc_kernel_launches)
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
   struct Rec {
@@ -170,7 +171,7 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
 
 enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_STATS, K_COUNT };
 const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_dedup_kernel",
-                                     "intra_search_kernel",     "intra_search_kernel/inter_frame",
+                                     "intra_search_kernel",     "intra_sweep_kernel/inter_frame",
                                      "unique_kernels",          "frame_stats_kernel"};
 
 cudaEvent_t pool_event(mptc_ctx *ctx) {
@@ -262,6 +263,13 @@ extern "C" {
 int32_t mptc_version(void) { return 100; }
 int32_t mptc_built_arch(void) { return 1030; }
 
+mptc_status mptc_kernel_launches(mptc_ctx *ctx, uint64_t *count) {
+  if (!ctx || !count) return MPTC_EINVAL;
+  *count = ctx->launches;
+  ctx->launches = 0;
+  return MPTC_OK;
+}
+
 const char *mptc_last_error(const mptc_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t height, mptc_ctx **out_ctx) {
@@ -349,6 +357,7 @@ mptc_status mptc_dxt1_encode(mptc_ctx *ctx, const uint8_t *rgb_dev, uint64_t *bl
   int grid = (ctx->nblk + threads - 1) / threads;
   {
     KernelTimer t(ctx, K_DXT1, s);
+    ++ctx->launches;
     mptc::dxt1_encode_kernel<<<grid, threads, 0, s>>>(rgb_dev, ctx->width, ctx->bw, ctx->nblk, blocks_dev,
                                                        orig_err_dev);
   }
@@ -372,6 +381,9 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   if (prev_final_dev) {
     KernelTimer t(ctx, K_INTER, s);
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
+    // weight descriptors, the search (learned: embeddings, scoring, search),
+    // pending compaction, sweep init + sweeps + dataflow fallback
+    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 1) + 2 + 2 + kSweeps;
     const int w = ctx->inter_warps;
     const int grid = (ctx->nblk + w - 1) / w;
     if (ctx->model) {
@@ -407,6 +419,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
       launch_intra_sweeps(P, ctx->pending, ctx->work + 5, ctx->sweep, ctx->nblk, ig, s);
     else
       mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
+    if (!prev_final_dev) ++ctx->launches;
   }
   MPTC_CUDA(cudaGetLastError());
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
@@ -419,6 +432,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   {
     KernelTimer t(ctx, K_STATS, s);
     frame_stats_kernel<<<ctx->sm_count, 256, 0, s>>>(m16, ctx->nblk, ctx->work + 2);
+    ctx->launches += 3;  // unique count + scatter, frame stats
   }
   MPTC_CUDA(cudaGetLastError());
   ctx->last_is_intra = prev_final_dev ? 0u : 1u;

@@ -89,6 +89,12 @@ class Encoder:
         check(lib().mptc_ctx_set_model(self._ctx, model.handle if model is not None else None,
                                        int(k) if model is not None else 0), self._ctx)
 
+    def kernel_launches(self) -> int:
+        """Kernels launched on this context since the last call."""
+        n = ctypes.c_uint64()
+        check(lib().mptc_kernel_launches(self._ctx, ctypes.byref(n)), self._ctx)
+        return int(n.value)
+
     def set_kernel_timing(self, enable: bool) -> None:
         check(lib().mptc_set_kernel_timing(self._ctx, int(enable)), self._ctx)
 
