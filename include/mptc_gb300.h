@@ -49,7 +49,10 @@ typedef struct mptc_config {
   int32_t search_area;
   int32_t err_threshold;
   int32_t intra_interval;
-  int32_t reserved;
+  /* Fixed-point sweeps of an inter frame's intra pass before the exact
+   * dataflow pass takes over (results are identical either way): 0 = the
+   * default (6), negative = none (dataflow only), at most 32. */
+  int32_t intra_sweeps;
 } mptc_config;
 
 typedef struct mptc_ctx mptc_ctx;

@@ -34,7 +34,7 @@ NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
 
 class Config(ctypes.Structure):
     _fields_ = [("search_area", ctypes.c_int32), ("err_threshold", ctypes.c_int32),
-                ("intra_interval", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("intra_interval", ctypes.c_int32), ("intra_sweeps", ctypes.c_int32)]
 
 
 class FrameStats(ctypes.Structure):

@@ -21,7 +21,8 @@ namespace {
 
 constexpr int kSearchWarps = 4;     // inter search: warps per CTA, one block per warp
 constexpr int kIntraThreads = 256;  // intra search: one block per CTA
-constexpr int kSweeps = 6;          // fixed-point sweeps of an inter frame's intra pass
+constexpr int kSweeps = 6;          // default fixed-point sweeps of an inter frame's intra pass
+constexpr int kMaxSweeps = 32;
 
 }  // namespace
 
@@ -43,7 +44,7 @@ struct mptc_ctx {
   uint32_t *order = nullptr;       // blocks in wavefront order
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
   float4 *wdesc = nullptr;         // refit weight sums of the previous frame's blocks
-  uint32_t *sweep = nullptr;       // intra sweeps: 2 estimate buffers of n words + kSweeps + 1 change flags
+  uint32_t *sweep = nullptr;       // intra sweeps: 2 estimate buffers of n words + kMaxSweeps + 1 change flags
   uint32_t *tile_counts = nullptr; // per unique tile
   uint64_t *stb = nullptr;         // stb blocks (encode_frame / host path)
   int32_t *orig_err = nullptr;
@@ -244,16 +245,26 @@ namespace {
 // The intra pass of an inter frame: fixed-point sweeps over the open blocks,
 // then the exact dataflow kernel only if the sweeps did not converge.
 // sweep: 2 * n estimate words followed by kSweeps + 1 change flags.
-void launch_intra_sweeps(const mptc::SearchParams &P, const uint32_t *pending, const uint32_t *n_pending,
-                         uint32_t *sweep, int n, int grid, cudaStream_t s) {
+// Sweeps to run for a configuration's intra_sweeps value.
+int sweep_count(int32_t cfg) { return cfg == 0 ? kSweeps : (cfg < 0 ? 0 : std::min(cfg, kMaxSweeps)); }
+
+// sweep: 2 * n estimate words followed by kMaxSweeps + 1 change flags.
+// Returns the number of kernels launched.
+int launch_intra_sweeps(const mptc::SearchParams &P, const uint32_t *pending, const uint32_t *n_pending,
+                        uint32_t *sweep, int n, int grid, int sweeps, cudaStream_t s) {
+  if (sweeps == 0) {
+    mptc::intra_search_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, -1);
+    return 1;
+  }
   uint32_t *est[2] = {sweep, sweep + n}, *changed = sweep + 2 * (size_t)n;
-  mptc::sweep_init_kernel<<<64, 256, 0, s>>>(pending, n_pending, P.stb, est[0], changed, kSweeps + 1);
-  for (int k = 0; k < kSweeps; ++k)
+  mptc::sweep_init_kernel<<<64, 256, 0, s>>>(pending, n_pending, P.stb, est[0], changed, sweeps + 1);
+  for (int k = 0; k < sweeps; ++k)
     mptc::intra_sweep_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, est[k & 1],
                                                                            est[(k + 1) & 1], changed + k,
                                                                            changed + k + 1);
   mptc::intra_search_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, -1,
-                                                                          changed + kSweeps);
+                                                                          changed + sweeps);
+  return sweeps + 2;
 }
 
 }  // namespace
@@ -306,7 +317,7 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
       dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
       dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1) || dalloc(&ctx->order, n) ||
-      dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 2 * n + kSweeps + 1))
+      dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 2 * n + kMaxSweeps + 1))
     return bad(MPTC_ENOMEM);
   if (cudaMemset(ctx->work, 0, 8 * sizeof(uint32_t)) != cudaSuccess) return bad(MPTC_ECUDA);
   mptc::wavefront_order_kernel<<<(ctx->nblk + 255) / 256, 256>>>(ctx->bw, ctx->bh, cfg->search_area, ctx->order);
@@ -383,7 +394,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
     // weight descriptors, the search (learned: embeddings, scoring, search),
     // pending compaction, sweep init + sweeps + dataflow fallback
-    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 1) + 2 + 2 + kSweeps;
+    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 1) + 2;
     const int w = ctx->inter_warps;
     const int grid = (ctx->nblk + w - 1) / w;
     if (ctx->model) {
@@ -416,7 +427,8 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     KernelTimer t(ctx, prev_final_dev ? K_PENDING : K_INTRA, s);
     const int ig = ctx->intra_cap > 0 ? std::min(ctx->intra_cap, ctx->intra_grid) : ctx->intra_grid;
     if (prev_final_dev)
-      launch_intra_sweeps(P, ctx->pending, ctx->work + 5, ctx->sweep, ctx->nblk, ig, s);
+      ctx->launches += launch_intra_sweeps(P, ctx->pending, ctx->work + 5, ctx->sweep, ctx->nblk, ig,
+                                           sweep_count(ctx->cfg.intra_sweeps), s);
     else
       mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
     if (!prev_final_dev) ++ctx->launches;
@@ -607,7 +619,7 @@ constexpr size_t kNaOrder = kNaOrig + kNaMaxBlocks * 4;         // u32 per block
 constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
 constexpr size_t kNaWdesc = kNaPending + kNaMaxBlocks * 4;      // float4 per block
 constexpr size_t kNaSweep = kNaWdesc + kNaMaxBlocks * 16;       // u32: 2 per block + change flags
-constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // u32[8]
+constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // u32[8] (after kMaxSweeps + 1 flags)
 constexpr size_t kNaTileCounts = kNaWork + 256;                 // u32 per tile
 constexpr size_t kNaBytes = kNaTileCounts + ((kNaTiles * 4 + 255) / 256) * 256;
 
@@ -713,7 +725,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
     mptc::inter_dedup_kernel<4><<<(n + 3) / 4, 4 * 32, 0, s>>>(P);
     mptc::pending_count_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles);
     mptc::pending_scatter_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles, ntiles, pend, work + 5);
-    launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, s);
+    launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, sweep_count(cfg->intra_sweeps), s);
   } else {
     mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, order, nullptr, n);
   }

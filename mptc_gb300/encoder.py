@@ -27,12 +27,12 @@ class Encoder:
     """One MPTC stream of fixed resolution (width, height multiples of 4)."""
 
     def __init__(self, width: int, height: int, search_area: int = 8, err_threshold: int = 5,
-                 intra_interval: int = 16):
+                 intra_interval: int = 16, intra_sweeps: int = 0):
         self.width, self.height = width, height
         self.bw, self.bh = width // 4, height // 4
         self.nblk = self.bw * self.bh
         self.intra_interval = intra_interval
-        cfg = Config(search_area, err_threshold, intra_interval, 0)
+        cfg = Config(search_area, err_threshold, intra_interval, intra_sweeps)
         h = ctypes.c_void_p()
         check(lib().mptc_ctx_create(ctypes.byref(cfg), width, height, ctypes.byref(h)))
         self._ctx = h

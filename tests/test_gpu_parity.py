@@ -185,3 +185,21 @@ def test_gpu_deterministic_and_consistent_2160p(torch_cuda):
         assert (src < idx[intra]).all()  # causal
         np.testing.assert_array_equal(interp[intra], interp[src])
         prev_final = fin
+
+
+@pytest.mark.parametrize("sweeps", [-1, 1, 2, 32])
+def test_gpu_intra_pass_same_for_any_sweep_count(torch_cuda, sweeps):
+    """The inter frames' intra pass gives the reference's result whether the
+    fixed-point sweeps converge (many sweeps), stop early and hand over to the
+    dataflow kernel (1-2 sweeps) or are skipped (dataflow only)."""
+    from mptc_gb300.encoder import Encoder
+    spec = StreamSpec(256, 192, 4, seed=90, n_squares=3, square_size=48, speed_min=3, speed_max=5)
+    frames = spec.generate()
+    ref = oracle.encode_stream(frames, 6, 2, 16)
+    enc = Encoder(256, 192, 6, 2, 16, intra_sweeps=sweeps)
+    for k, f in enumerate(frames):
+        o = enc.encode_frame_host(f)
+        np.testing.assert_array_equal(o.final, ref[k].final, err_msg=f"frame {k} final")
+        np.testing.assert_array_equal(o.motion, ref[k].motion, err_msg=f"frame {k} motion")
+        np.testing.assert_array_equal(o.unique, ref[k].unique, err_msg=f"frame {k} unique")
+    enc.close()
