@@ -123,12 +123,13 @@ template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) learned_inter_kernel(SearchParams P, const uint16_t *__restrict__ topk,
                                                                   int K, uint32_t *__restrict__ fallbacks) {
   __shared__ BlockTab s_tab[WARPS];
+  __shared__ DedupTab s_dd[WARPS];
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   build_snap_tables(s_snap5, s_snap6);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   BlockTab &tab = s_tab[warp];
-  const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
+  const int nblk = P.bw * P.bh, w2 = 2 * P.sa;
   const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
   for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
     const int by = idx / P.bw, bx = idx - by * P.bw;
@@ -158,52 +159,25 @@ __global__ void __launch_bounds__(WARPS * 32) learned_inter_kernel(SearchParams 
     const bool pass = e != kInvalid && e <= 0 && e <= P.thr;
     const int key = pass ? ((e + 0x10000) << 8) | lane : 0x7fffffff;  // min err_diff, then best score
     const int best = __reduce_min_sync(kFull, key);
-    int sel_pos, sel_refit;
-    uint32_t sel_cand, sel_eps;
-    bool accept;
+    uint64_t word;
     if (best != 0x7fffffff) {
       const int who = best & 0xFF;
-      sel_pos = __shfl_sync(kFull, pos, who);
-      sel_cand = __shfl_sync(kFull, cand, who);
-      sel_eps = __shfl_sync(kFull, eps, who);
-      sel_refit = __shfl_sync(kFull, refit, who);
-      accept = true;
-    } else {
-      if (lane == 0) atomicAdd(fallbacks, 1u);
-      SelState st;
-      sel_init(st);
-      for (int base = 0; base < npos; base += 32) {
-        const int p = base + lane;
-        const int row = p / w2, col = p - row * w2;
-        const int j = by - P.sa + row, i = bx - P.sa + col;
-        int ee = kInvalid, rf = 0;
-        uint32_t c = 0, ep = 0;
-        if (p < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
-          const size_t nidx = (size_t)j * P.bw + i;
-          c = __ldg(prev_hi + 2 * nidx);
-          const float4 d = __ldg(P.wdesc + nidx);
-          const WeightSums ws{d.x, d.y, d.z, d.w};
-          ee = eval_candidate(tab, pg, s_snap5, s_snap6, c, ws, own, orig, sumsq, ep, rf);
-        }
-        sel_chunk(st, lane, row, ee, p, c, ep, rf);
-      }
-      accept = st.min_e <= P.thr;
-      sel_pos = st.sel_pos;
-      sel_cand = st.sel_cand;
-      sel_eps = st.sel_eps;
-      sel_refit = st.sel_refit;
-    }
-    if (lane == 0) {
-      uint64_t word = 0;
-      if (accept) {
-        const int row = sel_pos / w2, col = sel_pos - (sel_pos / w2) * w2;
-        const uint64_t blk = sel_refit ? ((uint64_t)sel_eps | ((uint64_t)sel_cand << 32)) : stb;
+      const int sel_pos = __shfl_sync(kFull, pos, who);
+      const uint32_t sel_cand = __shfl_sync(kFull, cand, who);
+      const uint32_t sel_eps = __shfl_sync(kFull, eps, who);
+      const int sel_refit = __shfl_sync(kFull, refit, who);
+      const uint64_t blk = sel_refit ? ((uint64_t)sel_eps | ((uint64_t)sel_cand << 32)) : stb;
+      if (lane == 0) {
+        const int row = sel_pos / w2, col = sel_pos - row * w2;
         P.final_blk[idx] = blk;
         P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
-        word = done_word(blk);
       }
-      P.done[idx] = word;
+      word = done_word(blk);
+    } else {
+      if (lane == 0) atomicAdd(fallbacks, 1u);
+      word = inter_block_search(P, tab, s_dd[warp], pg, s_snap5, s_snap6, idx, bx, by, stb, orig, sumsq, lane);
     }
+    if (lane == 0) P.done[idx] = word;
     __syncwarp();
   }
 }

@@ -408,7 +408,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
       const size_t smem = (size_t)nu8 * mptc::kEmb * 2 + 16 * mptc::kEmb * 2 + (size_t)16 * nu8 * 4;
       dim3 tg((ctx->bw + mptc::kTileW - 1) / mptc::kTileW, (ctx->bh + mptc::kTileH - 1) / mptc::kTileH);
       mptc::score_topk_kernel<<<tg, 128, smem, s>>>(ctx->femb, ctx->gemb, ctx->bw, ctx->bh, sa, ctx->topk_k, ctx->topk);
-      mptc::learned_inter_kernel<8><<<(ctx->nblk + 7) / 8, 256, 0, s>>>(P, ctx->topk, ctx->topk_k, ctx->work + 6);
+      mptc::learned_inter_kernel<4><<<(ctx->nblk + 3) / 4, 128, 0, s>>>(P, ctx->topk, ctx->topk_k, ctx->work + 6);
     } else if (w == 2)
       mptc::inter_dedup_kernel<2><<<grid, 2 * 32, 0, s>>>(P);
     else

@@ -396,6 +396,146 @@ struct DedupTab {
 
 __device__ __forceinline__ uint32_t dedup_hash(uint32_t v) { return (v * 2654435761u) >> 24; }
 
+// The exhaustive inter search of block idx by one warp: every distinct window
+// word evaluated once, the reference's selection, the final block and motion
+// code written when accepted. Returns the block's completion word (0: left
+// open for the intra pass), the same in every lane.
+__device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, const BlockTab &tab, DedupTab &dd,
+                                                       const PixelGroups &pg, const uint8_t *s_snap5,
+                                                       const uint8_t *s_snap6, int idx, int bx, int by,
+                                                       uint64_t stb, int orig, int sumsq, int lane) {
+  const uint32_t own = (uint32_t)(stb >> 32);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int w2 = 2 * P.sa, npos = w2 * w2;
+  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
+  LaneSel ls_;
+  int ls[8];  // slot of each of the lane's positions in the current span
+  for (int span = 0; span < npos; span += kDedupSpan) {
+    for (int b = lane; b < kDedupBuckets; b += 32) dd.key[b] = own;
+    __syncwarp();
+    uint32_t lc[8], ln[8];
+    unsigned valid = 0;
+    int nuniq = 0;
+    // all candidate loads of the span first, so their latencies overlap
+    {
+      const int pos0 = span + lane;
+      int row = pos0 / w2, col = pos0 - row * w2;
+      const int drow = 32 / w2, dcol = 32 - drow * w2;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int pos = pos0 + 32 * c;
+        const int j = by - P.sa + row, i = bx - P.sa + col;
+        uint32_t cand = own, nidx = 0;
+        if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
+          nidx = (uint32_t)(j * P.bw + i);
+          cand = __ldg(prev_hi + 2 * (size_t)nidx);
+          valid |= 1u << c;
+        }
+        lc[c] = cand;
+        ln[c] = nidx;
+        row += drow;
+        col += dcol;
+        if (col >= w2) {
+          col -= w2;
+          ++row;
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t cand = lc[c], nidx = ln[c];
+      const bool need = cand != own;  // invalid positions hold `own` too
+      const unsigned peers = __match_any_sync(kFull, cand);
+      const int leader = __ffs(peers) - 1;
+      uint32_t b = dedup_hash(cand);
+      bool is_new = false, found = false;
+      if (need && lane == leader) {
+        for (int probe = 0; probe < kDedupBuckets; ++probe) {
+          const uint32_t old = atomicCAS(&dd.key[b], own, cand);
+          if (old == own) {
+            is_new = true;
+            break;
+          }
+          if (old == cand) {
+            found = true;
+            break;
+          }
+          b = (b + 1) & (kDedupBuckets - 1);
+        }
+      }
+      const unsigned newm = __ballot_sync(kFull, is_new);
+      int slot = -1;
+      if (is_new) {
+        slot = nuniq + __popc(newm & lt_mask);
+        dd.slot[b] = (uint16_t)slot;
+        dd.nidx[slot] = nidx;
+      } else if (found) {
+        slot = dd.slot[b];  // inserted by an earlier chunk of this span
+      }
+      ls[c] = __shfl_sync(kFull, slot, leader);
+      nuniq += __popc(newm);
+      __syncwarp();  // this chunk's slot writes land before later chunks read them
+    }
+    __syncwarp();
+    for (int k = lane; k < nuniq; k += 32) {
+      const uint32_t nidx = dd.nidx[k];
+      const uint32_t cand = __ldg(prev_hi + 2 * (size_t)nidx);
+      const float4 d = __ldg(P.wdesc + nidx);
+      const WeightSums ws{d.x, d.y, d.z, d.w};
+      uint32_t eps = 0;
+      int refit = 0;
+      dd.e[k] = eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+      dd.eps[k] = eps;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if ((valid >> c) & 1u) {
+        const int pos = span + 32 * c + lane;
+        ls_.add(pos, pos / w2, lc[c] == own ? 0 : dd.e[ls[c]]);
+      }
+    }
+    __syncwarp();
+  }
+  int m;
+  const int sel = warp_select(ls_, w2, m);
+  const bool accept = sel >= 0 && m <= P.thr;  // warp-uniform
+  uint64_t word = 0;
+  if (accept) {
+    // the selected position's index word and refit: the owning lane looks
+    // them up (one span) or evaluates the word again (several spans)
+    const int owner = sel & 31;
+    uint64_t blk = 0;
+    if (lane == owner) {
+      const int i = bx - P.sa + sel % w2, j = by - P.sa + sel / w2;
+      const uint32_t cand = __ldg(prev_hi + 2 * (size_t)(j * P.bw + i));
+      if (cand == own) {
+        blk = stb;
+      } else if (npos <= kDedupSpan) {
+        const int c = sel >> 5;
+        int slot = 0;
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc)
+          if (cc == c) slot = ls[cc];
+        blk = (uint64_t)dd.eps[slot] | ((uint64_t)cand << 32);
+      } else {
+        const float4 d = __ldg(P.wdesc + (size_t)(j * P.bw + i));
+        const WeightSums ws{d.x, d.y, d.z, d.w};
+        uint32_t eps = 0;
+        int refit = 0;
+        eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+        blk = (uint64_t)eps | ((uint64_t)cand << 32);
+      }
+      const int row = sel / w2, col = sel - row * w2;
+      P.final_blk[idx] = blk;
+      P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
+      word = done_word(blk);
+    }
+    word = __shfl_sync(kFull, word, owner);
+  }
+  return word;
+}
+
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) inter_dedup_kernel(SearchParams P) {
   __shared__ BlockTab s_tab[WARPS];
@@ -405,142 +545,13 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) inter_dedup_kernel(Sea
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   BlockTab &tab = s_tab[warp];
-  DedupTab &dd = s_dd[warp];
-  const unsigned lt_mask = (1u << lane) - 1u;
-  const int nblk = P.bw * P.bh, w2 = 2 * P.sa, npos = w2 * w2;
-  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
+  const int nblk = P.bw * P.bh;
   for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
     const int by = idx / P.bw, bx = idx - by * P.bw;
     const int sumsq = stage_block(tab, P.rgb, P.width, bx, by, lane);
     const PixelGroups pg = load_groups(tab);
-    const uint64_t stb = P.stb[idx];
-    const uint32_t own = (uint32_t)(stb >> 32);
-    const int orig = P.orig_err[idx];
-    LaneSel ls_;
-    int ls[8];  // slot of each of the lane's positions in the current span
-    for (int span = 0; span < npos; span += kDedupSpan) {
-      for (int b = lane; b < kDedupBuckets; b += 32) dd.key[b] = own;
-      __syncwarp();
-      uint32_t lc[8], ln[8];
-      unsigned valid = 0;
-      int nuniq = 0;
-      // all candidate loads of the span first, so their latencies overlap
-      {
-        const int pos0 = span + lane;
-        int row = pos0 / w2, col = pos0 - row * w2;
-        const int drow = 32 / w2, dcol = 32 - drow * w2;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          const int pos = pos0 + 32 * c;
-          const int j = by - P.sa + row, i = bx - P.sa + col;
-          uint32_t cand = own, nidx = 0;
-          if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
-            nidx = (uint32_t)(j * P.bw + i);
-            cand = __ldg(prev_hi + 2 * (size_t)nidx);
-            valid |= 1u << c;
-          }
-          lc[c] = cand;
-          ln[c] = nidx;
-          row += drow;
-          col += dcol;
-          if (col >= w2) {
-            col -= w2;
-            ++row;
-          }
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const uint32_t cand = lc[c], nidx = ln[c];
-        const bool need = cand != own;  // invalid positions hold `own` too
-        const unsigned peers = __match_any_sync(kFull, cand);
-        const int leader = __ffs(peers) - 1;
-        uint32_t b = dedup_hash(cand);
-        bool is_new = false, found = false;
-        if (need && lane == leader) {
-          for (int probe = 0; probe < kDedupBuckets; ++probe) {
-            const uint32_t old = atomicCAS(&dd.key[b], own, cand);
-            if (old == own) {
-              is_new = true;
-              break;
-            }
-            if (old == cand) {
-              found = true;
-              break;
-            }
-            b = (b + 1) & (kDedupBuckets - 1);
-          }
-        }
-        const unsigned newm = __ballot_sync(kFull, is_new);
-        int slot = -1;
-        if (is_new) {
-          slot = nuniq + __popc(newm & lt_mask);
-          dd.slot[b] = (uint16_t)slot;
-          dd.nidx[slot] = nidx;
-        } else if (found) {
-          slot = dd.slot[b];  // inserted by an earlier chunk of this span
-        }
-        ls[c] = __shfl_sync(kFull, slot, leader);
-        nuniq += __popc(newm);
-        __syncwarp();  // this chunk's slot writes land before later chunks read them
-      }
-      __syncwarp();
-      for (int k = lane; k < nuniq; k += 32) {
-        const uint32_t nidx = dd.nidx[k];
-        const uint32_t cand = __ldg(prev_hi + 2 * (size_t)nidx);
-        const float4 d = __ldg(P.wdesc + nidx);
-        const WeightSums ws{d.x, d.y, d.z, d.w};
-        uint32_t eps = 0;
-        int refit = 0;
-        dd.e[k] = eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
-        dd.eps[k] = eps;
-      }
-      __syncwarp();
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        if ((valid >> c) & 1u) {
-          const int pos = span + 32 * c + lane;
-          ls_.add(pos, pos / w2, lc[c] == own ? 0 : dd.e[ls[c]]);
-        }
-      }
-      __syncwarp();
-    }
-    int m;
-    const int sel = warp_select(ls_, w2, m);
-    const bool accept = sel >= 0 && m <= P.thr;  // warp-uniform
-    uint64_t word = 0;
-    if (accept) {
-      // the selected position's index word and refit: the owning lane looks
-      // them up (one span) or evaluates the word again (several spans)
-      const int owner = sel & 31;
-      uint64_t blk = 0;
-      if (lane == owner) {
-        const int i = bx - P.sa + sel % w2, j = by - P.sa + sel / w2;
-        const uint32_t cand = __ldg(prev_hi + 2 * (size_t)(j * P.bw + i));
-        if (cand == own) {
-          blk = stb;
-        } else if (npos <= kDedupSpan) {
-          const int c = sel >> 5;
-          int slot = 0;
-#pragma unroll
-          for (int cc = 0; cc < 8; ++cc)
-            if (cc == c) slot = ls[cc];
-          blk = (uint64_t)dd.eps[slot] | ((uint64_t)cand << 32);
-        } else {
-          const float4 d = __ldg(P.wdesc + (size_t)(j * P.bw + i));
-          const WeightSums ws{d.x, d.y, d.z, d.w};
-          uint32_t eps = 0;
-          int refit = 0;
-          eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
-          blk = (uint64_t)eps | ((uint64_t)cand << 32);
-        }
-        const int row = sel / w2, col = sel - row * w2;
-        P.final_blk[idx] = blk;
-        P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
-        word = done_word(blk);
-      }
-      word = __shfl_sync(kFull, word, owner);
-    }
+    const uint64_t word = inter_block_search(P, tab, s_dd[warp], pg, s_snap5, s_snap6, idx, bx, by, P.stb[idx],
+                                             P.orig_err[idx], sumsq, lane);
     if (lane == 0) P.done[idx] = word;
     __syncwarp();
   }
