@@ -70,6 +70,22 @@ def intra_schedule(n: int, interval: int) -> list[bool]:
     return out
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest value of x over the ranks (the whole job's time): the
+    replicas' timings are reduced once, after the timed region."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units all ranks processed per second of the slowest rank."""
+    return world * units_per_rank / seconds
+
+
 # --------------------------------------------------------------------------
 # CPU baseline: the oracle (CPU restatement of the reference hot path)
 # --------------------------------------------------------------------------
@@ -272,12 +288,8 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
     enc.set_kernel_timing(False)
     ktimes = enc.kernel_times()
     launches = enc.kernel_launches()
-    elapsed_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        tt = torch.tensor([elapsed_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(tt.item())
-    value = world * nf * args.steps / (elapsed_ms * 1e-3)
+    elapsed_ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
+    value = whole_job_rate(nf * args.steps, world, elapsed_ms * 1e-3)
     st = enc.stats(stream)  # also raises on a device-side timeout
     if args.quick:
         if rank == 0:
@@ -307,12 +319,8 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         host_step()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = world * nf * e2e_steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e_value = whole_job_rate(nf * e2e_steps, world, e2e_s)
     h2d = nf * W * H * 3
     d2h = nf * (n * 8 + n * 2 + n * 4 + 12)
     e2e_enc.close()
@@ -419,13 +427,9 @@ def run_batch(args, rank: int, world: int, dist) -> None:
     if dist is not None:
         dist.barrier()
     clocks = clk.stop()
-    elapsed_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        tt = torch.tensor([elapsed_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(tt.item())
+    elapsed_ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     b.fetch(0)  # raises on a device-side timeout
-    value = world * S * nf * args.steps / (elapsed_ms * 1e-3)
+    value = whole_job_rate(S * nf * args.steps, world, elapsed_ms * 1e-3)
     if rank == 0:
         cfg = workload_config()
         cfg.update({"workload": f"batched 1080p MPTC encode: {S} concurrent streams x {nf} frames",
