@@ -67,66 +67,6 @@ struct WeightSums {
   float asq, bsq, ab, f;  // f = 1 / (asq*bsq - ab*ab)
 };
 
-// Selection state of the reference's candidate loop (warp-uniform).
-struct SelState {
-  int min_e;        // running min err_diff, kInvalid when nothing valid yet
-  int broken_row;   // row left by `break` (-1 none)
-  int sel_pos;      // scan position of the selection
-  uint32_t sel_cand;
-  uint32_t sel_eps;   // ep1 | ep2 << 16 (RGB565) of the refit, 0 for identity
-  int sel_refit;
-};
-
-__device__ __forceinline__ void sel_init(SelState &s) {
-  s.min_e = kInvalid;
-  s.broken_row = -1;
-  s.sel_pos = -1;
-  s.sel_cand = 0;
-  s.sel_eps = 0;
-  s.sel_refit = 0;
-}
-
-// One 32-position chunk (positions strictly increasing with the lane) of the
-// reference loop; `e` is kInvalid for skipped positions.
-__device__ __forceinline__ void sel_chunk(SelState &s, int lane, int row, int e, int pos, uint32_t cand,
-                                          uint32_t eps, int refit) {
-  bool active = (e != kInvalid) && (row != s.broken_row);
-  if (s.min_e > 0) {
-    const unsigned le0 = __ballot_sync(kFull, active && e <= 0);
-    const int first = le0 ? __ffs(le0) - 1 : 32;
-    const bool pre = active && lane < first;  // all positive here
-    const int m = __reduce_min_sync(kFull, pre ? e : kInvalid);
-    if (m < s.min_e) {
-      const int who = __ffs(__ballot_sync(kFull, pre && e == m)) - 1;
-      s.min_e = m;
-      s.sel_pos = __shfl_sync(kFull, pos, who);
-      s.sel_cand = __shfl_sync(kFull, cand, who);
-      s.sel_eps = __shfl_sync(kFull, eps, who);
-      s.sel_refit = __shfl_sync(kFull, refit, who);
-    }
-    if (!le0) return;
-    s.min_e = 0;
-    s.sel_pos = __shfl_sync(kFull, pos, first);
-    s.sel_cand = __shfl_sync(kFull, cand, first);
-    s.sel_eps = __shfl_sync(kFull, eps, first);
-    s.sel_refit = __shfl_sync(kFull, refit, first);
-    s.broken_row = __shfl_sync(kFull, row, first);
-    active = active && lane > first && row != s.broken_row;
-  }
-  // min is 0: only err_diff < 0 in a row not yet left can replace it, and the
-  // first such position of each later row does (then leaves that row).
-  const bool neg = active && e < 0;
-  if (__any_sync(kFull, neg)) {
-    const int maxrow = __reduce_max_sync(kFull, neg ? row : -1);
-    const int who = __ffs(__ballot_sync(kFull, neg && row == maxrow)) - 1;
-    s.sel_pos = __shfl_sync(kFull, pos, who);
-    s.sel_cand = __shfl_sync(kFull, cand, who);
-    s.sel_eps = __shfl_sync(kFull, eps, who);
-    s.sel_refit = __shfl_sync(kFull, refit, who);
-    s.broken_row = maxrow;
-  }
-}
-
 // ToFiveBits / ToSixBits (codec/dxt_image.cpp:72-121) as 256-entry tables,
 // built per CTA in shared memory: value -> snapped 8-bit value.
 __device__ __forceinline__ uint8_t snap_value(uint32_t x, uint32_t keep, uint32_t step, uint32_t sh) {
@@ -348,6 +288,37 @@ __device__ __forceinline__ int warp_select(const LaneSel &l, int w2, int &m) {
   const int p = __reduce_min_sync(kFull, l.min_e == m ? l.min_pos : 0x7fffffff);
   return p == 0x7fffffff ? -1 : p;
 }
+
+// The same closed form for a CTA whose threads each hold positions base + tid
+// of successive rounds, keeping for each of the three statistics the
+// candidate data of its position (the owner of the selected position writes
+// the result).
+struct SelPick {
+  uint32_t cand = 0, eps = 0;
+  int refit = 0;
+};
+struct ThreadSel : LaneSel {
+  SelPick le0, neg, mn;
+  __device__ __forceinline__ void add(int pos, int row, int e, uint32_t cand, uint32_t eps, int refit) {
+    if (e == kInvalid) return;
+    if (e <= 0 && pos < le0_pos) {
+      le0_pos = pos;
+      le0 = SelPick{cand, eps, refit};
+    }
+    if (e < 0) {
+      const int key = (row << 16) | (0xFFFF - pos);
+      if (key > neg_key) {
+        neg_key = key;
+        neg = SelPick{cand, eps, refit};
+      }
+    }
+    if (e < min_e) {
+      min_e = e;
+      min_pos = pos;
+      mn = SelPick{cand, eps, refit};
+    }
+  }
+};
 
 // Completion word of a final block: bit 32 set, the low half the block's
 // index word, which is all a waiting block reads of it.
@@ -657,66 +628,57 @@ struct CtaReduce {
   __device__ __forceinline__ int max(int v) { return -min(-v); }
 };
 
-// Selection state shared by the CTA (written by one thread between barriers).
-struct CtaSel {
-  int min_e, broken_row, sel_pos, sel_refit;
-  uint32_t sel_cand, sel_eps;
-};
-
-// The selection rule of the reference loop (as in sel_chunk) over one round
-// of THREADS consecutive scan positions, thread k holding position base + k.
+// Closed-form selection over the CTA (see LaneSel): two or three block-wide
+// reductions. Returns the selected position (-1: none valid), its m, and in
+// `pick` the statistic that holds it (0 first e <= 0, 1 last-row e < 0, 2
+// first minimum); the position's owner is thread sel % THREADS.
 template <int THREADS>
-__device__ __forceinline__ void cta_sel_round(CtaSel &s, CtaReduce<THREADS> &red, int row, int e, int pos,
-                                              uint32_t cand, uint32_t eps, int refit) {
-  const int tid = threadIdx.x;
-  const int min_e = s.min_e, broken = s.broken_row;
-  bool active = (e != kInvalid) && (row != broken);
-  int first = 0x7fffffff;
-  if (min_e > 0) {
-    first = red.min(active && e <= 0 ? tid : 0x7fffffff);
-    const bool pre = active && tid < first;  // all positive here
-    const int m = red.min(pre ? e : kInvalid);
-    if (m < min_e) {
-      const int who = red.min(pre && e == m ? tid : 0x7fffffff);
-      if (tid == who) {
-        s.min_e = m;
-        s.sel_pos = pos;
-        s.sel_cand = cand;
-        s.sel_eps = eps;
-        s.sel_refit = refit;
-      }
+__device__ __forceinline__ int cta_select(const LaneSel &t, CtaReduce<THREADS> &red, int w2, int &m, int &pick) {
+  const int p0 = red.min(t.le0_pos);
+  if (p0 != 0x7fffffff) {
+    m = 0;
+    const int key = red.max(t.neg_key);
+    if (key >= 0 && (key >> 16) > p0 / w2) {
+      pick = 1;
+      return 0xFFFF - (key & 0xFFFF);
     }
-    if (first != 0x7fffffff) {
-      __syncthreads();  // the update above lands before the first-e<=0 one
-      if (tid == first) {
-        s.min_e = 0;
-        s.sel_pos = pos;
-        s.sel_cand = cand;
-        s.sel_eps = eps;
-        s.sel_refit = refit;
-        s.broken_row = row;
-      }
-      __syncthreads();
-      active = active && tid > first && row != s.broken_row;
-    } else {
-      active = false;  // min stays positive: no position of this round is <= 0
+    pick = 0;
+    return p0;
+  }
+  m = red.min(t.min_e);
+  const int p = red.min(t.min_e == m ? t.min_pos : 0x7fffffff);
+  pick = 2;
+  return p == 0x7fffffff ? -1 : p;
+}
+
+// Selection and output of one block of the intra search: the CTA reduces
+// the threads' statistics, then one thread writes the final block and motion
+// code (and, when `publish`, the block's completion word). Returns the
+// block's completion word in that thread and 0 in the others. Ends with a
+// barrier.
+template <int THREADS>
+__device__ __forceinline__ uint64_t publish_intra(const SearchParams &P, const ThreadSel &ts, CtaReduce<THREADS> &red,
+                                                  int idx, uint64_t stb, int w2, int tid, bool publish) {
+  int m, pick;
+  const int sel = cta_select<THREADS>(ts, red, w2, m, pick);
+  const bool accept = sel >= 0 && m <= P.thr;
+  uint64_t out = 0;
+  if (accept ? tid == sel % THREADS : tid == 0) {
+    uint16_t code = 0xFFFFu;
+    uint64_t blk = stb;
+    if (accept) {
+      const SelPick &pk = pick == 0 ? ts.le0 : (pick == 1 ? ts.neg : ts.mn);
+      const int row = sel / w2, col = sel - row * w2;
+      code = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
+      if (pk.refit) blk = (uint64_t)pk.eps | ((uint64_t)pk.cand << 32);
     }
-  }
-  if (min_e > 0 && first == 0x7fffffff) {
-    __syncthreads();
-    return;
-  }
-  // min is 0: the first err_diff < 0 of the last row that has one wins.
-  const bool neg = active && e < 0;
-  const int key = red.max(neg ? ((row << 16) | (0xFFFF - tid)) : -1);
-  if (key >= 0 && tid == 0xFFFF - (key & 0xFFFF)) {
-    s.sel_pos = pos;
-    s.sel_cand = cand;
-    s.sel_eps = eps;
-    s.sel_refit = refit;
-    s.broken_row = row;
+    P.final_blk[idx] = blk;
+    P.motion[idx] = code;
+    if (publish) st_relaxed(P.done + idx, done_word(blk));  // waiters read only this word
+    out = done_word(blk);
   }
   __syncthreads();
+  return out;
 }
 
 // IntraSearch, codec/dxt_image.cpp:652-713, as a dataflow over the blocks
@@ -737,7 +699,6 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
   __shared__ int s_red[2 * (THREADS / 32)];
-  __shared__ CtaSel s_sel;
   __shared__ int s_claim, s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
   build_weight_table(s_wk);
@@ -754,15 +715,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
     const int by = idx / P.bw, bx = idx - by * P.bw;
     if (tid < 32) {
       const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
-      if (tid == 0) {
-        s_sumsq = sq;
-        s_sel.min_e = kInvalid;
-        s_sel.broken_row = -1;
-        s_sel.sel_pos = -1;
-        s_sel.sel_cand = 0;
-        s_sel.sel_eps = 0;
-        s_sel.sel_refit = 0;
-      }
+      if (tid == 0) s_sumsq = sq;
     }
     __syncthreads();
     const uint64_t stb = __ldg(P.stb + idx);
@@ -770,38 +723,25 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
     const int orig = __ldg(P.orig_err + idx);
     const int sumsq = s_sumsq;
     const PixelGroups pg = load_groups(s_tab);
+    ThreadSel ts;
     for (int base = 0; base < npos; base += THREADS) {
       const int pos = base + tid;
       const int row = pos / w2, col = pos - row * w2;
       const int j = by - row, i = bx + P.sa - 1 - col;
-      int e = kInvalid, refit = 0;
-      uint32_t cand = 0, eps = 0;
       if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
         const size_t nidx = (size_t)j * P.bw + i;
         const uint64_t w = wait_done(P.done, nidx, P.status);
         if (w) {
-          cand = (uint32_t)w;
+          const uint32_t cand = (uint32_t)w;
+          uint32_t eps = 0;
+          int refit = 0;
           const WeightSums ws = weight_sums(cand, s_wk);
-          e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+          const int e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+          ts.add(pos, row, e, cand, eps, refit);
         }
       }
-      cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
     }
-    if (tid == 0) {
-      uint16_t m;
-      uint64_t blk = stb;
-      if (s_sel.min_e <= P.thr) {
-        const int row = s_sel.sel_pos / w2, col = s_sel.sel_pos - (s_sel.sel_pos / w2) * w2;
-        m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
-        if (s_sel.sel_refit) blk = (uint64_t)s_sel.sel_eps | ((uint64_t)s_sel.sel_cand << 32);
-      } else {
-        m = 0xFFFFu;
-      }
-      P.final_blk[idx] = blk;
-      P.motion[idx] = m;
-      st_relaxed(P.done + idx, done_word(blk));  // waiters read only this word
-    }
-    __syncthreads();
+    publish_intra(P, ts, red, idx, stb, w2, tid, true);
   }
 }
 
@@ -829,7 +769,6 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
   __shared__ int s_red[2 * (THREADS / 32)];
-  __shared__ CtaSel s_sel;
   __shared__ int s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
   build_weight_table(s_wk);
@@ -842,15 +781,7 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
     const int by = idx / P.bw, bx = idx - by * P.bw;
     if (tid < 32) {
       const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
-      if (tid == 0) {
-        s_sumsq = sq;
-        s_sel.min_e = kInvalid;
-        s_sel.broken_row = -1;
-        s_sel.sel_pos = -1;
-        s_sel.sel_cand = 0;
-        s_sel.sel_eps = 0;
-        s_sel.sel_refit = 0;
-      }
+      if (tid == 0) s_sumsq = sq;
     }
     __syncthreads();
     const uint64_t stb = __ldg(P.stb + idx);
@@ -858,38 +789,28 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
     const int orig = __ldg(P.orig_err + idx);
     const int sumsq = s_sumsq;
     const PixelGroups pg = load_groups(s_tab);
+    ThreadSel ts;
     for (int base = 0; base < npos; base += THREADS) {
       const int pos = base + tid;
       const int row = pos / w2, col = pos - row * w2;
       const int j = by - row, i = bx + P.sa - 1 - col;
-      int e = kInvalid, refit = 0;
-      uint32_t cand = 0, eps = 0;
       if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
         const size_t nidx = (size_t)j * P.bw + i;
         const uint64_t w = __ldcg(P.done + nidx);
-        cand = w ? (uint32_t)w : __ldcg(cur + nidx);
+        const uint32_t cand = w ? (uint32_t)w : __ldcg(cur + nidx);
+        uint32_t eps = 0;
+        int refit = 0;
         const WeightSums ws = weight_sums(cand, s_wk);
-        e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+        const int e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+        ts.add(pos, row, e, cand, eps, refit);
       }
-      cta_sel_round<THREADS>(s_sel, red, row, e, pos, cand, eps, refit);
     }
-    if (tid == 0) {
-      uint16_t m;
-      uint64_t blk = stb;
-      if (s_sel.min_e <= P.thr) {
-        const int row = s_sel.sel_pos / w2, col = s_sel.sel_pos - (s_sel.sel_pos / w2) * w2;
-        m = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
-        if (s_sel.sel_refit) blk = (uint64_t)s_sel.sel_eps | ((uint64_t)s_sel.sel_cand << 32);
-      } else {
-        m = 0xFFFFu;
-      }
-      P.final_blk[idx] = blk;
-      P.motion[idx] = m;
-      const uint32_t x = (uint32_t)(blk >> 32);
+    const uint64_t w = publish_intra(P, ts, red, idx, stb, w2, tid, false);
+    if (w != 0) {  // the thread that wrote the result
+      const uint32_t x = (uint32_t)w;
       next[idx] = x;
       if (x != __ldcg(cur + idx)) atomicOr(changed_out, 1u);
     }
-    __syncthreads();
   }
 }
 
