@@ -39,7 +39,7 @@ C_CAND, C_DXT = 600, 1500
 # DRAM bytes (read + write) per launch of the search kernels on the 1080p
 # stream, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum);
 # the summaries under profiles/ give the commands.
-NCU_TRAFFIC = {"inter_dedup_kernel": 10_948_096, "intra_search_kernel": 9_857_536}
+NCU_TRAFFIC = {"inter_dedup_kernel": 10_948_352, "intra_search_kernel": 9_593_600}
 
 
 def algo_bytes(kernel: str, n: int) -> int:
