@@ -651,6 +651,74 @@ __device__ __forceinline__ int cta_select(const LaneSel &t, CtaReduce<THREADS> &
   return p == 0x7fffffff ? -1 : p;
 }
 
+// Per-block cache of evaluated index words for the intra search. Refit and
+// error depend only on the block and the word, and a block's causal window
+// holds few distinct words (about 33 of 240 positions on the 1080p stream,
+// and the word a block waits for last is almost always one of them), so each
+// thread first looks its word up: a hit skips the evaluation, which takes the
+// refit off the dataflow's critical path and most of the issue load off the
+// SMs. Entries: key = word (the block's own word marks an empty bucket, as the
+// identity candidate is never evaluated), val = eps << 32 | err_diff written
+// once, all ones while the owner is still evaluating (no valid entry has
+// eps = 0xFFFFFFFF, since its high half would be q2 < q1 <= 0xFFFF). A thread
+// that finds its word still being evaluated, or no free bucket within the
+// probe limit, evaluates it itself; results are identical either way.
+constexpr int kEvalBuckets = 512;
+constexpr int kEvalProbes = 16;
+constexpr uint64_t kEvalPending = ~0ull;
+
+struct EvalCache {
+  uint32_t key[kEvalBuckets];
+  unsigned long long val[kEvalBuckets];
+};
+
+__device__ __forceinline__ void eval_cache_reset(EvalCache &c, uint32_t own) {
+  for (int b = threadIdx.x; b < kEvalBuckets; b += blockDim.x) {
+    c.key[b] = own;
+    c.val[b] = kEvalPending;
+  }
+}
+
+__device__ __forceinline__ int cached_eval(EvalCache &c, const BlockTab &tab, const PixelGroups &pg,
+                                           const uint8_t *snap5, const uint8_t *snap6, const float4 *wk,
+                                           uint32_t cand, uint32_t own, int orig, int sumsq, uint32_t &eps,
+                                           int &refit) {
+  if (cand == own) {
+    eps = 0;
+    refit = 0;
+    return 0;
+  }
+  refit = 1;
+  uint32_t b = dedup_hash(cand) & (kEvalBuckets - 1);
+  int slot = -1;
+  for (int probe = 0; probe < kEvalProbes; ++probe) {
+    const uint32_t k = *(volatile uint32_t *)&c.key[b];
+    if (k == cand) {
+      const unsigned long long v = *(volatile unsigned long long *)&c.val[b];
+      if (v != kEvalPending) {
+        eps = (uint32_t)(v >> 32);
+        return (int)(uint32_t)v;
+      }
+      break;  // being evaluated by another thread: evaluate here too
+    }
+    if (k == own) {
+      const uint32_t old = atomicCAS(&c.key[b], own, cand);
+      if (old == own) {
+        slot = (int)b;
+        break;
+      }
+      if (old == cand) break;
+    }
+    b = (b + 1) & (kEvalBuckets - 1);
+  }
+  const WeightSums ws = weight_sums(cand, wk);
+  const int e = eval_candidate(tab, pg, snap5, snap6, cand, ws, own, orig, sumsq, eps, refit);
+  if (e == kInvalid) eps = 0;
+  if (slot >= 0)
+    *(volatile unsigned long long *)&c.val[slot] = ((unsigned long long)eps << 32) | (uint32_t)e;
+  return e;
+}
+
 // Selection and output of one block of the intra search: the CTA reduces
 // the threads' statistics, then one thread writes the final block and motion
 // code (and, when `publish`, the block's completion word). Returns the
@@ -696,6 +764,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
                                                                const uint32_t *__restrict__ run_flag = nullptr) {
   if (run_flag && __ldcg(run_flag) == 0u) return;  // the sweeps below converged
   __shared__ BlockTab s_tab;
+  __shared__ EvalCache s_cache;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
   __shared__ int s_red[2 * (THREADS / 32)];
@@ -713,13 +782,14 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
     if (k >= n_pend) break;
     const int idx = (int)__ldcg(pending + k);
     const int by = idx / P.bw, bx = idx - by * P.bw;
+    const uint64_t stb = __ldg(P.stb + idx);
+    const uint32_t own = (uint32_t)(stb >> 32);
+    eval_cache_reset(s_cache, own);
     if (tid < 32) {
       const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
       if (tid == 0) s_sumsq = sq;
     }
     __syncthreads();
-    const uint64_t stb = __ldg(P.stb + idx);
-    const uint32_t own = (uint32_t)(stb >> 32);
     const int orig = __ldg(P.orig_err + idx);
     const int sumsq = s_sumsq;
     const PixelGroups pg = load_groups(s_tab);
@@ -735,8 +805,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
           const uint32_t cand = (uint32_t)w;
           uint32_t eps = 0;
           int refit = 0;
-          const WeightSums ws = weight_sums(cand, s_wk);
-          const int e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+          const int e = cached_eval(s_cache, s_tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq, eps, refit);
           ts.add(pos, row, e, cand, eps, refit);
         }
       }
@@ -766,6 +835,7 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
                                                               uint32_t *__restrict__ changed_out) {
   if (__ldcg(changed_in) == 0u) return;
   __shared__ BlockTab s_tab;
+  __shared__ EvalCache s_cache;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
   __shared__ int s_red[2 * (THREADS / 32)];
@@ -779,13 +849,14 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
   for (int k = blockIdx.x; k < n_pend; k += gridDim.x) {
     const int idx = (int)__ldcg(pending + k);
     const int by = idx / P.bw, bx = idx - by * P.bw;
+    const uint64_t stb = __ldg(P.stb + idx);
+    const uint32_t own = (uint32_t)(stb >> 32);
+    eval_cache_reset(s_cache, own);
     if (tid < 32) {
       const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
       if (tid == 0) s_sumsq = sq;
     }
     __syncthreads();
-    const uint64_t stb = __ldg(P.stb + idx);
-    const uint32_t own = (uint32_t)(stb >> 32);
     const int orig = __ldg(P.orig_err + idx);
     const int sumsq = s_sumsq;
     const PixelGroups pg = load_groups(s_tab);
@@ -800,8 +871,7 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
         const uint32_t cand = w ? (uint32_t)w : __ldcg(cur + nidx);
         uint32_t eps = 0;
         int refit = 0;
-        const WeightSums ws = weight_sums(cand, s_wk);
-        const int e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+        const int e = cached_eval(s_cache, s_tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq, eps, refit);
         ts.add(pos, row, e, cand, eps, refit);
       }
     }
