@@ -663,7 +663,7 @@ __device__ __forceinline__ int cta_select(const LaneSel &t, CtaReduce<THREADS> &
 // eps = 0xFFFFFFFF, since its high half would be q2 < q1 <= 0xFFFF). A thread
 // that finds its word still being evaluated, or no free bucket within the
 // probe limit, evaluates it itself; results are identical either way.
-constexpr int kEvalBuckets = 512;
+constexpr int kEvalBuckets = 512;  // power of two, indexed by a 9-bit hash
 constexpr int kEvalProbes = 16;
 constexpr uint64_t kEvalPending = ~0ull;
 
@@ -689,7 +689,7 @@ __device__ __forceinline__ int cached_eval(EvalCache &c, const BlockTab &tab, co
     return 0;
   }
   refit = 1;
-  uint32_t b = dedup_hash(cand) & (kEvalBuckets - 1);
+  uint32_t b = (cand * 2654435761u) >> 23;  // 9 bits: kEvalBuckets
   int slot = -1;
   for (int probe = 0; probe < kEvalProbes; ++probe) {
     const uint32_t k = *(volatile uint32_t *)&c.key[b];
