@@ -679,10 +679,30 @@ __device__ __forceinline__ void eval_cache_reset(EvalCache &c, uint32_t own) {
   }
 }
 
-__device__ __forceinline__ int cached_eval(EvalCache &c, const BlockTab &tab, const PixelGroups &pg,
+// Whether a CTA consults its cache: on content where a window's words are
+// all different (noise) lookups never hit and only cost time, so after a block
+// in which fewer than a quarter of the threads that looked a word up found it,
+// the cache is bypassed for the next 8 blocks, then tried again. All threads
+// update it with the same block-wide counts, so it stays CTA-uniform.
+struct CacheUse {
+  bool on = true;
+  int off_left = 0;
+  __device__ __forceinline__ void update(int looked, int hits) {
+    if (on) {
+      if (looked >= 32 && 4 * hits < looked) {
+        on = false;
+        off_left = 8;
+      }
+    } else if (--off_left <= 0) {
+      on = true;
+    }
+  }
+};
+
+__device__ __forceinline__ int cached_eval(EvalCache &c, bool use, const BlockTab &tab, const PixelGroups &pg,
                                            const uint8_t *snap5, const uint8_t *snap6, const float4 *wk,
                                            uint32_t cand, uint32_t own, int orig, int sumsq, uint32_t &eps,
-                                           int &refit) {
+                                           int &refit, int &looked, int &hits) {
   if (cand == own) {
     eps = 0;
     refit = 0;
@@ -691,11 +711,13 @@ __device__ __forceinline__ int cached_eval(EvalCache &c, const BlockTab &tab, co
   refit = 1;
   uint32_t b = (cand * 2654435761u) >> 23;  // 9 bits: kEvalBuckets
   int slot = -1;
-  for (int probe = 0; probe < kEvalProbes; ++probe) {
+  for (int probe = 0; use && probe < kEvalProbes; ++probe) {
     const uint32_t k = *(volatile uint32_t *)&c.key[b];
     if (k == cand) {
       const unsigned long long v = *(volatile unsigned long long *)&c.val[b];
+      ++looked;
       if (v != kEvalPending) {
+        ++hits;
         eps = (uint32_t)(v >> 32);
         return (int)(uint32_t)v;
       }
@@ -704,10 +726,14 @@ __device__ __forceinline__ int cached_eval(EvalCache &c, const BlockTab &tab, co
     if (k == own) {
       const uint32_t old = atomicCAS(&c.key[b], own, cand);
       if (old == own) {
+        ++looked;
         slot = (int)b;
         break;
       }
-      if (old == cand) break;
+      if (old == cand) {
+        ++looked;
+        break;
+      }
     }
     b = (b + 1) & (kEvalBuckets - 1);
   }
@@ -772,6 +798,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
   build_snap_tables(s_snap5, s_snap6);
   build_weight_table(s_wk);
   CtaReduce<THREADS> red{s_red, 0};
+  CacheUse cache;
   const int tid = threadIdx.x, lane = tid & 31;
   const int n_pend = n_pending_host >= 0 ? n_pending_host : (int)__ldcg(n_pending_dev);
   const int w2 = 2 * P.sa, npos = w2 * w2;
@@ -794,6 +821,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
     const int sumsq = s_sumsq;
     const PixelGroups pg = load_groups(s_tab);
     ThreadSel ts;
+    int looked = 0, hits = 0;
     for (int base = 0; base < npos; base += THREADS) {
       const int pos = base + tid;
       const int row = pos / w2, col = pos - row * w2;
@@ -805,12 +833,14 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
           const uint32_t cand = (uint32_t)w;
           uint32_t eps = 0;
           int refit = 0;
-          const int e = cached_eval(s_cache, s_tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq, eps, refit);
+          const int e = cached_eval(s_cache, cache.on, s_tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq,
+                                    eps, refit, looked, hits);
           ts.add(pos, row, e, cand, eps, refit);
         }
       }
     }
     publish_intra(P, ts, red, idx, stb, w2, tid, true);
+    cache.update(__syncthreads_count(looked > 0), __syncthreads_count(hits > 0));
   }
 }
 
@@ -843,6 +873,7 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
   build_snap_tables(s_snap5, s_snap6);
   build_weight_table(s_wk);
   CtaReduce<THREADS> red{s_red, 0};
+  CacheUse cache;
   const int tid = threadIdx.x, lane = tid & 31;
   const int n_pend = (int)__ldcg(n_pending_dev);
   const int w2 = 2 * P.sa, npos = w2 * w2;
@@ -861,6 +892,7 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
     const int sumsq = s_sumsq;
     const PixelGroups pg = load_groups(s_tab);
     ThreadSel ts;
+    int looked = 0, hits = 0;
     for (int base = 0; base < npos; base += THREADS) {
       const int pos = base + tid;
       const int row = pos / w2, col = pos - row * w2;
@@ -871,11 +903,13 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
         const uint32_t cand = w ? (uint32_t)w : __ldcg(cur + nidx);
         uint32_t eps = 0;
         int refit = 0;
-        const int e = cached_eval(s_cache, s_tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq, eps, refit);
+        const int e = cached_eval(s_cache, cache.on, s_tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq,
+                                  eps, refit, looked, hits);
         ts.add(pos, row, e, cand, eps, refit);
       }
     }
     const uint64_t w = publish_intra(P, ts, red, idx, stb, w2, tid, false);
+    cache.update(__syncthreads_count(looked > 0), __syncthreads_count(hits > 0));
     if (w != 0) {  // the thread that wrote the result
       const uint32_t x = (uint32_t)w;
       next[idx] = x;
