@@ -680,10 +680,11 @@ __device__ __forceinline__ void eval_cache_reset(EvalCache &c, uint32_t own) {
 }
 
 // Whether a CTA consults its cache: on content where a window's words are
-// all different (noise) lookups never hit and only cost time, so after a block
-// in which fewer than a quarter of the threads that looked a word up found it,
-// the cache is bypassed for the next 8 blocks, then tried again. All threads
-// update it with the same block-wide counts, so it stays CTA-uniform.
+// all different (noise) lookups never find a repeat and only cost time, so
+// after a block in which fewer than a quarter of the threads that looked a word
+// up found it already present (evaluated or being evaluated), the cache is
+// bypassed for the next 8 blocks, then tried again. All threads update it with
+// the same block-wide counts, so it stays CTA-uniform.
 struct CacheUse {
   bool on = true;
   int off_left = 0;
@@ -716,8 +717,8 @@ __device__ __forceinline__ int cached_eval(EvalCache &c, bool use, const BlockTa
     if (k == cand) {
       const unsigned long long v = *(volatile unsigned long long *)&c.val[b];
       ++looked;
+      ++hits;  // the word is a repeat, even if its result is not written yet
       if (v != kEvalPending) {
-        ++hits;
         eps = (uint32_t)(v >> 32);
         return (int)(uint32_t)v;
       }
@@ -732,6 +733,7 @@ __device__ __forceinline__ int cached_eval(EvalCache &c, bool use, const BlockTa
       }
       if (old == cand) {
         ++looked;
+        ++hits;
         break;
       }
     }
