@@ -378,6 +378,8 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
   const uint32_t own = (uint32_t)(stb >> 32);
   const unsigned lt_mask = (1u << lane) - 1u;
   const int w2 = 2 * P.sa, npos = w2 * w2;
+  // pos / w2 as one multiply-high: exact for pos < 2^16 and w2 <= 126
+  const uint32_t w2_magic = 0xFFFFFFFFu / (uint32_t)w2 + 1u;
   const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
   LaneSel ls_;
   int ls[8];  // slot of each of the lane's positions in the current span
@@ -463,7 +465,7 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
     for (int c = 0; c < 8; ++c) {
       if ((valid >> c) & 1u) {
         const int pos = span + 32 * c + lane;
-        ls_.add(pos, pos / w2, lc[c] == own ? 0 : dd.e[ls[c]]);
+        ls_.add(pos, (int)__umulhi((uint32_t)pos, w2_magic), lc[c] == own ? 0 : dd.e[ls[c]]);
       }
     }
     __syncwarp();
