@@ -376,7 +376,6 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
                                                        const uint8_t *s_snap6, int idx, int bx, int by,
                                                        uint64_t stb, int orig, int sumsq, int lane) {
   const uint32_t own = (uint32_t)(stb >> 32);
-  const unsigned lt_mask = (1u << lane) - 1u;
   const int w2 = 2 * P.sa, npos = w2 * w2;
   // pos / w2 as one multiply-high: exact for pos < 2^16 and w2 <= 126
   const uint32_t w2_magic = 0xFFFFFFFFu / (uint32_t)w2 + 1u;
@@ -388,7 +387,6 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
     __syncwarp();
     uint32_t lc[8], ln[8];
     unsigned valid = 0;
-    int nuniq = 0;
     // all candidate loads of the span first, so their latencies overlap
     {
       const int pos0 = span + lane;
@@ -414,41 +412,65 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
         }
       }
     }
+    // Insert the lane's eight words at once: the first probes (home buckets)
+    // are issued back to back so their latencies overlap; a lane learns
+    // whether it inserted a word or found it there. Equal words of several
+    // lanes meet in the same bucket and the atomics sort out one inserter.
+    // The rare collision with another word continues probing. New words are
+    // numbered by a warp scan; the others read the number once written.
+    uint32_t bk[8];
+    unsigned newmask = 0, probemask = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      const uint32_t cand = lc[c], nidx = ln[c];
-      const bool need = cand != own;  // invalid positions hold `own` too
-      const unsigned peers = __match_any_sync(kFull, cand);
-      const int leader = __ffs(peers) - 1;
-      uint32_t b = dedup_hash(cand);
-      bool is_new = false, found = false;
-      if (need && lane == leader) {
-        for (int probe = 0; probe < kDedupBuckets; ++probe) {
-          const uint32_t old = atomicCAS(&dd.key[b], own, cand);
-          if (old == own) {
-            is_new = true;
-            break;
+      const uint32_t cand = lc[c];  // invalid positions hold `own`: no entry
+      bk[c] = dedup_hash(cand);
+      if (cand != own) {
+        const uint32_t old = atomicCAS(&dd.key[bk[c]], own, cand);
+        if (old == own)
+          newmask |= 1u << c;
+        else if (old != cand)
+          probemask |= 1u << c;
+      }
+    }
+    if (probemask) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        if ((probemask >> c) & 1u) {
+          uint32_t b = bk[c];
+          for (int probe = 1; probe < kDedupBuckets; ++probe) {
+            b = (b + 1) & (kDedupBuckets - 1);
+            const uint32_t old = atomicCAS(&dd.key[b], own, lc[c]);
+            if (old == own) {
+              newmask |= 1u << c;
+              break;
+            }
+            if (old == lc[c]) break;
           }
-          if (old == cand) {
-            found = true;
-            break;
-          }
-          b = (b + 1) & (kDedupBuckets - 1);
+          bk[c] = b;
         }
       }
-      const unsigned newm = __ballot_sync(kFull, is_new);
-      int slot = -1;
-      if (is_new) {
-        slot = nuniq + __popc(newm & lt_mask);
-        dd.slot[b] = (uint16_t)slot;
-        dd.nidx[slot] = nidx;
-      } else if (found) {
-        slot = dd.slot[b];  // inserted by an earlier chunk of this span
-      }
-      ls[c] = __shfl_sync(kFull, slot, leader);
-      nuniq += __popc(newm);
-      __syncwarp();  // this chunk's slot writes land before later chunks read them
     }
+    // exclusive warp scan of the lanes' new-word counts
+    const int mine = __popc(newmask);
+    int incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(kFull, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const int nuniq = __shfl_sync(kFull, incl, 31);
+    int next = incl - mine;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if ((newmask >> c) & 1u) {
+        dd.slot[bk[c]] = (uint16_t)next;
+        dd.nidx[next] = ln[c];
+        ++next;
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < 8; ++c) ls[c] = lc[c] != own ? (int)dd.slot[bk[c]] : 0;
     __syncwarp();
     for (int k = lane; k < nuniq; k += 32) {
       const uint32_t nidx = dd.nidx[k];
