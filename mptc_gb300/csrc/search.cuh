@@ -412,23 +412,27 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
         }
       }
     }
-    // Insert the lane's eight words at once: the first probes (home buckets)
-    // are issued back to back so their latencies overlap; a lane learns
-    // whether it inserted a word or found it there. Equal words of several
-    // lanes meet in the same bucket and the atomics sort out one inserter.
-    // The rare collision with another word continues probing. New words are
-    // numbered by a warp scan; the others read the number once written.
+    // Insert the span's distinct words. Equal words of a chunk are grouped
+    // first (__match_any_sync) and only the lowest lane of a group inserts, so
+    // the atomics meet few equal keys; the eight chunks' groupings and first
+    // probes are issued back to back so their latencies overlap. The rare
+    // collision with another word continues probing. New words are numbered
+    // by a warp scan; each lane then looks its word's number up.
     uint32_t bk[8];
-    unsigned newmask = 0, probemask = 0;
+    unsigned lead = 0, newmask = 0, probemask = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      const uint32_t cand = lc[c];  // invalid positions hold `own`: no entry
-      bk[c] = dedup_hash(cand);
-      if (cand != own) {
-        const uint32_t old = atomicCAS(&dd.key[bk[c]], own, cand);
+      const int leader = __ffs(__match_any_sync(kFull, lc[c])) - 1;
+      bk[c] = dedup_hash(lc[c]);
+      if (lc[c] != own && leader == lane) lead |= 1u << c;  // invalid positions hold `own`
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if ((lead >> c) & 1u) {
+        const uint32_t old = atomicCAS(&dd.key[bk[c]], own, lc[c]);
         if (old == own)
           newmask |= 1u << c;
-        else if (old != cand)
+        else if (old != lc[c])
           probemask |= 1u << c;
       }
     }
@@ -470,7 +474,15 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
     }
     __syncwarp();
 #pragma unroll
-    for (int c = 0; c < 8; ++c) ls[c] = lc[c] != own ? (int)dd.slot[bk[c]] : 0;
+    for (int c = 0; c < 8; ++c) {
+      int sl = 0;
+      if (lc[c] != own) {
+        uint32_t b = bk[c];  // the word's bucket for an inserting lane, its home bucket otherwise
+        for (int probe = 0; probe < kDedupBuckets && dd.key[b] != lc[c]; ++probe) b = (b + 1) & (kDedupBuckets - 1);
+        sl = dd.slot[b];
+      }
+      ls[c] = sl;
+    }
     __syncwarp();
     for (int k = lane; k < nuniq; k += 32) {
       const uint32_t nidx = dd.nidx[k];
