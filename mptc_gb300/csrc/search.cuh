@@ -376,6 +376,7 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
                                                        const uint8_t *s_snap6, int idx, int bx, int by,
                                                        uint64_t stb, int orig, int sumsq, int lane) {
   const uint32_t own = (uint32_t)(stb >> 32);
+  const unsigned lt_mask = (1u << lane) - 1u;
   const int w2 = 2 * P.sa, npos = w2 * w2;
   // pos / w2 as one multiply-high: exact for pos < 2^16 and w2 <= 126
   const uint32_t w2_magic = 0xFFFFFFFFu / (uint32_t)w2 + 1u;
@@ -387,6 +388,7 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
     __syncwarp();
     uint32_t lc[8], ln[8];
     unsigned valid = 0;
+    int nuniq = 0;
     // all candidate loads of the span first, so their latencies overlap
     {
       const int pos0 = span + lane;
@@ -412,76 +414,40 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
         }
       }
     }
-    // Insert the span's distinct words. Equal words of a chunk are grouped
-    // first (__match_any_sync) and only the lowest lane of a group inserts, so
-    // the atomics meet few equal keys; the eight chunks' groupings and first
-    // probes are issued back to back so their latencies overlap. The rare
-    // collision with another word continues probing. New words are numbered
-    // by a warp scan; each lane then looks its word's number up.
-    uint32_t bk[8];
-    unsigned lead = 0, newmask = 0, probemask = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      const int leader = __ffs(__match_any_sync(kFull, lc[c])) - 1;
-      bk[c] = dedup_hash(lc[c]);
-      if (lc[c] != own && leader == lane) lead |= 1u << c;  // invalid positions hold `own`
-    }
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      if ((lead >> c) & 1u) {
-        const uint32_t old = atomicCAS(&dd.key[bk[c]], own, lc[c]);
-        if (old == own)
-          newmask |= 1u << c;
-        else if (old != lc[c])
-          probemask |= 1u << c;
-      }
-    }
-    if (probemask) {
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        if ((probemask >> c) & 1u) {
-          uint32_t b = bk[c];
-          for (int probe = 1; probe < kDedupBuckets; ++probe) {
-            b = (b + 1) & (kDedupBuckets - 1);
-            const uint32_t old = atomicCAS(&dd.key[b], own, lc[c]);
-            if (old == own) {
-              newmask |= 1u << c;
-              break;
-            }
-            if (old == lc[c]) break;
+      const uint32_t cand = lc[c], nidx = ln[c];
+      const bool need = cand != own;  // invalid positions hold `own` too
+      const unsigned peers = __match_any_sync(kFull, cand);
+      const int leader = __ffs(peers) - 1;
+      uint32_t b = dedup_hash(cand);
+      bool is_new = false, found = false;
+      if (need && lane == leader) {
+        for (int probe = 0; probe < kDedupBuckets; ++probe) {
+          const uint32_t old = atomicCAS(&dd.key[b], own, cand);
+          if (old == own) {
+            is_new = true;
+            break;
           }
-          bk[c] = b;
+          if (old == cand) {
+            found = true;
+            break;
+          }
+          b = (b + 1) & (kDedupBuckets - 1);
         }
       }
-    }
-    // exclusive warp scan of the lanes' new-word counts
-    const int mine = __popc(newmask);
-    int incl = mine;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int v = __shfl_up_sync(kFull, incl, d);
-      if (lane >= d) incl += v;
-    }
-    const int nuniq = __shfl_sync(kFull, incl, 31);
-    int next = incl - mine;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      if ((newmask >> c) & 1u) {
-        dd.slot[bk[c]] = (uint16_t)next;
-        dd.nidx[next] = ln[c];
-        ++next;
+      const unsigned newm = __ballot_sync(kFull, is_new);
+      int slot = -1;
+      if (is_new) {
+        slot = nuniq + __popc(newm & lt_mask);
+        dd.slot[b] = (uint16_t)slot;
+        dd.nidx[slot] = nidx;
+      } else if (found) {
+        slot = dd.slot[b];  // inserted by an earlier chunk of this span
       }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      int sl = 0;
-      if (lc[c] != own) {
-        uint32_t b = bk[c];  // the word's bucket for an inserting lane, its home bucket otherwise
-        for (int probe = 0; probe < kDedupBuckets && dd.key[b] != lc[c]; ++probe) b = (b + 1) & (kDedupBuckets - 1);
-        sl = dd.slot[b];
-      }
-      ls[c] = sl;
+      ls[c] = __shfl_sync(kFull, slot, leader);
+      nuniq += __popc(newm);
+      __syncwarp();  // this chunk's slot writes land before later chunks read them
     }
     __syncwarp();
     for (int k = lane; k < nuniq; k += 32) {
