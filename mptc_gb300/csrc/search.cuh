@@ -361,6 +361,7 @@ struct DedupTab {
   uint32_t key[kDedupBuckets];  // index word, or the block's own word when empty
   uint16_t slot[kDedupBuckets];
   uint32_t nidx[kDedupSpan];    // a window block holding each distinct word
+  uint16_t bkt[kDedupSpan];     // the bucket holding each distinct word
   int e[kDedupSpan];
   uint32_t eps[kDedupSpan];
 };
@@ -442,6 +443,7 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
         slot = nuniq + __popc(newm & lt_mask);
         dd.slot[b] = (uint16_t)slot;
         dd.nidx[slot] = nidx;
+        dd.bkt[slot] = (uint16_t)b;
       } else if (found) {
         slot = dd.slot[b];  // inserted by an earlier chunk of this span
       }
@@ -451,8 +453,7 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
     }
     __syncwarp();
     for (int k = lane; k < nuniq; k += 32) {
-      const uint32_t nidx = dd.nidx[k];
-      const uint32_t cand = __ldg(prev_hi + 2 * (size_t)nidx);
+      const uint32_t nidx = dd.nidx[k], cand = dd.key[dd.bkt[k]];
       const float4 d = __ldg(P.wdesc + nidx);
       const WeightSums ws{d.x, d.y, d.z, d.w};
       uint32_t eps = 0;
@@ -476,28 +477,31 @@ __device__ __forceinline__ uint64_t inter_block_search(const SearchParams &P, co
   uint64_t word = 0;
   if (accept) {
     // the selected position's index word and refit: the owning lane looks
-    // them up (one span) or evaluates the word again (several spans)
+    // them up (one span; slot -1 marks the block's own word) or evaluates the
+    // word again (several spans)
     const int owner = sel & 31;
     uint64_t blk = 0;
     if (lane == owner) {
-      const int i = bx - P.sa + sel % w2, j = by - P.sa + sel / w2;
-      const uint32_t cand = __ldg(prev_hi + 2 * (size_t)(j * P.bw + i));
-      if (cand == own) {
-        blk = stb;
-      } else if (npos <= kDedupSpan) {
+      if (npos <= kDedupSpan) {
         const int c = sel >> 5;
-        int slot = 0;
+        int slot = -1;
 #pragma unroll
         for (int cc = 0; cc < 8; ++cc)
           if (cc == c) slot = ls[cc];
-        blk = (uint64_t)dd.eps[slot] | ((uint64_t)cand << 32);
+        blk = slot < 0 ? stb : ((uint64_t)dd.eps[slot] | ((uint64_t)dd.key[dd.bkt[slot]] << 32));
       } else {
-        const float4 d = __ldg(P.wdesc + (size_t)(j * P.bw + i));
-        const WeightSums ws{d.x, d.y, d.z, d.w};
-        uint32_t eps = 0;
-        int refit = 0;
-        eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
-        blk = (uint64_t)eps | ((uint64_t)cand << 32);
+        const int i = bx - P.sa + sel % w2, j = by - P.sa + sel / w2;
+        const uint32_t cand = __ldg(prev_hi + 2 * (size_t)(j * P.bw + i));
+        if (cand == own) {
+          blk = stb;
+        } else {
+          const float4 d = __ldg(P.wdesc + (size_t)(j * P.bw + i));
+          const WeightSums ws{d.x, d.y, d.z, d.w};
+          uint32_t eps = 0;
+          int refit = 0;
+          eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+          blk = (uint64_t)eps | ((uint64_t)cand << 32);
+        }
       }
       const int row = sel / w2, col = sel - row * w2;
       P.final_blk[idx] = blk;
