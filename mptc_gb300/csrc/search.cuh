@@ -952,7 +952,7 @@ __global__ void __launch_bounds__(256) sweep_init_kernel(const uint32_t *__restr
 // Order-preserving compaction of the pending blocks (done == 0) of the
 // wavefront order: per-tile counts, then a scan of the counts and an ordered
 // scatter, as for the unique palette below.
-constexpr int kPendTile = 4096;
+constexpr int kPendTile = 1024;
 
 __global__ void __launch_bounds__(256) pending_count_kernel(const uint32_t *__restrict__ order,
                                                             const uint64_t *__restrict__ done, int n,
@@ -1015,7 +1015,8 @@ __global__ void __launch_bounds__(256) pending_scatter_kernel(const uint32_t *__
 // The unique palette lists the stb interp of every unaccepted block in raster
 // order (codec/dxt_image.cpp:953-954). Two passes: per-tile counts, then a
 // scan of the tile counts and an ordered scatter.
-constexpr int kUniqTile = 4096;
+constexpr int kUniqTile = 1024;
+static_assert(kUniqTile == kPendTile, "the host sizes both scans' grids with one tile count");
 
 __global__ void __launch_bounds__(256) unique_count_kernel(const uint16_t *__restrict__ motion, int nblk,
                                                            uint32_t *__restrict__ tile_counts) {
