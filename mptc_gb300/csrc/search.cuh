@@ -949,6 +949,35 @@ __global__ void __launch_bounds__(256) sweep_init_kernel(const uint32_t *__restr
     for (int f = threadIdx.x; f < n_flags; f += blockDim.x) changed[f] = f == 0 ? 1u : 0u;
 }
 
+// Sum of tile_counts[0 .. ntiles) and of the counts before this CTA's tile,
+// by all 256 threads of the CTA (one count per thread per pass, then warp and
+// block sums). Ends with a barrier; s_warp (8 entries) is scratch.
+__device__ __forceinline__ void tile_prefix(const uint32_t *__restrict__ tile_counts, int ntiles, uint32_t *s_warp,
+                                            uint32_t &before, uint32_t &total) {
+  uint32_t b = 0, t = 0;
+  for (int i = threadIdx.x; i < ntiles; i += blockDim.x) {
+    const uint32_t c = __ldg(tile_counts + i);
+    t += c;
+    if (i < (int)blockIdx.x) b += c;
+  }
+  b = __reduce_add_sync(0xffffffffu, b);
+  t = __reduce_add_sync(0xffffffffu, t);
+  __shared__ uint32_t s_t[8];
+  if ((threadIdx.x & 31) == 0) {
+    s_warp[threadIdx.x >> 5] = b;
+    s_t[threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  before = 0;
+  total = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    before += s_warp[w];
+    total += s_t[w];
+  }
+  __syncthreads();  // s_warp is reused by the caller
+}
+
 // Order-preserving compaction of the pending blocks (done == 0) of the
 // wavefront order: per-tile counts, then a scan of the counts and an ordered
 // scatter, as for the unique palette below.
@@ -979,16 +1008,15 @@ __global__ void __launch_bounds__(256) pending_scatter_kernel(const uint32_t *__
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    uint32_t b = 0, total = 0;
-    for (int t = 0; t < ntiles; ++t) {
-      if (t < (int)blockIdx.x) b += tile_counts[t];
-      total += tile_counts[t];
+  {
+    uint32_t b, total;
+    tile_prefix(tile_counts, ntiles, s_warp, b, total);
+    if (threadIdx.x == 0) {
+      s_base = b;
+      if (blockIdx.x == 0) *n_pending = total;
     }
-    s_base = b;
-    if (blockIdx.x == 0) *n_pending = total;
+    __syncthreads();
   }
-  __syncthreads();
   const int t0 = blockIdx.x * kPendTile, t1 = min(n, t0 + kPendTile);
   for (int c0 = t0; c0 < t1; c0 += 256) {
     const int i = c0 + threadIdx.x;
@@ -1042,16 +1070,15 @@ __global__ void __launch_bounds__(256) unique_scatter_kernel(const uint16_t *__r
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    uint32_t b = 0, total = 0;
-    for (int t = 0; t < ntiles; ++t) {
-      if (t < (int)blockIdx.x) b += tile_counts[t];
-      total += tile_counts[t];
+  {
+    uint32_t b, total;
+    tile_prefix(tile_counts, ntiles, s_warp, b, total);
+    if (threadIdx.x == 0) {
+      s_base = b;
+      if (blockIdx.x == 0) *n_unique = total;
     }
-    s_base = b;
-    if (blockIdx.x == 0) *n_unique = total;
+    __syncthreads();
   }
-  __syncthreads();
   const int t0 = blockIdx.x * kUniqTile, t1 = min(nblk, t0 + kUniqTile);
   for (int c0 = t0; c0 < t1; c0 += 256) {
     const int i = c0 + threadIdx.x;
