@@ -614,44 +614,36 @@ __global__ void __launch_bounds__(256) wavefront_order_kernel(int bw, int bh, in
   }
 }
 
-// Closed-form selection over the CTA (see LaneSel) with one barrier: each
-// warp reduces its threads' three statistics (first e <= 0 position; largest
-// e < 0 key; the first minimum as the pair (biased err_diff, position), whose
-// lexicographic minimum is the first position of the smallest err_diff), one
-// thread per warp stores them, and after the barrier every thread combines the
-// warps' partials. Returns the selected position (-1: none valid), its m, and
-// in `pick` the statistic that holds it (0 first e <= 0, 1 last-row e < 0, 2
-// first minimum); the position's owner is thread sel % THREADS. `part` holds
-// 4 ints per warp; it is rewritten only after the caller's next barrier.
+// Block-wide reductions for the intra CTA (THREADS/32 warps). `buf` holds two
+// alternating rows of per-warp partials so one barrier per reduction suffices.
 template <int THREADS>
-__device__ __forceinline__ int cta_select(const LaneSel &t, int *part, int w2, int &m, int &pick) {
-  constexpr int NW = THREADS / 32;
-  const int le0 = __reduce_min_sync(kFull, t.le0_pos);
-  const int neg = __reduce_max_sync(kFull, t.neg_key);
-  const int hi = t.min_e == kInvalid ? 0x7fffffff : t.min_e + 0x40000000;  // err_diff is within +-2^17
-  const int whi = __reduce_min_sync(kFull, hi);
-  const int wlo = __reduce_min_sync(kFull, hi == whi ? t.min_pos : 0x7fffffff);
-  if ((threadIdx.x & 31) == 0) {
-    int *q = part + 4 * (threadIdx.x >> 5);
-    q[0] = le0;
-    q[1] = neg;
-    q[2] = whi;
-    q[3] = wlo;
-  }
-  __syncthreads();
-  int p0 = 0x7fffffff, key = -1, mh = 0x7fffffff, ml = 0x7fffffff;
+struct CtaReduce {
+  int *buf;  // [2][THREADS/32]
+  int phase;
+  __device__ __forceinline__ int min(int v) {
+    const int w = __reduce_min_sync(kFull, v);
+    int *b = buf + phase * (THREADS / 32);
+    phase ^= 1;
+    if ((threadIdx.x & 31) == 0) b[threadIdx.x >> 5] = w;
+    __syncthreads();
+    int r = b[0];
 #pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    const int *q = part + 4 * w;
-    p0 = min(p0, q[0]);
-    key = max(key, q[1]);
-    if (q[2] < mh || (q[2] == mh && q[3] < ml)) {
-      mh = q[2];
-      ml = q[3];
-    }
+    for (int k = 1; k < THREADS / 32; ++k) r = r < b[k] ? r : b[k];
+    return r;
   }
+  __device__ __forceinline__ int max(int v) { return -min(-v); }
+};
+
+// Closed-form selection over the CTA (see LaneSel): two or three block-wide
+// reductions. Returns the selected position (-1: none valid), its m, and in
+// `pick` the statistic that holds it (0 first e <= 0, 1 last-row e < 0, 2
+// first minimum); the position's owner is thread sel % THREADS.
+template <int THREADS>
+__device__ __forceinline__ int cta_select(const LaneSel &t, CtaReduce<THREADS> &red, int w2, int &m, int &pick) {
+  const int p0 = red.min(t.le0_pos);
   if (p0 != 0x7fffffff) {
     m = 0;
+    const int key = red.max(t.neg_key);
     if (key >= 0 && (key >> 16) > p0 / w2) {
       pick = 1;
       return 0xFFFF - (key & 0xFFFF);
@@ -659,13 +651,10 @@ __device__ __forceinline__ int cta_select(const LaneSel &t, int *part, int w2, i
     pick = 0;
     return p0;
   }
+  m = red.min(t.min_e);
+  const int p = red.min(t.min_e == m ? t.min_pos : 0x7fffffff);
   pick = 2;
-  if (mh == 0x7fffffff) {
-    m = kInvalid;
-    return -1;
-  }
-  m = mh - 0x40000000;
-  return ml;
+  return p == 0x7fffffff ? -1 : p;
 }
 
 // Per-block cache of evaluated index words for the intra search. Refit and
@@ -770,10 +759,10 @@ __device__ __forceinline__ int cached_eval(EvalCache &c, bool use, const BlockTa
 // block's completion word in that thread and 0 in the others. Ends with a
 // barrier.
 template <int THREADS>
-__device__ __forceinline__ uint64_t publish_intra(const SearchParams &P, const ThreadSel &ts, int *part, int idx,
-                                                  uint64_t stb, int w2, int tid, bool publish) {
+__device__ __forceinline__ uint64_t publish_intra(const SearchParams &P, const ThreadSel &ts, CtaReduce<THREADS> &red,
+                                                  int idx, uint64_t stb, int w2, int tid, bool publish) {
   int m, pick;
-  const int sel = cta_select<THREADS>(ts, part, w2, m, pick);
+  const int sel = cta_select<THREADS>(ts, red, w2, m, pick);
   const bool accept = sel >= 0 && m <= P.thr;
   uint64_t out = 0;
   if (accept ? tid == sel % THREADS : tid == 0) {
@@ -812,10 +801,11 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
   __shared__ EvalCache s_cache;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
-  __shared__ int s_part[4 * (THREADS / 32)];
+  __shared__ int s_red[2 * (THREADS / 32)];
   __shared__ int s_claim, s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
   build_weight_table(s_wk);
+  CtaReduce<THREADS> red{s_red, 0};
   CacheUse cache;
   const int tid = threadIdx.x, lane = tid & 31;
   const int n_pend = n_pending_host >= 0 ? n_pending_host : (int)__ldcg(n_pending_dev);
@@ -857,7 +847,7 @@ __global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, c
         }
       }
     }
-    publish_intra<THREADS>(P, ts, s_part, idx, stb, w2, tid, true);
+    publish_intra(P, ts, red, idx, stb, w2, tid, true);
     cache.update(__syncthreads_count(looked > 0), __syncthreads_count(hits > 0));
   }
 }
@@ -886,10 +876,11 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
   __shared__ EvalCache s_cache;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   __shared__ float4 s_wk[4];
-  __shared__ int s_part[4 * (THREADS / 32)];
+  __shared__ int s_red[2 * (THREADS / 32)];
   __shared__ int s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
   build_weight_table(s_wk);
+  CtaReduce<THREADS> red{s_red, 0};
   CacheUse cache;
   const int tid = threadIdx.x, lane = tid & 31;
   const int n_pend = (int)__ldcg(n_pending_dev);
@@ -925,7 +916,7 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
         ts.add(pos, row, e, cand, eps, refit);
       }
     }
-    const uint64_t w = publish_intra<THREADS>(P, ts, s_part, idx, stb, w2, tid, false);
+    const uint64_t w = publish_intra(P, ts, red, idx, stb, w2, tid, false);
     cache.update(__syncthreads_count(looked > 0), __syncthreads_count(hits > 0));
     if (w != 0) {  // the thread that wrote the result
       const uint32_t x = (uint32_t)w;
