@@ -174,7 +174,7 @@ mptc_status mptc_batch_fetch(mptc_batch *batch, int32_t i, uint64_t *final_host,
 mptc_status mptc_batch_encode(mptc_batch *batch, const int32_t *is_intra, void *stream);
 /* Autotuner: times the candidate launch shapes on the current inputs and the
  * given intra/inter pattern (without advancing the streams) and keeps the
- * fastest: warps per CTA of the inter search (4, 8, 16) and the CTA count of
+ * fastest: warps per CTA of the inter search (2, 4) and the CTA count of
  * each stream's intra search. Writes the chosen values (synchronises). */
 mptc_status mptc_batch_autotune(mptc_batch *batch, const int32_t *is_intra, int32_t *inter_warps,
                                 int32_t *intra_ctas, void *stream);
