@@ -19,7 +19,8 @@
 
 namespace {
 
-constexpr int kSearchWarps = 4;     // inter search: warps per CTA, one block per warp
+constexpr int kSearchWarps = 4;     // inter search: warps per CTA
+constexpr int kInterRun = 4;        // inter search at sa <= 8: blocks per warp (a run of a row)
 constexpr int kIntraThreads = 256;  // intra search: one block per CTA
 constexpr int kSweeps = 6;          // default fixed-point sweeps of an inter frame's intra pass
 constexpr int kMaxSweeps = 32;
@@ -40,7 +41,9 @@ struct mptc_ctx {
   mptc_internal::EmbedWorkspace ews;
   // device scratch
   uint64_t *done = nullptr;        // per block completion words
-  uint32_t *work = nullptr;        // [0] dataflow counter, [1] status, [2..4] stats, [5] pending, [6] fallbacks, [5] pending count
+  // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count,
+  // [6] fallbacks, [7] inter run counter, [8] overflow count
+  uint32_t *work = nullptr;
   uint32_t *order = nullptr;       // blocks in wavefront order
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
   float4 *wdesc = nullptr;         // refit weight sums of the previous frame's blocks
@@ -267,6 +270,41 @@ int launch_intra_sweeps(const mptc::SearchParams &P, const uint32_t *pending, co
   return sweeps + 2;
 }
 
+// The exhaustive inter search: one warp per run of kInterRun blocks of a row
+// at sa <= 8 (the runs share the deduplication of their windows; a persistent
+// grid of 32 warps per SM takes the runs from the zeroed counter work[7]),
+// then one CTA per block for the blocks of overflowing runs, listed in
+// ovf_list (work[8] of them); one warp per block for larger windows.
+// work: the zeroed counter words. Returns the number of kernels launched.
+int launch_inter_search(const mptc::SearchParams &P, int warps, uint32_t *work, uint32_t *ovf_list, int sm_count,
+                        cudaStream_t s) {
+  const int nblk = P.bw * P.bh;
+  if (P.sa > 8) {
+    if (warps == 2)
+      mptc::inter_dedup_kernel<2><<<(nblk + 1) / 2, 2 * 32, 0, s>>>(P);
+    else
+      mptc::inter_dedup_kernel<4><<<(nblk + 3) / 4, 4 * 32, 0, s>>>(P);
+    return 1;
+  }
+  const int nruns = (P.bw + kInterRun - 1) / kInterRun * P.bh;
+  const int ctas = std::min((nruns + warps - 1) / warps, sm_count * (32 / warps));
+  // the last rows one block at a time: about two blocks per warp
+  const int tail = std::min(P.bh, (2 * ctas * warps + P.bw - 1) / P.bw);
+  uint32_t *next = work + 7, *novf = work + 8;
+  // the default search area 8 with its window constants folded
+  if (P.sa == 8 && warps == 2)
+    mptc::inter_run_kernel<2, kInterRun, 8><<<ctas, 2 * 32, 0, s>>>(P, next, tail, novf, ovf_list);
+  else if (P.sa == 8)
+    mptc::inter_run_kernel<4, kInterRun, 8><<<ctas, 4 * 32, 0, s>>>(P, next, tail, novf, ovf_list);
+  else if (warps == 2)
+    mptc::inter_run_kernel<2, kInterRun, 0><<<ctas, 2 * 32, 0, s>>>(P, next, tail, novf, ovf_list);
+  else
+    mptc::inter_run_kernel<4, kInterRun, 0><<<ctas, 4 * 32, 0, s>>>(P, next, tail, novf, ovf_list);
+  // the overflow list is short: four CTAs per SM, idle ones return at once
+  mptc::inter_overflow_kernel<256><<<std::min(4 * sm_count, nblk), 256, 0, s>>>(P, ovf_list, novf);
+  return 2;
+}
+
 }  // namespace
 
 extern "C" {
@@ -313,13 +351,13 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
     return bad(MPTC_ECUDA);
   ctx->intra_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
   const size_t n = (size_t)ctx->nblk;
-  if (dalloc(&ctx->done, n) || dalloc(&ctx->work, 8) || dalloc(&ctx->tile_counts, (size_t)ctx->ntiles) ||
+  if (dalloc(&ctx->done, n) || dalloc(&ctx->work, 16) || dalloc(&ctx->tile_counts, (size_t)ctx->ntiles) ||
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
       dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
       dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1) || dalloc(&ctx->order, n) ||
       dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 2 * n + kMaxSweeps + 1))
     return bad(MPTC_ENOMEM);
-  if (cudaMemset(ctx->work, 0, 8 * sizeof(uint32_t)) != cudaSuccess) return bad(MPTC_ECUDA);
+  if (cudaMemset(ctx->work, 0, 16 * sizeof(uint32_t)) != cudaSuccess) return bad(MPTC_ECUDA);
   mptc::wavefront_order_kernel<<<(ctx->nblk + 255) / 256, 256>>>(ctx->bw, ctx->bh, cfg->search_area, ctx->order);
   if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return bad(MPTC_ECUDA);
   if (cudaMallocHost(reinterpret_cast<void **>(&ctx->pin_in), n * 48) != cudaSuccess ||
@@ -388,15 +426,13 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   if (prev_final_dev == final_dev) return fail(ctx, MPTC_EINVAL, "mptc_reencode: prev and final alias");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   mptc::SearchParams P = make_params(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev);
-  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, 8 * sizeof(uint32_t), s));
+  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, 16 * sizeof(uint32_t), s));
   if (prev_final_dev) {
     KernelTimer t(ctx, K_INTER, s);
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
     // weight descriptors, the search (learned: embeddings, scoring, search),
     // pending compaction, sweep init + sweeps + dataflow fallback
-    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 1) + 2;
-    const int w = ctx->inter_warps;
-    const int grid = (ctx->nblk + w - 1) / w;
+    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 0) + 2;
     if (ctx->model) {
       // learned proposal: embeddings, top-K window positions, exact test of the K
       mptc_status es = mptc_internal::model_embed_frame(ctx->model, ctx->ews, rgb_dev, ctx->width, stb_dev, ctx->nblk,
@@ -409,10 +445,9 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
       dim3 tg((ctx->bw + mptc::kTileW - 1) / mptc::kTileW, (ctx->bh + mptc::kTileH - 1) / mptc::kTileH);
       mptc::score_topk_kernel<<<tg, 128, smem, s>>>(ctx->femb, ctx->gemb, ctx->bw, ctx->bh, sa, ctx->topk_k, ctx->topk);
       mptc::learned_inter_kernel<4><<<(ctx->nblk + 3) / 4, 128, 0, s>>>(P, ctx->topk, ctx->topk_k, ctx->work + 6);
-    } else if (w == 2)
-      mptc::inter_dedup_kernel<2><<<grid, 2 * 32, 0, s>>>(P);
-    else
-      mptc::inter_dedup_kernel<4><<<(ctx->nblk + 3) / 4, 4 * 32, 0, s>>>(P);
+    } else {
+      ctx->launches += launch_inter_search(P, ctx->inter_warps, ctx->work, ctx->pending, ctx->sm_count, s);
+    }
     MPTC_CUDA(cudaGetLastError());
   } else {
     MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint64_t), s));
@@ -619,7 +654,7 @@ constexpr size_t kNaOrder = kNaOrig + kNaMaxBlocks * 4;         // u32 per block
 constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
 constexpr size_t kNaWdesc = kNaPending + kNaMaxBlocks * 4;      // float4 per block
 constexpr size_t kNaSweep = kNaWdesc + kNaMaxBlocks * 16;       // u32: 2 per block + change flags
-constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // u32[8] (after kMaxSweeps + 1 flags)
+constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // u32[16] (after kMaxSweeps + 1 flags)
 constexpr size_t kNaTileCounts = kNaWork + 256;                 // u32 per tile
 constexpr size_t kNaBytes = kNaTileCounts + ((kNaTiles * 4 + 255) / 256) * 256;
 
@@ -700,7 +735,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
 
   // The scratch keeps the previous call's contents: clear the counters, and
   // the completion flags when no inter pass will write them.
-  if (cudaMemsetAsync(work, 0, 8 * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
+  if (cudaMemsetAsync(work, 0, 16 * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
   if (!prev_final_dev && cudaMemsetAsync(done, 0, nblk * sizeof(uint64_t), s) != cudaSuccess) return MPTC_ECUDA;
   mptc::wavefront_order_kernel<<<(n + 255) / 256, 256, 0, s>>>(bw, bh, cfg->search_area, order);
   mptc::dxt1_encode_kernel<<<(n + 127) / 128, 128, 0, s>>>(rgb_dev, width, bw, n, stb, orig);
@@ -722,7 +757,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   P.thr = cfg->err_threshold;
   if (prev_final_dev) {
     mptc::weight_desc_kernel<<<(n + 255) / 256, 256, 0, s>>>(prev_final_dev, n, wdesc);
-    mptc::inter_dedup_kernel<4><<<(n + 3) / 4, 4 * 32, 0, s>>>(P);
+    launch_inter_search(P, kSearchWarps, work, pend, d->sm_count, s);
     mptc::pending_count_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles);
     mptc::pending_scatter_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles, ntiles, pend, work + 5);
     launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, sweep_count(cfg->intra_sweeps), s);

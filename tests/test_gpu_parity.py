@@ -100,6 +100,28 @@ def test_gpu_matches_oracle_params(torch_cuda, w, h, sa, thr, ii, seed):
         np.testing.assert_array_equal(o[3], r.unique, err_msg=f"frame {k} unique")
 
 
+@pytest.mark.parametrize("sa,thr", [(8, 5), (8, 400), (5, 60), (2, 5)])
+def test_gpu_matches_oracle_noisy(torch_cuda, sa, thr):
+    """Noise on the left half (every window word distinct: the inter search's
+    run table overflows and the blocks are searched one by one) beside a
+    slowly moving gradient on the right (runs share their windows)."""
+    rng = np.random.default_rng(100 + sa + thr)
+    n, h, w = 3, 64, 128
+    frames = rng.integers(0, 256, size=(n, h, w, 3), dtype=np.uint8)
+    yy, xx = np.mgrid[0:h, 0:w // 2]
+    for k in range(n):
+        g = (xx * 3 + yy * 2 + 5 * k) % 256
+        frames[k, :, w // 2:, 0] = g
+        frames[k, :, w // 2:, 1] = (g // 2 + 40) % 256
+        frames[k, :, w // 2:, 2] = 255 - g
+    outs = gpu_stream(frames, sa, thr, 16)
+    ref = oracle.encode_stream(frames, sa, thr, 16)
+    for k, (o, r) in enumerate(zip(outs, ref)):
+        np.testing.assert_array_equal(o[1], r.final, err_msg=f"frame {k} final")
+        np.testing.assert_array_equal(o[2], r.motion, err_msg=f"frame {k} motion")
+        np.testing.assert_array_equal(o[3], r.unique, err_msg=f"frame {k} unique")
+
+
 def test_gpu_intra_1080p_matches_oracle(torch_cuda):
     """A full 1080p intra frame: ~129k blocks chained through the causal window."""
     frames = StreamSpec(1920, 1080, 1, seed=77).generate()
