@@ -39,7 +39,7 @@ C_CAND, C_DXT = 600, 1500
 # DRAM bytes (read + write) per launch of the search kernels on the 1080p
 # stream, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum);
 # the summaries under profiles/ give the commands.
-NCU_TRAFFIC = {"inter_dedup_kernel": 10_948_352, "intra_search_kernel": 9_593_600}
+NCU_TRAFFIC = {"inter_search": 10_906_368 + 96_768, "intra_search_kernel": 9_363_968 + 185_856}
 
 
 def algo_bytes(kernel: str, n: int) -> int:
@@ -351,14 +351,14 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
         avg_s = tot / nl * 1e-3
         units = None
         if info is not None:
-            units = {"inter_dedup_kernel": info["inter_visited"],
+            units = {"inter_search": info["inter_visited"],
                      "intra_search_kernel": info["intra_visited"],
                      "intra_sweep_kernel/inter_frame": info["inter_frame_intra_visited"],
                      "dxt1_encode_kernel": n}.get(name)
         if units is not None:
             per = C_DXT if name == "dxt1_encode_kernel" else C_CAND
             ref_units = units
-            if name == "inter_dedup_kernel":
+            if name == "inter_search":
                 # the kernel evaluates each distinct index word of a window once
                 units = info["inter_distinct"]
             ach = units * per / avg_s / 1e9

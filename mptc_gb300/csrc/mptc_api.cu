@@ -20,7 +20,7 @@
 namespace {
 
 constexpr int kSearchWarps = 4;     // inter search: warps per CTA
-constexpr int kInterRun = 4;        // inter search at sa <= 8: blocks per warp (a run of a row)
+constexpr int kInterRun = 8;        // inter search at sa <= 8: blocks per warp (a run of a row)
 constexpr int kIntraThreads = 256;  // intra search: one block per CTA
 constexpr int kSweeps = 6;          // default fixed-point sweeps of an inter frame's intra pass
 constexpr int kMaxSweeps = 32;
@@ -174,7 +174,10 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
 }
 
 enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_STATS, K_COUNT };
-const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_dedup_kernel",
+// inter_search: the inter search kernels of an inter frame (inter_run_kernel
+// and inter_overflow_kernel at sa <= 8, inter_dedup_kernel above; the
+// learned proposal's kernels when a model is attached)
+const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_search",
                                      "intra_search_kernel",     "intra_sweep_kernel/inter_frame",
                                      "unique_kernels",          "frame_stats_kernel"};
 
@@ -428,11 +431,11 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   mptc::SearchParams P = make_params(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev);
   MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, 16 * sizeof(uint32_t), s));
   if (prev_final_dev) {
-    KernelTimer t(ctx, K_INTER, s);
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
     // weight descriptors, the search (learned: embeddings, scoring, search),
     // pending compaction, sweep init + sweeps + dataflow fallback
     ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 0) + 2;
+    KernelTimer t(ctx, K_INTER, s);
     if (ctx->model) {
       // learned proposal: embeddings, top-K window positions, exact test of the K
       mptc_status es = mptc_internal::model_embed_frame(ctx->model, ctx->ews, rgb_dev, ctx->width, stb_dev, ctx->nblk,
