@@ -5,8 +5,9 @@ search + unique palette) over the 120-frame 1920x1080 synthetic stream
 (search area 8, error threshold 5, intra interval 16: 8 intra + 112 inter
 frames). `value` times K steps with the frames already resident in HBM
 (746 MB of input, larger than the 129 MB L2, so nothing stays cached between
-steps); `e2e` times the same stream through the C ABI's host-buffer call
-(pinned host frames in, final blocks / motion codes / unique palette out).
+steps); `e2e` times the same stream through the C ABI's host-buffer stream
+call, mptc_encode_stream_host (pinned host frames in, final blocks / motion
+codes / unique palette out, the copies overlapping the encode).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
@@ -299,18 +300,19 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
         return
 
     # ---- end to end through the C ABI's host-buffer call --------------------
+    # one mptc_encode_stream_host call per step over the stream's frames in
+    # pinned host memory: uploads and downloads overlap the encode
     pin_frames = torch.from_numpy(frames_np).pin_memory()
     fb = pin_frames.numpy()
-    out_final = torch.empty(n, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
-    out_mot = torch.empty(2 * n, dtype=torch.uint8).pin_memory().numpy()
-    out_uni = torch.empty(n, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
-    from mptc_gb300.encoder import FrameOutput
-    out = FrameOutput(out_final, out_mot, out_uni)
+    from mptc_gb300.encoder import StreamOutput
+    out = StreamOutput(torch.empty((nf, n), dtype=torch.int64).pin_memory().numpy().view(np.uint64),
+                       torch.empty((nf, 2 * n), dtype=torch.uint8).pin_memory().numpy(),
+                       torch.empty((nf, n), dtype=torch.int32).pin_memory().numpy().view(np.uint32),
+                       torch.empty(nf, dtype=torch.int32).pin_memory().numpy().view(np.uint32))
     e2e_enc = Encoder(W, H, SA, THR, II)
 
     def host_step():
-        for f in range(nf):
-            e2e_enc.encode_frame_host(fb[f], is_intra=sched[f], out=out)
+        e2e_enc.encode_stream_host(fb, is_intra=sched, out=out)
 
     host_step()  # warm-up
     if dist is not None:
@@ -322,7 +324,7 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e_value = whole_job_rate(nf * e2e_steps, world, e2e_s)
     h2d = nf * W * H * 3
-    d2h = nf * (n * 8 + n * 2 + n * 4 + 12)
+    d2h = nf * (n * 8 + n * 2 + n * 4 + 4) + 4  # per frame: final, motion, palette, count; the run's status
     e2e_enc.close()
 
     # ---- roofline of the dominant kernel -------------------------------------

@@ -109,6 +109,21 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
                                    uint64_t *stb_host, uint64_t *final_host, uint8_t *motion_host,
                                    uint32_t *unique_host, uint32_t *n_unique_host, void *stream);
 
+/* A run of n_frames frames from HOST buffers, the host encoder loop of
+ * codec/codec.cpp:1383-1394 in one call: the same results as n_frames
+ * successive mptc_encode_frame_host calls (the stream continues across
+ * calls). frames_host holds the frames back to back (width*height*3 bytes
+ * each), is_intra[k] flags frame k; frame k's outputs go to
+ * final_host + k*nblk, motion_host + k*2*nblk, unique_host + k*nblk (its
+ * n_unique_host[k] first entries; the copy covers all nblk) with
+ * nblk = (width/4)*(height/4). With every buffer pinned, the copies run on
+ * two streams of the context: frame k+1's upload and frame k-1's download
+ * overlap frame k's encode; pageable buffers go frame by frame through the
+ * pinned staging. Returns once every output is in host memory. */
+mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, int32_t n_frames,
+                                    const int32_t *is_intra, uint64_t *final_host, uint8_t *motion_host,
+                                    uint32_t *unique_host, uint32_t *n_unique_host, void *stream);
+
 /* Largest frame, in 4x4 blocks, that mptc_encode_frame_noalloc accepts
  * (131072 blocks: 1920x1080 is 129600, 2048x1024 is 131072). */
 #define MPTC_NOALLOC_MAX_BLOCKS 131072

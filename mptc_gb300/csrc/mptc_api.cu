@@ -61,6 +61,18 @@ struct mptc_ctx {
   uint8_t *pin_out = nullptr;
   int cur = 0;                 // which final_dev holds the latest frame
   bool have_prev = false;
+  // pipelined host runs (mptc_encode_stream_host), allocated on first use:
+  // slot 0 is the host path's buffers above, slot 1 a second set
+  struct Pipe {
+    bool ready = false;
+    uint8_t *rgb[2] = {nullptr, nullptr};
+    uint8_t *motion[2] = {nullptr, nullptr};
+    uint32_t *unique[2] = {nullptr, nullptr};
+    uint32_t *n_unique[2] = {nullptr, nullptr};
+    uint32_t *status = nullptr;  // OR of the run's frame status words
+    cudaStream_t cin = nullptr, cout = nullptr;
+    cudaEvent_t start = nullptr, in_ready[2] = {}, comp_done[2] = {}, out_done[2] = {};
+  } pipe;
   uint32_t last_is_intra = 0;
   std::string err;
   // opt-in per-kernel event timing
@@ -393,6 +405,19 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   mptc_internal::embed_workspace_free(ctx->ews);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
+  {
+    mptc_ctx::Pipe &p = ctx->pipe;
+    cudaFree(p.rgb[1]);
+    cudaFree(p.motion[1]);
+    cudaFree(p.unique[1]);
+    cudaFree(p.n_unique[1]);
+    cudaFree(p.status);
+    if (p.cin) cudaStreamDestroy(p.cin);
+    if (p.cout) cudaStreamDestroy(p.cout);
+    for (cudaEvent_t e : {p.start, p.in_ready[0], p.in_ready[1], p.comp_done[0], p.comp_done[1], p.out_done[0],
+                          p.out_done[1]})
+      if (e) cudaEventDestroy(e);
+  }
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
   delete ctx;
   return MPTC_OK;
@@ -560,6 +585,113 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
   *n_unique_host = nu;
   ctx->cur = nxt;
   ctx->have_prev = true;
+  return MPTC_OK;
+}
+
+namespace {
+
+__global__ void status_or_kernel(const uint32_t *__restrict__ work, uint32_t *__restrict__ acc) {
+  if (threadIdx.x == 0) *acc |= work[1];
+}
+
+mptc_status pipe_init(mptc_ctx *ctx) {
+  mptc_ctx::Pipe &p = ctx->pipe;
+  if (p.ready) return MPTC_OK;
+  const size_t n = (size_t)ctx->nblk;
+  p.rgb[0] = ctx->rgb_dev;
+  p.motion[0] = ctx->motion_dev;
+  p.unique[0] = ctx->unique_dev;
+  p.n_unique[0] = ctx->n_unique_dev;
+  cudaError_t e = cudaMalloc(&p.rgb[1], n * 48);
+  if (e == cudaSuccess) e = cudaMalloc(&p.motion[1], n * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&p.unique[1], n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&p.n_unique[1], 4);
+  if (e == cudaSuccess) e = cudaMalloc(&p.status, 4);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p.cin, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p.cout, cudaStreamNonBlocking);
+  for (cudaEvent_t *ev : {&p.start, &p.in_ready[0], &p.in_ready[1], &p.comp_done[0], &p.comp_done[1],
+                          &p.out_done[0], &p.out_done[1]})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return fail(ctx, e == cudaErrorMemoryAllocation ? MPTC_ENOMEM : MPTC_ECUDA,
+                                    std::string("encode_stream_host: ") + cudaGetErrorString(e));
+  p.ready = true;
+  return MPTC_OK;
+}
+
+}  // namespace
+
+mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, int32_t n_frames,
+                                    const int32_t *is_intra, uint64_t *final_host, uint8_t *motion_host,
+                                    uint32_t *unique_host, uint32_t *n_unique_host, void *stream) {
+  if (!ctx) return MPTC_EINVAL;
+  if (n_frames < 0 || (n_frames > 0 && (!frames_host || !is_intra || !final_host || !motion_host || !unique_host ||
+                                        !n_unique_host)))
+    return fail(ctx, MPTC_EINVAL, "mptc_encode_stream_host: null pointer or negative frame count");
+  if (n_frames == 0) return MPTC_OK;
+  if (!is_intra[0] && !ctx->have_prev)
+    return fail(ctx, MPTC_ESTATE, "mptc_encode_stream_host: inter frame without a previous frame");
+  const size_t n = (size_t)ctx->nblk, in_bytes = n * 48;
+  if (!is_pinned(frames_host) || !is_pinned(final_host) || !is_pinned(motion_host) || !is_pinned(unique_host) ||
+      !is_pinned(n_unique_host)) {
+    // pageable buffers: frame by frame through the host path's pinned staging
+    for (int32_t k = 0; k < n_frames; ++k) {
+      const mptc_status st =
+          mptc_encode_frame_host(ctx, frames_host + k * in_bytes, is_intra[k], nullptr, final_host + k * n,
+                                 motion_host + k * 2 * n, unique_host + k * n, n_unique_host + k, stream);
+      if (st != MPTC_OK) return st;
+    }
+    return MPTC_OK;
+  }
+  mptc_status st = pipe_init(ctx);
+  if (st != MPTC_OK) return st;
+  mptc_ctx::Pipe &p = ctx->pipe;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the copy streams start after the work already queued on `stream`
+  MPTC_CUDA(cudaMemsetAsync(p.status, 0, 4, s));
+  MPTC_CUDA(cudaEventRecord(p.start, s));
+  MPTC_CUDA(cudaStreamWaitEvent(p.cin, p.start, 0));
+  MPTC_CUDA(cudaStreamWaitEvent(p.cout, p.start, 0));
+  // frame k uses buffer slot k & 1; its upload waits until frame k-2 has
+  // been encoded (the slot's input is free), its encode until frame k-2's
+  // outputs are downloaded (the slot's outputs and final blocks are free)
+  auto upload = [&](int32_t k) -> cudaError_t {
+    const int slot = k & 1;
+    cudaError_t e = k >= 2 ? cudaStreamWaitEvent(p.cin, p.comp_done[slot], 0) : cudaSuccess;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(p.rgb[slot], frames_host + k * in_bytes, in_bytes, cudaMemcpyHostToDevice, p.cin);
+    if (e == cudaSuccess) e = cudaEventRecord(p.in_ready[slot], p.cin);
+    return e;
+  };
+  MPTC_CUDA(upload(0));
+  if (n_frames > 1) MPTC_CUDA(upload(1));
+  for (int32_t k = 0; k < n_frames; ++k) {
+    const int slot = k & 1;
+    MPTC_CUDA(cudaStreamWaitEvent(s, p.in_ready[slot], 0));
+    if (k >= 2) MPTC_CUDA(cudaStreamWaitEvent(s, p.out_done[slot], 0));
+    const int nxt = ctx->have_prev ? 1 - ctx->cur : ctx->cur;
+    const uint64_t *prev = is_intra[k] ? nullptr : ctx->final_dev[ctx->cur];
+    st = mptc_encode_frame(ctx, p.rgb[slot], prev, ctx->stb, ctx->final_dev[nxt], p.motion[slot], p.unique[slot],
+                           p.n_unique[slot], stream);
+    if (st != MPTC_OK) return st;
+    status_or_kernel<<<1, 32, 0, s>>>(ctx->work, p.status);
+    ++ctx->launches;
+    MPTC_CUDA(cudaEventRecord(p.comp_done[slot], s));
+    ctx->cur = nxt;
+    ctx->have_prev = true;
+    MPTC_CUDA(cudaStreamWaitEvent(p.cout, p.comp_done[slot], 0));
+    MPTC_CUDA(cudaMemcpyAsync(final_host + k * n, ctx->final_dev[nxt], n * 8, cudaMemcpyDeviceToHost, p.cout));
+    MPTC_CUDA(cudaMemcpyAsync(motion_host + k * 2 * n, p.motion[slot], n * 2, cudaMemcpyDeviceToHost, p.cout));
+    MPTC_CUDA(cudaMemcpyAsync(unique_host + k * n, p.unique[slot], n * 4, cudaMemcpyDeviceToHost, p.cout));
+    MPTC_CUDA(cudaMemcpyAsync(n_unique_host + k, p.n_unique[slot], 4, cudaMemcpyDeviceToHost, p.cout));
+    MPTC_CUDA(cudaEventRecord(p.out_done[slot], p.cout));
+    if (k + 2 < n_frames) MPTC_CUDA(upload(k + 2));
+  }
+  // `stream` completes after the last download; the run's status word
+  MPTC_CUDA(cudaStreamWaitEvent(s, p.out_done[(n_frames - 1) & 1], 0));
+  uint32_t *h = reinterpret_cast<uint32_t *>(ctx->pin_out);
+  MPTC_CUDA(cudaMemcpyAsync(h, p.status, 4, cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaStreamSynchronize(s));
+  if (*h & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
   return MPTC_OK;
 }
 

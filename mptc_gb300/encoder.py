@@ -23,6 +23,18 @@ class FrameOutput:
     stb: np.ndarray | None = None
 
 
+@dataclass
+class StreamOutput:
+    """Outputs of a run of frames (encode_stream_host), one row per frame."""
+    final: np.ndarray     # (frames, nblk) u64
+    motion: np.ndarray    # (frames, 2 * nblk) u8
+    unique: np.ndarray    # (frames, nblk) u32: frame k's palette is unique[k, :n_unique[k]]
+    n_unique: np.ndarray  # (frames,) u32
+
+    def frame(self, k: int) -> FrameOutput:
+        return FrameOutput(self.final[k], self.motion[k], self.unique[k, : int(self.n_unique[k])])
+
+
 class Encoder:
     """One MPTC stream of fixed resolution (width, height multiples of 4)."""
 
@@ -106,20 +118,49 @@ class Encoder:
         return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(n.value)}
 
     # -- host API -----------------------------------------------------------
+    def _intra_flag(self, is_intra: bool | None) -> bool:
+        """The caller's flag, or the next one of the reference's schedule."""
+        if is_intra is not None:
+            return bool(is_intra)
+        flag = self._next_intra
+        if self._intra_num <= self.intra_interval:
+            self._next_intra = False
+            if self._intra_num == self.intra_interval:
+                self._next_intra = True
+                self._intra_num = 1
+            else:
+                self._intra_num += 1
+        return flag
+
+    def encode_stream_host(self, frames: np.ndarray, is_intra=None,
+                           out: StreamOutput | None = None) -> StreamOutput:
+        """A run of frames (frames, height, width, 3) from host memory in one
+        call (mptc_encode_stream_host); the stream continues across calls.
+        is_intra: a flag per frame, or None for the reference's schedule.
+        With pinned frames and outputs the uploads and downloads overlap the
+        encode; otherwise the frames go one by one."""
+        f = np.ascontiguousarray(frames, dtype=np.uint8)
+        assert f.ndim == 4 and f.shape[1:] == (self.height, self.width, 3)
+        n = f.shape[0]
+        flags = np.array([self._intra_flag(None if is_intra is None else is_intra[k]) for k in range(n)],
+                         dtype=np.int32)
+        if out is None:
+            out = StreamOutput(np.empty((n, self.nblk), np.uint64), np.empty((n, 2 * self.nblk), np.uint8),
+                               np.empty((n, self.nblk), np.uint32), np.empty(n, np.uint32))
+        assert out.final.shape[0] >= n and out.final.flags.c_contiguous and out.motion.flags.c_contiguous
+        assert out.unique.flags.c_contiguous and out.n_unique.flags.c_contiguous
+        check(lib().mptc_encode_stream_host(self._ctx, f.ctypes.data, n, flags.ctypes.data,
+                                            out.final.ctypes.data, out.motion.ctypes.data,
+                                            out.unique.ctypes.data, out.n_unique.ctypes.data, None),
+              self._ctx)
+        return out
+
     def encode_frame_host(self, frame: np.ndarray, is_intra: bool | None = None,
                           want_stb: bool = False, out: FrameOutput | None = None) -> FrameOutput:
         """One frame from host memory; successive calls form a stream. With
         is_intra=None the reference's intra-interval schedule is applied
         (frame 1 intra, then every intra_interval-th, codec/codec.cpp:1462-1469)."""
-        if is_intra is None:
-            is_intra = self._next_intra
-            if self._intra_num <= self.intra_interval:
-                self._next_intra = False
-                if self._intra_num == self.intra_interval:
-                    self._next_intra = True
-                    self._intra_num = 1
-                else:
-                    self._intra_num += 1
+        is_intra = self._intra_flag(is_intra)
         f = np.ascontiguousarray(frame, dtype=np.uint8)
         assert f.shape == (self.height, self.width, 3)
         if out is None:

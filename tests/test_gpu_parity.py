@@ -160,6 +160,38 @@ def test_gpu_device_api_matches_host_api(torch_cuda):
     enc.close()
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_gpu_stream_host_matches_frame_host(torch_cuda, pinned):
+    """mptc_encode_stream_host (pipelined copies with pinned buffers, frame by
+    frame with pageable ones) gives the per-frame host call's results, and the
+    stream continues across calls."""
+    torch = torch_cuda
+    from mptc_gb300.encoder import Encoder, StreamOutput
+    frames = StreamSpec(256, 128, 7, seed=21, n_squares=3, square_size=40, speed_min=2,
+                        speed_max=5).generate()
+    ref = gpu_stream(frames, 8, 5, 3)
+    enc = Encoder(256, 128, 8, 5, 3)
+    n = enc.nblk
+
+    def buf(shape, dtype):
+        t = torch.zeros(shape, dtype=dtype)
+        return (t.pin_memory() if pinned else t).numpy()
+
+    src = buf(frames.shape, torch.uint8)
+    src[:] = frames
+    out = StreamOutput(buf((7, n), torch.int64).view(np.uint64), buf((7, 2 * n), torch.uint8),
+                       buf((7, n), torch.int32).view(np.uint32), buf((7,), torch.int32).view(np.uint32))
+    for a, b in ((0, 4), (4, 7)):
+        enc.encode_stream_host(src[a:b], out=StreamOutput(out.final[a:b], out.motion[a:b], out.unique[a:b],
+                                                          out.n_unique[a:b]))
+    for k in range(7):
+        o = out.frame(k)
+        np.testing.assert_array_equal(o.final, ref[k][1], err_msg=f"frame {k} final")
+        np.testing.assert_array_equal(o.motion, ref[k][2], err_msg=f"frame {k} motion")
+        np.testing.assert_array_equal(o.unique, ref[k][3], err_msg=f"frame {k} unique")
+    enc.close()
+
+
 def test_gpu_rejects_bad_arguments(torch_cuda):
     from mptc_gb300._lib import MptcError
     from mptc_gb300.encoder import Encoder
