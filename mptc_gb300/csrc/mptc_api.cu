@@ -24,6 +24,9 @@ constexpr int kInterRun = 8;        // inter search at sa <= 8: blocks per warp 
 constexpr int kIntraThreads = 256;  // intra search: one block per CTA
 constexpr int kSweeps = 6;          // default fixed-point sweeps of an inter frame's intra pass
 constexpr int kMaxSweeps = 32;
+constexpr int kWorkWords = 16;      // counters and flags at the start of the per-frame work area
+// The per-frame work area: kWorkWords words, then two u64 tile states per scan tile.
+size_t work_bytes(int ntiles) { return (kWorkWords + 4 * (size_t)ntiles) * sizeof(uint32_t); }
 
 }  // namespace
 
@@ -42,13 +45,15 @@ struct mptc_ctx {
   // device scratch
   uint64_t *done = nullptr;        // per block completion words
   // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count,
-  // [6] fallbacks, [7] inter run counter, [8] overflow count
+  // [6] fallbacks, [7] inter run counter, [8] overflow count, [10] pending
+  // scan tile counter, [11] unique scan tile counter; then the two scans'
+  // tile states (tile_state), all zeroed per frame (kWorkWords + 4 * ntiles)
   uint32_t *work = nullptr;
+  uint64_t *tile_state = nullptr;  // [0, ntiles) pending scan, [ntiles, 2 ntiles) unique scan
   uint32_t *order = nullptr;       // blocks in wavefront order
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
   float4 *wdesc = nullptr;         // refit weight sums of the previous frame's blocks
   uint32_t *sweep = nullptr;       // intra sweeps: 2 estimate buffers of n words + kMaxSweeps + 1 change flags
-  uint32_t *tile_counts = nullptr; // per unique tile
   uint64_t *stb = nullptr;         // stb blocks (encode_frame / host path)
   int32_t *orig_err = nullptr;
   // host-path buffers
@@ -185,13 +190,13 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
   return P;
 }
 
-enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_STATS, K_COUNT };
+enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_COUNT };
 // inter_search: the inter search kernels of an inter frame (inter_run_kernel
 // and inter_overflow_kernel at sa <= 8, inter_dedup_kernel above; the
 // learned proposal's kernels when a model is attached)
 const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_search",
                                      "intra_search_kernel",     "intra_sweep_kernel/inter_frame",
-                                     "unique_kernels",          "frame_stats_kernel"};
+                                     "unique_scan_kernel"};
 
 cudaEvent_t pool_event(mptc_ctx *ctx) {
   if (ctx->ev_used == ctx->ev_pool.size()) {
@@ -238,23 +243,6 @@ __global__ void alu_probe_kernel(int iters, int32_t *sink) {
   if (t == 12345.678f) *sink = (int32_t)t;  // never true; keeps the chains live
 }
 
-__global__ void frame_stats_kernel(const uint16_t *__restrict__ motion, int nblk, uint32_t *__restrict__ stats) {
-  int ni = 0, na = 0, nu = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
-    const uint16_t m = motion[i];
-    nu += m == 0xFFFFu;
-    ni += m != 0xFFFFu && (m & 0x80u);
-    na += m != 0xFFFFu && !(m & 0x80u);
-  }
-  ni = __reduce_add_sync(0xffffffffu, ni);
-  na = __reduce_add_sync(0xffffffffu, na);
-  nu = __reduce_add_sync(0xffffffffu, nu);
-  if ((threadIdx.x & 31) == 0) {
-    if (ni) atomicAdd(stats + 0, (uint32_t)ni);
-    if (na) atomicAdd(stats + 1, (uint32_t)na);
-    if (nu) atomicAdd(stats + 2, (uint32_t)nu);
-  }
-}
 
 }  // namespace
 
@@ -262,12 +250,12 @@ namespace {
 
 // The intra pass of an inter frame: fixed-point sweeps over the open blocks,
 // then the exact dataflow kernel only if the sweeps did not converge.
-// sweep: 2 * n estimate words followed by kSweeps + 1 change flags.
 // Sweeps to run for a configuration's intra_sweeps value.
 int sweep_count(int32_t cfg) { return cfg == 0 ? kSweeps : (cfg < 0 ? 0 : std::min(cfg, kMaxSweeps)); }
 
-// sweep: 2 * n estimate words followed by kMaxSweeps + 1 change flags.
-// Returns the number of kernels launched.
+// sweep: 2 * n estimate words followed by kMaxSweeps + 1 change flags; the
+// pending scan has set the first estimates and flags. Returns the number of
+// kernels launched.
 int launch_intra_sweeps(const mptc::SearchParams &P, const uint32_t *pending, const uint32_t *n_pending,
                         uint32_t *sweep, int n, int grid, int sweeps, cudaStream_t s) {
   if (sweeps == 0) {
@@ -275,14 +263,13 @@ int launch_intra_sweeps(const mptc::SearchParams &P, const uint32_t *pending, co
     return 1;
   }
   uint32_t *est[2] = {sweep, sweep + n}, *changed = sweep + 2 * (size_t)n;
-  mptc::sweep_init_kernel<<<64, 256, 0, s>>>(pending, n_pending, P.stb, est[0], changed, sweeps + 1);
   for (int k = 0; k < sweeps; ++k)
     mptc::intra_sweep_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, est[k & 1],
                                                                            est[(k + 1) & 1], changed + k,
                                                                            changed + k + 1);
   mptc::intra_search_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, -1,
                                                                           changed + sweeps);
-  return sweeps + 2;
+  return sweeps + 1;
 }
 
 // The exhaustive inter search: one warp per run of kInterRun blocks of a row
@@ -351,7 +338,7 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
   ctx->bw = width / 4;
   ctx->bh = height / 4;
   ctx->nblk = ctx->bw * ctx->bh;
-  ctx->ntiles = (ctx->nblk + mptc::kUniqTile - 1) / mptc::kUniqTile;
+  ctx->ntiles = (ctx->nblk + mptc::kScanTile - 1) / mptc::kScanTile;
   auto bad = [&](mptc_status st) {
     mptc_ctx_destroy(ctx);
     return st;
@@ -366,13 +353,14 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
     return bad(MPTC_ECUDA);
   ctx->intra_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
   const size_t n = (size_t)ctx->nblk;
-  if (dalloc(&ctx->done, n) || dalloc(&ctx->work, 16) || dalloc(&ctx->tile_counts, (size_t)ctx->ntiles) ||
+  if (dalloc(&ctx->done, n) || dalloc(&ctx->work, kWorkWords + 4 * (size_t)ctx->ntiles) ||
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
       dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
       dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1) || dalloc(&ctx->order, n) ||
       dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 2 * n + kMaxSweeps + 1))
     return bad(MPTC_ENOMEM);
-  if (cudaMemset(ctx->work, 0, 16 * sizeof(uint32_t)) != cudaSuccess) return bad(MPTC_ECUDA);
+  ctx->tile_state = reinterpret_cast<uint64_t *>(ctx->work + kWorkWords);
+  if (cudaMemset(ctx->work, 0, work_bytes(ctx->ntiles)) != cudaSuccess) return bad(MPTC_ECUDA);
   mptc::wavefront_order_kernel<<<(ctx->nblk + 255) / 256, 256>>>(ctx->bw, ctx->bh, cfg->search_area, ctx->order);
   if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return bad(MPTC_ECUDA);
   if (cudaMallocHost(reinterpret_cast<void **>(&ctx->pin_in), n * 48) != cudaSuccess ||
@@ -386,7 +374,6 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   if (!ctx) return MPTC_EINVAL;
   cudaFree(ctx->done);
   cudaFree(ctx->work);
-  cudaFree(ctx->tile_counts);
   cudaFree(ctx->stb);
   cudaFree(ctx->orig_err);
   cudaFree(ctx->rgb_dev);
@@ -454,12 +441,12 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   if (prev_final_dev == final_dev) return fail(ctx, MPTC_EINVAL, "mptc_reencode: prev and final alias");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   mptc::SearchParams P = make_params(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev);
-  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, 16 * sizeof(uint32_t), s));
+  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, work_bytes(ctx->ntiles), s));
   if (prev_final_dev) {
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
     // weight descriptors, the search (learned: embeddings, scoring, search),
     // pending compaction, sweep init + sweeps + dataflow fallback
-    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 0) + 2;
+    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 0) + 1;
     KernelTimer t(ctx, K_INTER, s);
     if (ctx->model) {
       // learned proposal: embeddings, top-K window positions, exact test of the K
@@ -481,10 +468,12 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint64_t), s));
   }
   if (prev_final_dev) {
-    // pending = blocks the inter pass left open, in wavefront order
-    mptc::pending_count_kernel<<<ctx->ntiles, 256, 0, s>>>(ctx->order, ctx->done, ctx->nblk, ctx->tile_counts);
-    mptc::pending_scatter_kernel<<<ctx->ntiles, 256, 0, s>>>(ctx->order, ctx->done, ctx->nblk, ctx->tile_counts,
-                                                            ctx->ntiles, ctx->pending, ctx->work + 5);
+    // pending = blocks the inter pass left open, in wavefront order, with
+    // the sweeps' first estimates and change flags
+    const int sw = sweep_count(ctx->cfg.intra_sweeps);
+    mptc::pending_scan_kernel<<<ctx->ntiles, 256, 0, s>>>(
+        ctx->order, ctx->done, stb_dev, ctx->nblk, ctx->ntiles, ctx->tile_state, ctx->work + 10, ctx->pending,
+        ctx->work + 5, ctx->sweep, ctx->sweep + 2 * (size_t)ctx->nblk, sw ? sw + 1 : 0, ctx->work + 1);
   }
   {
     KernelTimer t(ctx, prev_final_dev ? K_PENDING : K_INTRA, s);
@@ -500,14 +489,10 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
   {
     KernelTimer t(ctx, K_UNIQUE, s);
-    mptc::unique_count_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, ctx->nblk, ctx->tile_counts);
-    mptc::unique_scatter_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, stb_dev, ctx->nblk, ctx->tile_counts,
-                                                           ctx->ntiles, unique_dev, n_unique_dev);
-  }
-  {
-    KernelTimer t(ctx, K_STATS, s);
-    frame_stats_kernel<<<ctx->sm_count, 256, 0, s>>>(m16, ctx->nblk, ctx->work + 2);
-    ctx->launches += 3;  // unique count + scatter, frame stats
+    mptc::unique_scan_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, stb_dev, ctx->nblk, ctx->ntiles,
+                                                        ctx->tile_state + ctx->ntiles, ctx->work + 11, unique_dev,
+                                                        n_unique_dev, ctx->work + 2, ctx->work + 1);
+    ++ctx->launches;
   }
   MPTC_CUDA(cudaGetLastError());
   ctx->last_is_intra = prev_final_dev ? 0u : 1u;
@@ -780,7 +765,7 @@ mptc_status mptc_alu_probe(int32_t blocks, int32_t iters, int32_t *sink_dev, dou
 namespace {
 
 constexpr size_t kNaMaxBlocks = MPTC_NOALLOC_MAX_BLOCKS;
-constexpr size_t kNaTiles = (kNaMaxBlocks + mptc::kUniqTile - 1) / mptc::kUniqTile;
+constexpr size_t kNaTiles = (kNaMaxBlocks + mptc::kScanTile - 1) / mptc::kScanTile;
 // byte offsets inside the scratch array (each 256-byte aligned)
 constexpr size_t kNaDone = 0;                                   // u64 per block
 constexpr size_t kNaStb = kNaDone + kNaMaxBlocks * 8;           // u64 per block
@@ -789,9 +774,8 @@ constexpr size_t kNaOrder = kNaOrig + kNaMaxBlocks * 4;         // u32 per block
 constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
 constexpr size_t kNaWdesc = kNaPending + kNaMaxBlocks * 4;      // float4 per block
 constexpr size_t kNaSweep = kNaWdesc + kNaMaxBlocks * 16;       // u32: 2 per block + change flags
-constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // u32[16] (after kMaxSweeps + 1 flags)
-constexpr size_t kNaTileCounts = kNaWork + 256;                 // u32 per tile
-constexpr size_t kNaBytes = kNaTileCounts + ((kNaTiles * 4 + 255) / 256) * 256;
+constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // work area (after kMaxSweeps + 1 flags)
+constexpr size_t kNaBytes = kNaWork + ((kWorkWords * 4 + kNaTiles * 16 + 255) / 256) * 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
@@ -860,17 +844,17 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   uint64_t *stb = stb_dev ? stb_dev : reinterpret_cast<uint64_t *>(d->scratch + kNaStb);
   int32_t *orig = reinterpret_cast<int32_t *>(d->scratch + kNaOrig);
   uint32_t *work = reinterpret_cast<uint32_t *>(d->scratch + kNaWork);
-  uint32_t *tiles = reinterpret_cast<uint32_t *>(d->scratch + kNaTileCounts);
+  uint64_t *tile_state = reinterpret_cast<uint64_t *>(work + kWorkWords);
   uint32_t *order = reinterpret_cast<uint32_t *>(d->scratch + kNaOrder);
   uint32_t *pend = reinterpret_cast<uint32_t *>(d->scratch + kNaPending);
   float4 *wdesc = reinterpret_cast<float4 *>(d->scratch + kNaWdesc);
   uint32_t *sweep = reinterpret_cast<uint32_t *>(d->scratch + kNaSweep);
   const int bw = width / 4, bh = height / 4, n = (int)nblk;
-  const int ntiles = (n + mptc::kUniqTile - 1) / mptc::kUniqTile;
+  const int ntiles = (n + mptc::kScanTile - 1) / mptc::kScanTile;
 
-  // The scratch keeps the previous call's contents: clear the counters, and
-  // the completion flags when no inter pass will write them.
-  if (cudaMemsetAsync(work, 0, 16 * sizeof(uint32_t), s) != cudaSuccess) return MPTC_ECUDA;
+  // The scratch keeps the previous call's contents: clear the counters and
+  // tile states, and the completion flags when no inter pass will write them.
+  if (cudaMemsetAsync(work, 0, work_bytes(ntiles), s) != cudaSuccess) return MPTC_ECUDA;
   if (!prev_final_dev && cudaMemsetAsync(done, 0, nblk * sizeof(uint64_t), s) != cudaSuccess) return MPTC_ECUDA;
   mptc::wavefront_order_kernel<<<(n + 255) / 256, 256, 0, s>>>(bw, bh, cfg->search_area, order);
   mptc::dxt1_encode_kernel<<<(n + 127) / 128, 128, 0, s>>>(rgb_dev, width, bw, n, stb, orig);
@@ -893,15 +877,17 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   if (prev_final_dev) {
     mptc::weight_desc_kernel<<<(n + 255) / 256, 256, 0, s>>>(prev_final_dev, n, wdesc);
     launch_inter_search(P, kSearchWarps, work, pend, d->sm_count, s);
-    mptc::pending_count_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles);
-    mptc::pending_scatter_kernel<<<ntiles, 256, 0, s>>>(order, done, n, tiles, ntiles, pend, work + 5);
-    launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, sweep_count(cfg->intra_sweeps), s);
+    const int sw = sweep_count(cfg->intra_sweeps);
+    mptc::pending_scan_kernel<<<ntiles, 256, 0, s>>>(order, done, stb, n, ntiles, tile_state, work + 10, pend,
+                                                    work + 5, sweep, sweep + 2 * (size_t)n, sw ? sw + 1 : 0,
+                                                    work + 1);
+    launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, sw, s);
   } else {
     mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, order, nullptr, n);
   }
   const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
-  mptc::unique_count_kernel<<<ntiles, 256, 0, s>>>(m16, n, tiles);
-  mptc::unique_scatter_kernel<<<ntiles, 256, 0, s>>>(m16, stb, n, tiles, ntiles, unique_dev, n_unique_dev);
+  mptc::unique_scan_kernel<<<ntiles, 256, 0, s>>>(m16, stb, n, ntiles, tile_state + ntiles, work + 11, unique_dev,
+                                                  n_unique_dev, work + 2, work + 1);
   noalloc_status_kernel<<<1, 32, 0, s>>>(work, n_unique_dev);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }

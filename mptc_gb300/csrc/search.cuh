@@ -1254,169 +1254,169 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
   }
 }
 
-// Start of the sweeps: open blocks' estimates = their stb words; changed[0] = 1.
-__global__ void __launch_bounds__(256) sweep_init_kernel(const uint32_t *__restrict__ pending,
-                                                         const uint32_t *__restrict__ n_pending_dev,
-                                                         const uint64_t *__restrict__ stb, uint32_t *__restrict__ cur,
-                                                         uint32_t *__restrict__ changed, int n_flags) {
-  const int n_pend = (int)__ldcg(n_pending_dev);
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_pend; k += gridDim.x * blockDim.x) {
-    const uint32_t idx = pending[k];
-    cur[idx] = (uint32_t)(stb[idx] >> 32);
+// ------------------------------------------------------ ordered compaction --
+// Single-pass ordered compactions (decoupled look-back, Merrill & Garland,
+// "Single-pass Parallel Prefix Scan with Decoupled Look-back", 2016): a CTA
+// per tile of kScanTile blocks takes tiles in order from a zeroed counter,
+// counts its tile, publishes the count, adds up its predecessors' published
+// counts (or the first inclusive prefix among them) and scatters its items
+// at the resulting offset. Tile states are 64-bit words, zeroed per frame:
+// 0 = not yet published, kTileAgg | v = the tile's count v, kTilePre | v =
+// the count of the tile and all tiles before it. A tile reads only tiles
+// taken before it by running CTAs, so the look-back always ends; each wait
+// is bounded like wait_done.
+constexpr int kScanTile = 1024;  // blocks per tile: 256 threads x 4
+constexpr uint64_t kTileAgg = 1ull << 62, kTilePre = 2ull << 62;
+
+// Warp 0 of the CTA owning `tile`: publishes `count` and returns (in every
+// lane) the sum of the counts of the tiles before it.
+__device__ __forceinline__ uint32_t lookback(uint64_t *state, int tile, uint32_t count, uint32_t *status) {
+  const int lane = threadIdx.x & 31;
+  if (tile == 0) {
+    if (lane == 0) st_relaxed(state, kTilePre | count);
+    return 0;
   }
-  if (blockIdx.x == 0)
-    for (int f = threadIdx.x; f < n_flags; f += blockDim.x) changed[f] = f == 0 ? 1u : 0u;
+  if (lane == 0) st_relaxed(state + tile, kTileAgg | count);
+  uint32_t before = 0;
+  for (int j = tile - 1;; j -= 32) {
+    const int k = j - lane;  // lane l reads the l-th nearest unread predecessor
+    uint64_t v = k >= 0 ? ld_relaxed(state + k) : kTilePre;
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 0; __any_sync(kFull, v == 0); ++it) {
+      if (v == 0) v = ld_relaxed(state + k);
+      if ((it & 63u) == 63u && (ld_acquire(status) & kDevTimeout || global_ns() - t0 > 1000000000ull)) {
+        atomicOr(status, kDevTimeout);
+        v = v ? v : kTilePre;  // give up: the result is flagged invalid
+      }
+    }
+    const unsigned pre = __ballot_sync(kFull, (v >> 62) == 2);
+    const int stop = pre ? __ffs(pre) - 1 : 31;  // the nearest inclusive prefix ends the look-back
+    before += __reduce_add_sync(kFull, lane <= stop ? (uint32_t)v : 0u);
+    if (pre) break;
+  }
+  if (lane == 0) st_relaxed(state + tile, kTilePre | (before + count));
+  return before;
 }
 
-// Sum of tile_counts[0 .. ntiles) and of the counts before this CTA's tile,
-// by all 256 threads of the CTA (one count per thread per pass, then warp and
-// block sums). Ends with a barrier; s_warp (8 entries) is scratch.
-__device__ __forceinline__ void tile_prefix(const uint32_t *__restrict__ tile_counts, int ntiles, uint32_t *s_warp,
-                                            uint32_t &before, uint32_t &total) {
-  uint32_t b = 0, t = 0;
-  for (int i = threadIdx.x; i < ntiles; i += blockDim.x) {
-    const uint32_t c = __ldg(tile_counts + i);
-    t += c;
-    if (i < (int)blockIdx.x) b += c;
+// CTA-wide exclusive scan of one count per thread (256 threads); returns the
+// thread's offset and the CTA total in `total`. Ends with a barrier.
+__device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t c, uint32_t *s_warp, uint32_t &total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t v = __shfl_up_sync(kFull, inc, d);
+    if (lane >= d) inc += v;
   }
-  b = __reduce_add_sync(0xffffffffu, b);
-  t = __reduce_add_sync(0xffffffffu, t);
-  __shared__ uint32_t s_t[8];
-  if ((threadIdx.x & 31) == 0) {
-    s_warp[threadIdx.x >> 5] = b;
-    s_t[threadIdx.x >> 5] = t;
-  }
+  if (lane == 31) s_warp[warp] = inc;
   __syncthreads();
-  before = 0;
+  uint32_t before = 0;
   total = 0;
 #pragma unroll
   for (int w = 0; w < 8; ++w) {
-    before += s_warp[w];
-    total += s_t[w];
+    const uint32_t t = s_warp[w];
+    before += w < warp ? t : 0u;
+    total += t;
   }
   __syncthreads();  // s_warp is reused by the caller
+  return before + inc - c;
 }
 
-// Order-preserving compaction of the pending blocks (done == 0) of the
-// wavefront order: per-tile counts, then a scan of the counts and an ordered
-// scatter, as for the unique palette below.
-constexpr int kPendTile = 1024;
-
-__global__ void __launch_bounds__(256) pending_count_kernel(const uint32_t *__restrict__ order,
-                                                            const uint64_t *__restrict__ done, int n,
-                                                            uint32_t *__restrict__ tile_counts) {
-  const int t0 = blockIdx.x * kPendTile;
-  int c = 0;
-  for (int i = t0 + threadIdx.x; i < min(n, t0 + kPendTile); i += blockDim.x) c += __ldg(done + order[i]) == 0ull;
-  c = __reduce_add_sync(kFull, c);
-  __shared__ int s[8];
-  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+// Inter frames: the blocks the inter pass left open (done == 0) in wavefront
+// order, into pending[0 .. *n_pending); for the fixed-point sweeps each open
+// block's first estimate is its stb word (cur[idx]) and the first n_flags
+// change flags read (1, 0, 0, ...).
+__global__ void __launch_bounds__(256) pending_scan_kernel(const uint32_t *__restrict__ order,
+                                                           const uint64_t *__restrict__ done,
+                                                           const uint64_t *__restrict__ stb, int n, int ntiles,
+                                                           uint64_t *state, uint32_t *claim,
+                                                           uint32_t *__restrict__ pending,
+                                                           uint32_t *__restrict__ n_pending,
+                                                           uint32_t *__restrict__ cur, uint32_t *__restrict__ changed,
+                                                           int n_flags, uint32_t *status) {
+  __shared__ int s_tile;
+  __shared__ uint32_t s_warp[8], s_before;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(claim, 1u);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int t = 0;
-    for (int w = 0; w < 8; ++w) t += s[w];
-    tile_counts[blockIdx.x] = (uint32_t)t;
+  const int tile = s_tile, i0 = tile * kScanTile + 4 * threadIdx.x;
+  uint32_t blk[4];
+  unsigned open = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = i0 + q;
+    blk[q] = i < n ? __ldg(order + i) : 0u;
+    if (i < n && __ldcg(done + blk[q]) == 0ull) open |= 1u << q;
   }
-}
-
-__global__ void __launch_bounds__(256) pending_scatter_kernel(const uint32_t *__restrict__ order,
-                                                              const uint64_t *__restrict__ done, int n,
-                                                              const uint32_t *__restrict__ tile_counts, int ntiles,
-                                                              uint32_t *__restrict__ pending,
-                                                              uint32_t *__restrict__ n_pending) {
-  __shared__ uint32_t s_base;
-  __shared__ uint32_t s_warp[8];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  {
-    uint32_t b, total;
-    tile_prefix(tile_counts, ntiles, s_warp, b, total);
-    if (threadIdx.x == 0) {
-      s_base = b;
-      if (blockIdx.x == 0) *n_pending = total;
+  uint32_t total;
+  uint32_t off = cta_exclusive_scan(__popc(open), s_warp, total);
+  if (threadIdx.x < 32) {
+    const uint32_t b = lookback(state, tile, total, status);
+    if (threadIdx.x == 0) s_before = b;
+  }
+  __syncthreads();
+  off += s_before;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if ((open >> q) & 1u) {
+      pending[off++] = blk[q];
+      cur[blk[q]] = (uint32_t)(__ldg(stb + blk[q]) >> 32);
     }
-    __syncthreads();
-  }
-  const int t0 = blockIdx.x * kPendTile, t1 = min(n, t0 + kPendTile);
-  for (int c0 = t0; c0 < t1; c0 += 256) {
-    const int i = c0 + threadIdx.x;
-    const uint32_t blk = i < t1 ? order[i] : 0u;
-    const bool u = i < t1 && __ldg(done + blk) == 0ull;
-    const unsigned bal = __ballot_sync(kFull, u);
-    if (lane == 0) s_warp[warp] = __popc(bal);
-    __syncthreads();
-    uint32_t off = s_base;
-    for (int w = 0; w < warp; ++w) off += s_warp[w];
-    off += __popc(bal & ((1u << lane) - 1u));
-    if (u) pending[off] = blk;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t t = 0;
-      for (int w = 0; w < 8; ++w) t += s_warp[w];
-      s_base += t;
-    }
-    __syncthreads();
-  }
+  if (tile == ntiles - 1 && threadIdx.x == 0) *n_pending = s_before + total;
+  if (tile == 0)
+    for (int f = threadIdx.x; f < n_flags; f += blockDim.x) changed[f] = f == 0 ? 1u : 0u;
 }
 
 // ----------------------------------------------------------------- unique --
 // The unique palette lists the stb interp of every unaccepted block in raster
-// order (codec/dxt_image.cpp:953-954). Two passes: per-tile counts, then a
-// scan of the tile counts and an ordered scatter.
-constexpr int kUniqTile = 1024;
-static_assert(kUniqTile == kPendTile, "the host sizes both scans' grids with one tile count");
-
-__global__ void __launch_bounds__(256) unique_count_kernel(const uint16_t *__restrict__ motion, int nblk,
-                                                           uint32_t *__restrict__ tile_counts) {
-  const int t0 = blockIdx.x * kUniqTile;
-  int c = 0;
-  for (int i = t0 + threadIdx.x; i < min(nblk, t0 + kUniqTile); i += blockDim.x) c += motion[i] == 0xFFFFu;
-  c = __reduce_add_sync(kFull, c);
-  __shared__ int s[8];
-  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+// order (codec/dxt_image.cpp:953-954), compacted in one pass; the same pass
+// counts the frame's inter, intra and unique blocks into stats[0..2].
+__global__ void __launch_bounds__(256) unique_scan_kernel(const uint16_t *__restrict__ motion,
+                                                          const uint64_t *__restrict__ stb, int nblk, int ntiles,
+                                                          uint64_t *state, uint32_t *claim,
+                                                          uint32_t *__restrict__ unique,
+                                                          uint32_t *__restrict__ n_unique,
+                                                          uint32_t *__restrict__ stats, uint32_t *status) {
+  __shared__ int s_tile;
+  __shared__ uint32_t s_warp[8], s_before;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(claim, 1u);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int t = 0;
-    for (int w = 0; w < 8; ++w) t += s[w];
-    tile_counts[blockIdx.x] = (uint32_t)t;
-  }
-}
-
-__global__ void __launch_bounds__(256) unique_scatter_kernel(const uint16_t *__restrict__ motion,
-                                                             const uint64_t *__restrict__ stb, int nblk,
-                                                             const uint32_t *__restrict__ tile_counts,
-                                                             int ntiles, uint32_t *__restrict__ unique,
-                                                             uint32_t *__restrict__ n_unique) {
-  __shared__ uint32_t s_base;
-  __shared__ uint32_t s_warp[8];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  {
-    uint32_t b, total;
-    tile_prefix(tile_counts, ntiles, s_warp, b, total);
-    if (threadIdx.x == 0) {
-      s_base = b;
-      if (blockIdx.x == 0) *n_unique = total;
+  const int tile = s_tile, i0 = tile * kScanTile + 4 * threadIdx.x;
+  unsigned uq = 0;
+  int ni = 0, na = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = i0 + q;
+    if (i < nblk) {
+      const uint16_t m = motion[i];
+      if (m == 0xFFFFu)
+        uq |= 1u << q;
+      else if (m & 0x80u)
+        ++ni;
+      else
+        ++na;
     }
-    __syncthreads();
   }
-  const int t0 = blockIdx.x * kUniqTile, t1 = min(nblk, t0 + kUniqTile);
-  for (int c0 = t0; c0 < t1; c0 += 256) {
-    const int i = c0 + threadIdx.x;
-    const bool u = i < t1 && motion[i] == 0xFFFFu;
-    const unsigned bal = __ballot_sync(kFull, u);
-    if (lane == 0) s_warp[warp] = __popc(bal);
-    __syncthreads();
-    uint32_t off = s_base;
-    for (int w = 0; w < warp; ++w) off += s_warp[w];
-    off += __popc(bal & ((1u << lane) - 1u));
-    if (u) unique[off] = (uint32_t)(stb[i] >> 32);
-    __syncthreads();
+  uint32_t total;
+  uint32_t off = cta_exclusive_scan(__popc(uq), s_warp, total);
+  ni = __reduce_add_sync(kFull, ni);
+  na = __reduce_add_sync(kFull, na);
+  if ((threadIdx.x & 31) == 0) {
+    if (ni) atomicAdd(stats + 0, (uint32_t)ni);
+    if (na) atomicAdd(stats + 1, (uint32_t)na);
+  }
+  if (threadIdx.x < 32) {
+    const uint32_t b = lookback(state, tile, total, status);
     if (threadIdx.x == 0) {
-      uint32_t t = 0;
-      for (int w = 0; w < 8; ++w) t += s_warp[w];
-      s_base += t;
+      s_before = b;
+      if (total) atomicAdd(stats + 2, total);
     }
-    __syncthreads();
   }
+  __syncthreads();
+  off += s_before;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if ((uq >> q) & 1u) unique[off++] = (uint32_t)(__ldg(stb + i0 + q) >> 32);
+  if (tile == ntiles - 1 && threadIdx.x == 0) *n_unique = s_before + total;
 }
 
 }  // namespace mptc
