@@ -5,7 +5,9 @@ search + unique palette) over the 120-frame 1920x1080 synthetic stream
 (search area 8, error threshold 5, intra interval 16: 8 intra + 112 inter
 frames). `value` times K steps with the frames already resident in HBM
 (746 MB of input, larger than the 129 MB L2, so nothing stays cached between
-steps); `e2e` times the same stream through the C ABI's host-buffer stream
+steps), one mptc_encode_stream_device call per step (outputs in HBM; intra
+frames on the call's second lane, concurrent with the inter frames before
+them); `e2e` times the same stream through the C ABI's host-buffer stream
 call, mptc_encode_stream_host (pinned host frames in, final blocks / motion
 codes / unique palette out, the copies overlapping the encode).
 
@@ -254,18 +256,18 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
     frames_dev = torch.from_numpy(frames_np).to(dev)
     enc = Encoder(W, H, SA, THR, II)
     n = enc.nblk
-    fin = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(2)]
-    stb = torch.empty(n, dtype=torch.int64, device=dev)
-    mot = torch.empty(2 * n, dtype=torch.uint8, device=dev)
-    uni = torch.empty(n, dtype=torch.int32, device=dev)
-    nu = torch.zeros(1, dtype=torch.int32, device=dev)
     sched = intra_schedule(nf, II)
     stream = torch.cuda.current_stream()
 
+    # a step is one mptc_encode_stream_device call over the stream's frames:
+    # outputs stay in HBM, intra frames run on the call's second lane
+    fin_all = torch.empty((nf, n), dtype=torch.int64, device=dev)
+    mot_all = torch.empty((nf, 2 * n), dtype=torch.uint8, device=dev)
+    uni_all = torch.empty((nf, n), dtype=torch.int32, device=dev)
+    nu_all = torch.empty(nf, dtype=torch.int32, device=dev)
+
     def step():
-        for f in range(nf):
-            prev = None if sched[f] else fin[(f - 1) % 2]
-            enc.encode_frame_device(frames_dev[f], prev, stb, fin[f % 2], mot, uni, nu, stream)
+        enc.encode_stream_device(frames_dev, fin_all, mot_all, uni_all, nu_all, is_intra=sched, stream=stream)
 
     for _ in range(args.warmup):
         step()
@@ -328,7 +330,12 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
     e2e_enc.close()
 
     # ---- roofline of the dominant kernel -------------------------------------
-    dom = max(ktimes.items(), key=lambda kv: kv[1][1])
+    # The step time is set by the first lane (stb encode, inter search, intra
+    # pass, palette of every inter frame): the intra frames run concurrently
+    # on the second lane. The dominant kernel is the first lane's largest; its
+    # event times include the contention with the overlapping intra frames.
+    dom = ("inter_search", ktimes["inter_search"]) if "inter_search" in ktimes else \
+        max(ktimes.items(), key=lambda kv: kv[1][1])
     line = dict(metric=METRIC, value=round(value, 3), unit="frames/s", n_gpus=world, steps=args.steps,
                 warmup=args.warmup, ms_per_step=round(elapsed_ms / args.steps, 3), higher_is_better=True,
                 scaling="weak", vs_baseline=None, dtype="fp32+int32", data="synthetic",
@@ -373,7 +380,9 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
                                     hbm=dict(achieved_gbs=round(algo_bytes(name, n) / avg_s / 1e9, 2),
                                              peak_gbs=6782.1, bytes_per_launch=algo_bytes(name, n)),
                                     peak_note="measured fp32 add probe (libmptc_gb300 mptc_alu_probe), "
-                                              "152 SMs x 128 lanes at the clock seen")
+                                              "152 SMs x 128 lanes at the clock seen",
+                                    timing_note="CUDA-event launch times inside the timed step, where the "
+                                                "intra frames of the second lane overlap the inter frames")
         print(json.dumps(line), flush=True)
     enc.close()
 

@@ -116,13 +116,28 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
  * each), is_intra[k] flags frame k; frame k's outputs go to
  * final_host + k*nblk, motion_host + k*2*nblk, unique_host + k*nblk (its
  * n_unique_host[k] first entries; the copy covers all nblk) with
- * nblk = (width/4)*(height/4). With every buffer pinned, the copies run on
- * two streams of the context: frame k+1's upload and frame k-1's download
- * overlap frame k's encode; pageable buffers go frame by frame through the
- * pinned staging. Returns once every output is in host memory. */
+ * nblk = (width/4)*(height/4). With every buffer pinned, the frames pass
+ * through a ring of device frame slots of the context, uploads and downloads
+ * on two copy streams overlap the encodes, and intra frames after the first
+ * are encoded on a second lane concurrently with the inter frames before
+ * them (see mptc_encode_stream_device); pageable buffers go frame by frame
+ * through the pinned staging. Returns once every output is in host memory. */
 mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, int32_t n_frames,
                                     const int32_t *is_intra, uint64_t *final_host, uint8_t *motion_host,
                                     uint32_t *unique_host, uint32_t *n_unique_host, void *stream);
+
+/* The same run on DEVICE buffers: frames_dev holds the frames back to back,
+ * frame k's outputs go to final_dev + k*nblk, motion_dev + k*2*nblk,
+ * unique_dev + k*nblk and n_unique_dev[k]. Intra frames depend on no earlier
+ * frame, so the call encodes them on a second context of its own and a second
+ * CUDA stream, concurrently with the inter frames before them; each inter
+ * frame that follows an intra frame waits for it. The results are those of
+ * n_frames successive mptc_encode_frame calls; the run's last final blocks
+ * become the context's previous frame (a later call or mptc_encode_frame_host
+ * continues the stream). Returns after `stream` has completed the run. */
+mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, int32_t n_frames,
+                                      const int32_t *is_intra, uint64_t *final_dev, uint8_t *motion_dev,
+                                      uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream);
 
 /* Largest frame, in 4x4 blocks, that mptc_encode_frame_noalloc accepts
  * (131072 blocks: 1920x1080 is 129600, 2048x1024 is 131072). */

@@ -17,7 +17,8 @@ STATUS_NAMES = {0: "MPTC_OK", 1: "MPTC_EINVAL", 2: "MPTC_ENOMEM", 3: "MPTC_ETIME
 # Every symbol include/mptc_gb300.h declares.
 EXPORTED = [
     "mptc_ctx_create", "mptc_ctx_destroy", "mptc_dxt1_encode", "mptc_reencode",
-    "mptc_encode_frame", "mptc_encode_frame_host", "mptc_encode_stream_host", "mptc_last_frame_stats",
+    "mptc_encode_frame", "mptc_encode_frame_host", "mptc_encode_stream_host", "mptc_encode_stream_device",
+    "mptc_last_frame_stats",
     "mptc_last_error",
     "mptc_version", "mptc_built_arch", "mptc_set_kernel_timing", "mptc_kernel_times",
     "mptc_alu_probe", "mptc_encode_frame_noalloc", "mptc_batch_create", "mptc_batch_destroy",
@@ -73,6 +74,7 @@ def lib() -> ctypes.CDLL:
         L.mptc_encode_frame.argtypes = [vp, vp, vp, vp, vp, vp, vp, u32p, vp]
         L.mptc_encode_frame_host.argtypes = [vp, vp, i32, vp, vp, vp, vp, u32p, vp]
         L.mptc_encode_stream_host.argtypes = [vp, vp, i32, vp, vp, vp, vp, vp, vp]
+        L.mptc_encode_stream_device.argtypes = [vp, vp, i32, vp, vp, vp, vp, vp, vp]
         L.mptc_last_frame_stats.argtypes = [vp, ctypes.POINTER(FrameStats), vp]
         L.mptc_last_error.argtypes = [vp]
         L.mptc_last_error.restype = ctypes.c_char_p

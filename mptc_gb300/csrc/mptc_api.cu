@@ -25,6 +25,8 @@ constexpr int kIntraThreads = 256;  // intra search: one block per CTA
 constexpr int kSweeps = 6;          // default fixed-point sweeps of an inter frame's intra pass
 constexpr int kMaxSweeps = 32;
 constexpr int kWorkWords = 16;      // counters and flags at the start of the per-frame work area
+constexpr int kRing = 24;           // host stream calls: device frame slots
+constexpr int kLaneIntraShare = 5;  // stream calls: intra lane CTAs = kLaneIntraShare/8 of the SM count
 // The per-frame work area: kWorkWords words, then two u64 tile states per scan tile.
 size_t work_bytes(int ntiles) { return (kWorkWords + 4 * (size_t)ntiles) * sizeof(uint32_t); }
 
@@ -66,18 +68,27 @@ struct mptc_ctx {
   uint8_t *pin_out = nullptr;
   int cur = 0;                 // which final_dev holds the latest frame
   bool have_prev = false;
-  // pipelined host runs (mptc_encode_stream_host), allocated on first use:
-  // slot 0 is the host path's buffers above, slot 1 a second set
-  struct Pipe {
+  // host runs (mptc_encode_stream_host), allocated on first use: a ring of
+  // kRing device frame slots (input, final blocks, motion, palette, count),
+  // frame k in slot k % kRing, with an upload and a download stream
+  struct Ring {
     bool ready = false;
-    uint8_t *rgb[2] = {nullptr, nullptr};
-    uint8_t *motion[2] = {nullptr, nullptr};
-    uint32_t *unique[2] = {nullptr, nullptr};
-    uint32_t *n_unique[2] = {nullptr, nullptr};
-    uint32_t *status = nullptr;  // OR of the run's frame status words
+    unsigned char *mem = nullptr;
+    uint8_t *rgb[kRing] = {};
+    uint64_t *fin[kRing] = {};
+    uint8_t *motion[kRing] = {};
+    uint32_t *unique[kRing] = {};
+    uint32_t *n_unique[kRing] = {};
     cudaStream_t cin = nullptr, cout = nullptr;
-    cudaEvent_t start = nullptr, in_ready[2] = {}, comp_done[2] = {}, out_done[2] = {};
-  } pipe;
+    cudaEvent_t up[kRing] = {}, enc[kRing] = {}, down[kRing] = {};
+  } ring;
+  // second lane of the stream calls, allocated on first use: intra frames
+  // depend on no earlier frame, so a run encodes them on their own context
+  // and CUDA stream, concurrently with the inter frames before them
+  mptc_ctx *lane_b = nullptr;
+  cudaStream_t lane_s = nullptr;
+  cudaEvent_t lane_start = nullptr, lane_done = nullptr;
+  uint32_t *run_status = nullptr;  // OR of a run's frame status words (device)
   uint32_t last_is_intra = 0;
   std::string err;
   // opt-in per-kernel event timing
@@ -316,8 +327,9 @@ int32_t mptc_built_arch(void) { return 1030; }
 
 mptc_status mptc_kernel_launches(mptc_ctx *ctx, uint64_t *count) {
   if (!ctx || !count) return MPTC_EINVAL;
-  *count = ctx->launches;
+  *count = ctx->launches + (ctx->lane_b ? ctx->lane_b->launches : 0);
   ctx->launches = 0;
+  if (ctx->lane_b) ctx->lane_b->launches = 0;
   return MPTC_OK;
 }
 
@@ -392,18 +404,19 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   mptc_internal::embed_workspace_free(ctx->ews);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
+  if (ctx->lane_b) mptc_ctx_destroy(ctx->lane_b);
+  if (ctx->lane_s) cudaStreamDestroy(ctx->lane_s);
+  if (ctx->lane_start) cudaEventDestroy(ctx->lane_start);
+  if (ctx->lane_done) cudaEventDestroy(ctx->lane_done);
+  cudaFree(ctx->run_status);
   {
-    mptc_ctx::Pipe &p = ctx->pipe;
-    cudaFree(p.rgb[1]);
-    cudaFree(p.motion[1]);
-    cudaFree(p.unique[1]);
-    cudaFree(p.n_unique[1]);
-    cudaFree(p.status);
-    if (p.cin) cudaStreamDestroy(p.cin);
-    if (p.cout) cudaStreamDestroy(p.cout);
-    for (cudaEvent_t e : {p.start, p.in_ready[0], p.in_ready[1], p.comp_done[0], p.comp_done[1], p.out_done[0],
-                          p.out_done[1]})
-      if (e) cudaEventDestroy(e);
+    mptc_ctx::Ring &r = ctx->ring;
+    cudaFree(r.mem);
+    if (r.cin) cudaStreamDestroy(r.cin);
+    if (r.cout) cudaStreamDestroy(r.cout);
+    for (int i = 0; i < kRing; ++i)
+      for (cudaEvent_t e : {r.up[i], r.enc[i], r.down[i]})
+        if (e) cudaEventDestroy(e);
   }
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
   delete ctx;
@@ -576,30 +589,64 @@ mptc_status mptc_encode_frame_host(mptc_ctx *ctx, const uint8_t *rgb_host, int32
 namespace {
 
 __global__ void status_or_kernel(const uint32_t *__restrict__ work, uint32_t *__restrict__ acc) {
-  if (threadIdx.x == 0) *acc |= work[1];
+  if (threadIdx.x == 0 && work[1]) atomicOr(acc, work[1]);  // two lanes may report at once
 }
 
-mptc_status pipe_init(mptc_ctx *ctx) {
-  mptc_ctx::Pipe &p = ctx->pipe;
-  if (p.ready) return MPTC_OK;
+// The second lane (context, stream, events) and the run status word.
+mptc_status lane_init(mptc_ctx *ctx) {
+  if (!ctx->run_status && cudaMalloc(&ctx->run_status, sizeof(uint32_t)) != cudaSuccess)
+    return fail(ctx, MPTC_ENOMEM, "stream call: status word");
+  if (ctx->lane_b) return MPTC_OK;
+  mptc_ctx *b = nullptr;
+  const mptc_status st = mptc_ctx_create(&ctx->cfg, ctx->width, ctx->height, &b);
+  if (st != MPTC_OK) return fail(ctx, st, "stream call: second lane context");
+  // the intra lane's stream has the highest priority: its latency-bound
+  // dataflow gets SM slots ahead of the inter kernels it overlaps
+  int prio_low = 0, prio_high = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->lane_s, cudaStreamNonBlocking, prio_high);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_start, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    mptc_ctx_destroy(b);
+    return fail(ctx, MPTC_ECUDA, std::string("stream call: ") + cudaGetErrorString(e));
+  }
+  b->timing = ctx->timing;
+  // five eighths of the SMs: the overlapped inter frames keep the rest
+  b->intra_cap = std::max(1, ctx->sm_count * kLaneIntraShare / 8);
+  ctx->lane_b = b;
+  return MPTC_OK;
+}
+
+mptc_status ring_init(mptc_ctx *ctx) {
+  mptc_ctx::Ring &r = ctx->ring;
+  if (r.ready) return MPTC_OK;
   const size_t n = (size_t)ctx->nblk;
-  p.rgb[0] = ctx->rgb_dev;
-  p.motion[0] = ctx->motion_dev;
-  p.unique[0] = ctx->unique_dev;
-  p.n_unique[0] = ctx->n_unique_dev;
-  cudaError_t e = cudaMalloc(&p.rgb[1], n * 48);
-  if (e == cudaSuccess) e = cudaMalloc(&p.motion[1], n * 2);
-  if (e == cudaSuccess) e = cudaMalloc(&p.unique[1], n * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&p.n_unique[1], 4);
-  if (e == cudaSuccess) e = cudaMalloc(&p.status, 4);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p.cin, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p.cout, cudaStreamNonBlocking);
-  for (cudaEvent_t *ev : {&p.start, &p.in_ready[0], &p.in_ready[1], &p.comp_done[0], &p.comp_done[1],
-                          &p.out_done[0], &p.out_done[1]})
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  auto up256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t per = up256(n * 48) + up256(n * 8) + up256(n * 2) + up256(n * 4) + 256;
+  cudaError_t e = cudaMalloc(&r.mem, per * kRing);
+  if (e == cudaSuccess) {
+    for (int i = 0; i < kRing; ++i) {
+      unsigned char *q = r.mem + per * i;
+      r.rgb[i] = q;
+      q += up256(n * 48);
+      r.fin[i] = reinterpret_cast<uint64_t *>(q);
+      q += up256(n * 8);
+      r.motion[i] = q;
+      q += up256(n * 2);
+      r.unique[i] = reinterpret_cast<uint32_t *>(q);
+      q += up256(n * 4);
+      r.n_unique[i] = reinterpret_cast<uint32_t *>(q);
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r.cin, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r.cout, cudaStreamNonBlocking);
+  for (int i = 0; i < kRing && e == cudaSuccess; ++i)
+    for (cudaEvent_t *ev : {&r.up[i], &r.enc[i], &r.down[i]})
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e != cudaSuccess) return fail(ctx, e == cudaErrorMemoryAllocation ? MPTC_ENOMEM : MPTC_ECUDA,
                                     std::string("encode_stream_host: ") + cudaGetErrorString(e));
-  p.ready = true;
+  r.ready = true;
   return MPTC_OK;
 }
 
@@ -627,54 +674,125 @@ mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, i
     }
     return MPTC_OK;
   }
-  mptc_status st = pipe_init(ctx);
+  mptc_status st = ring_init(ctx);
+  if (st == MPTC_OK) st = lane_init(ctx);
   if (st != MPTC_OK) return st;
-  mptc_ctx::Pipe &p = ctx->pipe;
+  mptc_ctx::Ring &r = ctx->ring;
+  mptc_ctx *b = ctx->lane_b;
+  b->timing = ctx->timing;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // the copy streams start after the work already queued on `stream`
-  MPTC_CUDA(cudaMemsetAsync(p.status, 0, 4, s));
-  MPTC_CUDA(cudaEventRecord(p.start, s));
-  MPTC_CUDA(cudaStreamWaitEvent(p.cin, p.start, 0));
-  MPTC_CUDA(cudaStreamWaitEvent(p.cout, p.start, 0));
-  // frame k uses buffer slot k & 1; its upload waits until frame k-2 has
-  // been encoded (the slot's input is free), its encode until frame k-2's
-  // outputs are downloaded (the slot's outputs and final blocks are free)
-  auto upload = [&](int32_t k) -> cudaError_t {
-    const int slot = k & 1;
-    cudaError_t e = k >= 2 ? cudaStreamWaitEvent(p.cin, p.comp_done[slot], 0) : cudaSuccess;
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(p.rgb[slot], frames_host + k * in_bytes, in_bytes, cudaMemcpyHostToDevice, p.cin);
-    if (e == cudaSuccess) e = cudaEventRecord(p.in_ready[slot], p.cin);
-    return e;
-  };
-  MPTC_CUDA(upload(0));
-  if (n_frames > 1) MPTC_CUDA(upload(1));
+  // the side streams start after the work already queued on `stream`
+  MPTC_CUDA(cudaMemsetAsync(ctx->run_status, 0, sizeof(uint32_t), s));
+  MPTC_CUDA(cudaEventRecord(ctx->lane_start, s));
+  for (cudaStream_t t : {r.cin, r.cout, ctx->lane_s}) MPTC_CUDA(cudaStreamWaitEvent(t, ctx->lane_start, 0));
+  // Frame k lives in slot k % kRing. Before its upload, the slot's previous
+  // frame (k - kRing) must be downloaded; before its encode writes the slot's
+  // final blocks, the frame after that one (k - kRing + 1, slot (k+1) %
+  // kRing, whose previous frame they were) must be encoded. Intra frames after
+  // the first run on the second lane (as in mptc_encode_stream_device); the
+  // inter frame after one waits for its encode.
+  const uint64_t *prev = ctx->have_prev ? ctx->final_dev[ctx->cur] : nullptr;
+  bool prev_in_lane = false;
   for (int32_t k = 0; k < n_frames; ++k) {
-    const int slot = k & 1;
-    MPTC_CUDA(cudaStreamWaitEvent(s, p.in_ready[slot], 0));
-    if (k >= 2) MPTC_CUDA(cudaStreamWaitEvent(s, p.out_done[slot], 0));
-    const int nxt = ctx->have_prev ? 1 - ctx->cur : ctx->cur;
-    const uint64_t *prev = is_intra[k] ? nullptr : ctx->final_dev[ctx->cur];
-    st = mptc_encode_frame(ctx, p.rgb[slot], prev, ctx->stb, ctx->final_dev[nxt], p.motion[slot], p.unique[slot],
-                           p.n_unique[slot], stream);
-    if (st != MPTC_OK) return st;
-    status_or_kernel<<<1, 32, 0, s>>>(ctx->work, p.status);
+    const int i = k % kRing, nx = (k + 1) % kRing;
+    const bool reuse = k >= kRing;  // slot events of this run recorded earlier
+    if (reuse) MPTC_CUDA(cudaStreamWaitEvent(r.cin, r.down[i], 0));
+    MPTC_CUDA(cudaMemcpyAsync(r.rgb[i], frames_host + k * in_bytes, in_bytes, cudaMemcpyHostToDevice, r.cin));
+    MPTC_CUDA(cudaEventRecord(r.up[i], r.cin));
+    const bool lane = is_intra[k] && k > 0;
+    cudaStream_t es = lane ? ctx->lane_s : s;
+    MPTC_CUDA(cudaStreamWaitEvent(es, r.up[i], 0));
+    if (k + 1 >= kRing) MPTC_CUDA(cudaStreamWaitEvent(es, r.enc[nx], 0));
+    if (!lane && prev_in_lane) MPTC_CUDA(cudaStreamWaitEvent(s, r.enc[(k + kRing - 1) % kRing], 0));
+    st = mptc_encode_frame(lane ? b : ctx, r.rgb[i], is_intra[k] ? nullptr : prev, nullptr, r.fin[i], r.motion[i],
+                           r.unique[i], r.n_unique[i], es);
+    if (st != MPTC_OK) return lane ? fail(ctx, st, std::string("intra lane: ") + b->err) : st;
+    status_or_kernel<<<1, 32, 0, es>>>(lane ? b->work : ctx->work, ctx->run_status);
     ++ctx->launches;
-    MPTC_CUDA(cudaEventRecord(p.comp_done[slot], s));
-    ctx->cur = nxt;
-    ctx->have_prev = true;
-    MPTC_CUDA(cudaStreamWaitEvent(p.cout, p.comp_done[slot], 0));
-    MPTC_CUDA(cudaMemcpyAsync(final_host + k * n, ctx->final_dev[nxt], n * 8, cudaMemcpyDeviceToHost, p.cout));
-    MPTC_CUDA(cudaMemcpyAsync(motion_host + k * 2 * n, p.motion[slot], n * 2, cudaMemcpyDeviceToHost, p.cout));
-    MPTC_CUDA(cudaMemcpyAsync(unique_host + k * n, p.unique[slot], n * 4, cudaMemcpyDeviceToHost, p.cout));
-    MPTC_CUDA(cudaMemcpyAsync(n_unique_host + k, p.n_unique[slot], 4, cudaMemcpyDeviceToHost, p.cout));
-    MPTC_CUDA(cudaEventRecord(p.out_done[slot], p.cout));
-    if (k + 2 < n_frames) MPTC_CUDA(upload(k + 2));
+    MPTC_CUDA(cudaEventRecord(r.enc[i], es));
+    prev_in_lane = lane;
+    prev = r.fin[i];
+    MPTC_CUDA(cudaStreamWaitEvent(r.cout, r.enc[i], 0));
+    MPTC_CUDA(cudaMemcpyAsync(final_host + k * n, r.fin[i], n * 8, cudaMemcpyDeviceToHost, r.cout));
+    MPTC_CUDA(cudaMemcpyAsync(motion_host + k * 2 * n, r.motion[i], n * 2, cudaMemcpyDeviceToHost, r.cout));
+    MPTC_CUDA(cudaMemcpyAsync(unique_host + k * n, r.unique[i], n * 4, cudaMemcpyDeviceToHost, r.cout));
+    MPTC_CUDA(cudaMemcpyAsync(n_unique_host + k, r.n_unique[i], 4, cudaMemcpyDeviceToHost, r.cout));
+    MPTC_CUDA(cudaEventRecord(r.down[i], r.cout));
   }
-  // `stream` completes after the last download; the run's status word
-  MPTC_CUDA(cudaStreamWaitEvent(s, p.out_done[(n_frames - 1) & 1], 0));
+  // `stream` completes after every download; the run's last final blocks
+  // become the context's previous frame
+  const int last = (n_frames - 1) % kRing;
+  MPTC_CUDA(cudaStreamWaitEvent(s, r.down[last], 0));
+  MPTC_CUDA(cudaMemcpyAsync(ctx->final_dev[0], prev, n * 8, cudaMemcpyDeviceToDevice, s));
+  ctx->cur = 0;
+  ctx->have_prev = true;
+  ctx->last_is_intra = is_intra[n_frames - 1] ? 1u : 0u;
   uint32_t *h = reinterpret_cast<uint32_t *>(ctx->pin_out);
-  MPTC_CUDA(cudaMemcpyAsync(h, p.status, 4, cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaMemcpyAsync(h, ctx->run_status, 4, cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaStreamSynchronize(s));
+  if (*h & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
+  return MPTC_OK;
+}
+
+mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, int32_t n_frames,
+                                      const int32_t *is_intra, uint64_t *final_dev, uint8_t *motion_dev,
+                                      uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream) {
+  if (!ctx) return MPTC_EINVAL;
+  if (n_frames < 0 || (n_frames > 0 && (!frames_dev || !is_intra || !final_dev || !motion_dev || !unique_dev ||
+                                        !n_unique_dev)))
+    return fail(ctx, MPTC_EINVAL, "mptc_encode_stream_device: null pointer or negative frame count");
+  if (n_frames == 0) return MPTC_OK;
+  if (!is_intra[0] && !ctx->have_prev)
+    return fail(ctx, MPTC_ESTATE, "mptc_encode_stream_device: inter frame without a previous frame");
+  if (!aligned(frames_dev, 16) || !aligned(final_dev, 8) || !aligned(motion_dev, 2) || !aligned(unique_dev, 4) ||
+      !aligned(n_unique_dev, 4))
+    return fail(ctx, MPTC_EINVAL, "mptc_encode_stream_device: misaligned pointer");
+  mptc_status st = lane_init(ctx);
+  if (st != MPTC_OK) return st;
+  mptc_ctx *b = ctx->lane_b;
+  b->timing = ctx->timing;
+  const size_t n = (size_t)ctx->nblk, in_bytes = n * 48;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the intra lane starts after the work already queued on `stream`
+  MPTC_CUDA(cudaMemsetAsync(ctx->run_status, 0, sizeof(uint32_t), s));
+  MPTC_CUDA(cudaEventRecord(ctx->lane_start, s));
+  MPTC_CUDA(cudaStreamWaitEvent(ctx->lane_s, ctx->lane_start, 0));
+  const uint64_t *prev = ctx->have_prev ? ctx->final_dev[ctx->cur] : nullptr;
+  bool prev_in_lane = false;  // the previous frame is an intra frame of the second lane
+  for (int32_t k = 0; k < n_frames; ++k) {
+    const uint8_t *in = frames_dev + k * in_bytes;
+    uint64_t *fin = final_dev + k * n;
+    // a leading intra frame has no inter frames to overlap: the first lane
+    // runs it with all SMs
+    if (is_intra[k] && k > 0) {
+      st = mptc_encode_frame(b, in, nullptr, nullptr, fin, motion_dev + 2 * k * n, unique_dev + k * n,
+                             n_unique_dev + k, ctx->lane_s);
+      if (st != MPTC_OK) return fail(ctx, st, std::string("intra lane: ") + b->err);
+      status_or_kernel<<<1, 32, 0, ctx->lane_s>>>(b->work, ctx->run_status);
+      ++ctx->launches;
+      MPTC_CUDA(cudaEventRecord(ctx->lane_done, ctx->lane_s));
+      prev_in_lane = true;
+    } else {
+      if (prev_in_lane) MPTC_CUDA(cudaStreamWaitEvent(s, ctx->lane_done, 0));
+      prev_in_lane = false;
+      st = mptc_encode_frame(ctx, in, is_intra[k] ? nullptr : prev, nullptr, fin, motion_dev + 2 * k * n,
+                             unique_dev + k * n, n_unique_dev + k, stream);
+      if (st != MPTC_OK) return st;
+      status_or_kernel<<<1, 32, 0, s>>>(ctx->work, ctx->run_status);
+      ++ctx->launches;
+    }
+    prev = fin;
+  }
+  // `stream` completes after both lanes; the run's last frame becomes the
+  // context's previous frame
+  MPTC_CUDA(cudaEventRecord(ctx->lane_done, ctx->lane_s));
+  MPTC_CUDA(cudaStreamWaitEvent(s, ctx->lane_done, 0));
+  MPTC_CUDA(cudaMemcpyAsync(ctx->final_dev[0], prev, n * 8, cudaMemcpyDeviceToDevice, s));
+  ctx->cur = 0;
+  ctx->have_prev = true;
+  ctx->last_is_intra = is_intra[n_frames - 1] ? 1u : 0u;
+  uint32_t *h = reinterpret_cast<uint32_t *>(ctx->pin_out);
+  MPTC_CUDA(cudaMemcpyAsync(h, ctx->run_status, 4, cudaMemcpyDeviceToHost, s));
   MPTC_CUDA(cudaStreamSynchronize(s));
   if (*h & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
   return MPTC_OK;
@@ -720,6 +838,7 @@ mptc_status mptc_decoded_sse(const uint8_t *rgb_dev, int32_t width, int32_t heig
 mptc_status mptc_set_kernel_timing(mptc_ctx *ctx, int32_t enable) {
   if (!ctx) return MPTC_EINVAL;
   ctx->timing = enable != 0;
+  if (ctx->lane_b) ctx->lane_b->timing = ctx->timing;
   return MPTC_OK;
 }
 
@@ -727,15 +846,18 @@ mptc_status mptc_kernel_times(mptc_ctx *ctx, mptc_kernel_time *out, int32_t max_
   if (!ctx || !n_entries || (max_entries > 0 && !out)) return MPTC_EINVAL;
   double ms[K_COUNT] = {0};
   int cnt[K_COUNT] = {0};
-  for (const auto &r : ctx->recs) {
-    MPTC_CUDA(cudaEventSynchronize(r.b));
-    float t = 0.f;
-    MPTC_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
-    ms[r.kernel] += t;
-    cnt[r.kernel] += 1;
+  for (mptc_ctx *c : {ctx, ctx->lane_b}) {  // the stream calls' intra lane too
+    if (!c) continue;
+    for (const auto &r : c->recs) {
+      MPTC_CUDA(cudaEventSynchronize(r.b));
+      float t = 0.f;
+      MPTC_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+      ms[r.kernel] += t;
+      cnt[r.kernel] += 1;
+    }
+    c->recs.clear();
+    c->ev_used = 0;
   }
-  ctx->recs.clear();
-  ctx->ev_used = 0;
   int n = 0;
   for (int k = 0; k < K_COUNT && n < max_entries; ++k) {
     if (!cnt[k]) continue;

@@ -1118,9 +1118,11 @@ __device__ __forceinline__ uint64_t publish_intra(const SearchParams &P, const T
 // unique: motion (255,255), final = stb block.
 // One CTA per block, one window position per thread and round; CTAs claim
 // pending blocks one at a time from P.work, so every block a CTA waits on was
-// claimed earlier by a running CTA and the dataflow cannot deadlock.
+// claimed earlier by a running CTA and the dataflow cannot deadlock. At most
+// 64 registers per thread: the stream calls run this kernel beside the inter
+// kernels of other frames, which then keep more CTAs per SM.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) intra_search_kernel(SearchParams P, const uint32_t *__restrict__ pending,
+__global__ void __launch_bounds__(THREADS, 4) intra_search_kernel(SearchParams P, const uint32_t *__restrict__ pending,
                                                                const uint32_t *__restrict__ n_pending_dev,
                                                                int n_pending_host,
                                                                const uint32_t *__restrict__ run_flag = nullptr) {

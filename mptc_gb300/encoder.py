@@ -76,6 +76,21 @@ class Encoder:
                                       motion.data_ptr(), unique.data_ptr(), n_unique.data_ptr(), s),
               self._ctx)
 
+    def encode_stream_device(self, frames, final, motion, unique, n_unique, is_intra=None, stream=None) -> None:
+        """A run of frames on the device (mptc_encode_stream_device): frames is a
+        CUDA uint8 tensor (n, height, width, 3); final (n, nblk) int64, motion
+        (n, 2*nblk) uint8, unique (n, nblk) int32 and n_unique (n,) int32 CUDA
+        tensors receive each frame's outputs. Intra frames run on a second
+        lane, concurrently with the inter frames before them. is_intra: a flag
+        per frame, or None for the reference's schedule."""
+        n = frames.shape[0]
+        flags = np.array([self._intra_flag(None if is_intra is None else is_intra[k]) for k in range(n)],
+                         dtype=np.int32)
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_encode_stream_device(self._ctx, frames.data_ptr(), n, flags.ctypes.data,
+                                              final.data_ptr(), motion.data_ptr(), unique.data_ptr(),
+                                              n_unique.data_ptr(), s), self._ctx)
+
     def dxt1_encode_device(self, rgb, stb, orig_err, stream=None):
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
         check(lib().mptc_dxt1_encode(self._ctx, rgb.data_ptr(), stb.data_ptr(),

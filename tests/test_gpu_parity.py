@@ -192,6 +192,37 @@ def test_gpu_stream_host_matches_frame_host(torch_cuda, pinned):
     enc.close()
 
 
+def test_gpu_stream_device_matches_frame_host(torch_cuda):
+    """mptc_encode_stream_device (intra frames on the second lane, concurrent
+    with the inter frames before them) gives the per-frame results, across
+    calls that start with an intra or an inter frame, and the stream then
+    continues through the per-frame host call."""
+    torch = torch_cuda
+    from mptc_gb300.encoder import Encoder
+    frames = StreamSpec(256, 128, 9, seed=23, n_squares=3, square_size=40, speed_min=2,
+                        speed_max=5).generate()
+    ref = gpu_stream(frames, 8, 5, 3)  # intra frames 0, 3, 6
+    enc = Encoder(256, 128, 8, 5, 3)
+    n, dev = enc.nblk, torch.device("cuda")
+    src = torch.from_numpy(frames).to(dev)
+    fin = torch.zeros((8, n), dtype=torch.int64, device=dev)
+    mot = torch.zeros((8, 2 * n), dtype=torch.uint8, device=dev)
+    uni = torch.zeros((8, n), dtype=torch.int32, device=dev)
+    nu = torch.zeros(8, dtype=torch.int32, device=dev)
+    for a, b in ((0, 5), (5, 8)):  # the second call starts with an inter frame
+        enc.encode_stream_device(src[a:b], fin[a:b], mot[a:b], uni[a:b], nu[a:b],
+                                 stream=torch.cuda.current_stream())
+    fin, mot, uni, nu = (t.cpu().numpy() for t in (fin, mot, uni, nu))
+    for k in range(8):
+        np.testing.assert_array_equal(fin[k].view(np.uint64), ref[k][1], err_msg=f"frame {k} final")
+        np.testing.assert_array_equal(mot[k], ref[k][2], err_msg=f"frame {k} motion")
+        np.testing.assert_array_equal(uni[k, : nu[k]].view(np.uint32), ref[k][3], err_msg=f"frame {k} unique")
+    o = enc.encode_frame_host(frames[8])  # an inter frame on the run's last frame
+    np.testing.assert_array_equal(o.final, ref[8][1])
+    np.testing.assert_array_equal(o.motion, ref[8][2])
+    enc.close()
+
+
 def test_gpu_rejects_bad_arguments(torch_cuda):
     from mptc_gb300._lib import MptcError
     from mptc_gb300.encoder import Encoder
