@@ -26,6 +26,7 @@ constexpr int kSweeps = 6;          // default fixed-point sweeps of an inter fr
 constexpr int kMaxSweeps = 32;
 constexpr int kWorkWords = 16;      // counters and flags at the start of the per-frame work area
 constexpr int kRing = 24;           // host stream calls: device frame slots
+constexpr int kStbRing = 8;         // stream calls: stb encodes of inter frames done ahead
 constexpr int kLaneIntraShare = 5;  // stream calls: intra lane CTAs = kLaneIntraShare/8 of the SM count
 // The per-frame work area: kWorkWords words, then two u64 tile states per scan tile.
 size_t work_bytes(int ntiles) { return (kWorkWords + 4 * (size_t)ntiles) * sizeof(uint32_t); }
@@ -89,6 +90,13 @@ struct mptc_ctx {
   cudaStream_t lane_s = nullptr;
   cudaEvent_t lane_start = nullptr, lane_done = nullptr;
   uint32_t *run_status = nullptr;  // OR of a run's frame status words (device)
+  // the stb encodes of a run's inter frames depend only on their input: a
+  // third stream computes them ahead into kStbRing slots (stb blocks, errors)
+  cudaStream_t stb_s = nullptr;
+  unsigned char *stb_mem = nullptr;
+  uint64_t *stb_slot[kStbRing] = {};
+  int32_t *orig_slot[kStbRing] = {};
+  cudaEvent_t stb_done[kStbRing] = {}, stb_free[kStbRing] = {};
   uint32_t last_is_intra = 0;
   std::string err;
   // opt-in per-kernel event timing
@@ -405,6 +413,11 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
   if (ctx->lane_b) mptc_ctx_destroy(ctx->lane_b);
+  if (ctx->stb_s) cudaStreamDestroy(ctx->stb_s);
+  cudaFree(ctx->stb_mem);
+  for (int i = 0; i < kStbRing; ++i)
+    for (cudaEvent_t e : {ctx->stb_done[i], ctx->stb_free[i]})
+      if (e) cudaEventDestroy(e);
   if (ctx->lane_s) cudaStreamDestroy(ctx->lane_s);
   if (ctx->lane_start) cudaEventDestroy(ctx->lane_start);
   if (ctx->lane_done) cudaEventDestroy(ctx->lane_done);
@@ -607,6 +620,15 @@ mptc_status lane_init(mptc_ctx *ctx) {
   if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->lane_s, cudaStreamNonBlocking, prio_high);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_start, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stb_s, cudaStreamNonBlocking);
+  const size_t n = (size_t)ctx->nblk, per = ((n * 12 + 255) & ~(size_t)255) + 256;
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->stb_mem, per * kStbRing);
+  for (int i = 0; i < kStbRing && e == cudaSuccess; ++i) {
+    ctx->stb_slot[i] = reinterpret_cast<uint64_t *>(ctx->stb_mem + per * i);
+    ctx->orig_slot[i] = reinterpret_cast<int32_t *>(ctx->stb_mem + per * i + n * 8);
+    e = cudaEventCreateWithFlags(&ctx->stb_done[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stb_free[i], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     mptc_ctx_destroy(b);
     return fail(ctx, MPTC_ECUDA, std::string("stream call: ") + cudaGetErrorString(e));
@@ -615,6 +637,25 @@ mptc_status lane_init(mptc_ctx *ctx) {
   // five eighths of the SMs: the overlapped inter frames keep the rest
   b->intra_cap = std::max(1, ctx->sm_count * kLaneIntraShare / 8);
   ctx->lane_b = b;
+  return MPTC_OK;
+}
+
+// An inter frame of a stream call on the first lane: its stb encode runs on
+// the stb stream (after `ready`, when not null, and after the slot's previous
+// frame), the reencode on `s` once the stb blocks are there. `count` numbers
+// the run's inter frames.
+mptc_status run_inter_frame(mptc_ctx *ctx, int count, const uint8_t *in, cudaEvent_t ready, const uint64_t *prev,
+                            uint64_t *fin, uint8_t *motion, uint32_t *unique, uint32_t *n_unique, cudaStream_t s) {
+  const int j = count % kStbRing;
+  if (ready) MPTC_CUDA(cudaStreamWaitEvent(ctx->stb_s, ready, 0));
+  if (count >= kStbRing) MPTC_CUDA(cudaStreamWaitEvent(ctx->stb_s, ctx->stb_free[j], 0));
+  mptc_status st = mptc_dxt1_encode(ctx, in, ctx->stb_slot[j], ctx->orig_slot[j], ctx->stb_s);
+  if (st != MPTC_OK) return st;
+  MPTC_CUDA(cudaEventRecord(ctx->stb_done[j], ctx->stb_s));
+  MPTC_CUDA(cudaStreamWaitEvent(s, ctx->stb_done[j], 0));
+  st = mptc_reencode(ctx, in, ctx->stb_slot[j], ctx->orig_slot[j], prev, fin, motion, unique, n_unique, s);
+  if (st != MPTC_OK) return st;
+  MPTC_CUDA(cudaEventRecord(ctx->stb_free[j], s));
   return MPTC_OK;
 }
 
@@ -684,7 +725,8 @@ mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, i
   // the side streams start after the work already queued on `stream`
   MPTC_CUDA(cudaMemsetAsync(ctx->run_status, 0, sizeof(uint32_t), s));
   MPTC_CUDA(cudaEventRecord(ctx->lane_start, s));
-  for (cudaStream_t t : {r.cin, r.cout, ctx->lane_s}) MPTC_CUDA(cudaStreamWaitEvent(t, ctx->lane_start, 0));
+  for (cudaStream_t t : {r.cin, r.cout, ctx->lane_s, ctx->stb_s}) MPTC_CUDA(cudaStreamWaitEvent(t, ctx->lane_start, 0));
+  int n_inter = 0;
   // Frame k lives in slot k % kRing. Before its upload, the slot's previous
   // frame (k - kRing) must be downloaded; before its encode writes the slot's
   // final blocks, the frame after that one (k - kRing + 1, slot (k+1) %
@@ -704,8 +746,12 @@ mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, i
     MPTC_CUDA(cudaStreamWaitEvent(es, r.up[i], 0));
     if (k + 1 >= kRing) MPTC_CUDA(cudaStreamWaitEvent(es, r.enc[nx], 0));
     if (!lane && prev_in_lane) MPTC_CUDA(cudaStreamWaitEvent(s, r.enc[(k + kRing - 1) % kRing], 0));
-    st = mptc_encode_frame(lane ? b : ctx, r.rgb[i], is_intra[k] ? nullptr : prev, nullptr, r.fin[i], r.motion[i],
-                           r.unique[i], r.n_unique[i], es);
+    if (is_intra[k])
+      st = mptc_encode_frame(lane ? b : ctx, r.rgb[i], nullptr, nullptr, r.fin[i], r.motion[i], r.unique[i],
+                             r.n_unique[i], es);
+    else
+      st = run_inter_frame(ctx, n_inter++, r.rgb[i], r.up[i], prev, r.fin[i], r.motion[i], r.unique[i],
+                           r.n_unique[i], s);
     if (st != MPTC_OK) return lane ? fail(ctx, st, std::string("intra lane: ") + b->err) : st;
     status_or_kernel<<<1, 32, 0, es>>>(lane ? b->work : ctx->work, ctx->run_status);
     ++ctx->launches;
@@ -757,8 +803,10 @@ mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, 
   MPTC_CUDA(cudaMemsetAsync(ctx->run_status, 0, sizeof(uint32_t), s));
   MPTC_CUDA(cudaEventRecord(ctx->lane_start, s));
   MPTC_CUDA(cudaStreamWaitEvent(ctx->lane_s, ctx->lane_start, 0));
+  MPTC_CUDA(cudaStreamWaitEvent(ctx->stb_s, ctx->lane_start, 0));
   const uint64_t *prev = ctx->have_prev ? ctx->final_dev[ctx->cur] : nullptr;
   bool prev_in_lane = false;  // the previous frame is an intra frame of the second lane
+  int n_inter = 0;
   for (int32_t k = 0; k < n_frames; ++k) {
     const uint8_t *in = frames_dev + k * in_bytes;
     uint64_t *fin = final_dev + k * n;
@@ -775,8 +823,12 @@ mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, 
     } else {
       if (prev_in_lane) MPTC_CUDA(cudaStreamWaitEvent(s, ctx->lane_done, 0));
       prev_in_lane = false;
-      st = mptc_encode_frame(ctx, in, is_intra[k] ? nullptr : prev, nullptr, fin, motion_dev + 2 * k * n,
-                             unique_dev + k * n, n_unique_dev + k, stream);
+      if (is_intra[k])
+        st = mptc_encode_frame(ctx, in, nullptr, nullptr, fin, motion_dev + 2 * k * n, unique_dev + k * n,
+                               n_unique_dev + k, stream);
+      else
+        st = run_inter_frame(ctx, n_inter++, in, nullptr, prev, fin, motion_dev + 2 * k * n, unique_dev + k * n,
+                             n_unique_dev + k, s);
       if (st != MPTC_OK) return st;
       status_or_kernel<<<1, 32, 0, s>>>(ctx->work, ctx->run_status);
       ++ctx->launches;
