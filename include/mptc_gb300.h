@@ -153,9 +153,9 @@ mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, 
  * the caller passes the configuration, the frame size, the input frame and
  * every output buffer; the kernels' scratch (per-block completion words, the
  * stb error of each block, the wavefront order, pending list and sweep
- * estimates of the intra search, the refit weight sums of the previous frame's
- * blocks, work counters, tile counts) lives in one
- * file-scope device array of about 6.5 MiB inside the library, which every GPU
+ * estimates and stored statistics of the intra search, the refit weight sums
+ * of the previous frame's blocks, work counters and scan tile states) lives in
+ * one file-scope device array of about 8.1 MiB inside the library, which every GPU
  * that loads the library holds until the process exits.
  *
  * Frames larger than MPTC_NOALLOC_MAX_BLOCKS blocks are rejected with

@@ -24,6 +24,9 @@ constexpr int kInterRun = 8;        // inter search at sa <= 8: blocks per warp 
 constexpr int kIntraThreads = 256;  // intra search: one block per CTA
 constexpr int kSweeps = 6;          // default fixed-point sweeps of an inter frame's intra pass
 constexpr int kMaxSweeps = 32;
+constexpr int kSweepPart = kIntraThreads / 32;  // stored sweep statistics per open block (one per warp)
+constexpr int kSweepPartCap = 32768;            // open blocks with stored statistics (context)
+constexpr int kSweepPartCapNoalloc = 4096;      // the same for mptc_encode_frame_noalloc
 constexpr int kWorkWords = 16;      // counters and flags at the start of the per-frame work area
 constexpr int kRing = 24;           // host stream calls: device frame slots
 constexpr int kStbRing = 8;         // stream calls: stb encodes of inter frames done ahead
@@ -57,6 +60,7 @@ struct mptc_ctx {
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
   float4 *wdesc = nullptr;         // refit weight sums of the previous frame's blocks
   uint32_t *sweep = nullptr;       // intra sweeps: 2 estimate buffers of n words + kMaxSweeps + 1 change flags
+  mptc::SweepPartial *sweep_part = nullptr;  // intra sweeps: stored statistics, kSweepPart per open block
   uint64_t *stb = nullptr;         // stb blocks (encode_frame / host path)
   int32_t *orig_err = nullptr;
   // host-path buffers
@@ -275,17 +279,19 @@ int sweep_count(int32_t cfg) { return cfg == 0 ? kSweeps : (cfg < 0 ? 0 : std::m
 // sweep: 2 * n estimate words followed by kMaxSweeps + 1 change flags; the
 // pending scan has set the first estimates and flags. Returns the number of
 // kernels launched.
+// part: kSweepPart statistics per open block for the first part_cap open
+// blocks (their final-block positions, kept from the first sweep).
 int launch_intra_sweeps(const mptc::SearchParams &P, const uint32_t *pending, const uint32_t *n_pending,
-                        uint32_t *sweep, int n, int grid, int sweeps, cudaStream_t s) {
+                        uint32_t *sweep, int n, int grid, int sweeps, mptc::SweepPartial *part, int part_cap,
+                        cudaStream_t s) {
   if (sweeps == 0) {
     mptc::intra_search_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, -1);
     return 1;
   }
   uint32_t *est[2] = {sweep, sweep + n}, *changed = sweep + 2 * (size_t)n;
   for (int k = 0; k < sweeps; ++k)
-    mptc::intra_sweep_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, est[k & 1],
-                                                                           est[(k + 1) & 1], changed + k,
-                                                                           changed + k + 1);
+    mptc::intra_sweep_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(
+        P, pending, n_pending, est[k & 1], est[(k + 1) & 1], changed + k, changed + k + 1, part, part_cap, k == 0);
   mptc::intra_search_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, -1,
                                                                           changed + sweeps);
   return sweeps + 1;
@@ -377,7 +383,8 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
       dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
       dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1) || dalloc(&ctx->order, n) ||
-      dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 2 * n + kMaxSweeps + 1))
+      dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 2 * n + kMaxSweeps + 1) ||
+      dalloc(&ctx->sweep_part, (size_t)kSweepPart * std::min(ctx->nblk, kSweepPartCap)))
     return bad(MPTC_ENOMEM);
   ctx->tile_state = reinterpret_cast<uint64_t *>(ctx->work + kWorkWords);
   if (cudaMemset(ctx->work, 0, work_bytes(ctx->ntiles)) != cudaSuccess) return bad(MPTC_ECUDA);
@@ -406,6 +413,7 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->pending);
   cudaFree(ctx->wdesc);
   cudaFree(ctx->sweep);
+  cudaFree(ctx->sweep_part);
   cudaFree(ctx->femb);
   cudaFree(ctx->gemb);
   cudaFree(ctx->topk);
@@ -506,7 +514,8 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     const int ig = ctx->intra_cap > 0 ? std::min(ctx->intra_cap, ctx->intra_grid) : ctx->intra_grid;
     if (prev_final_dev)
       ctx->launches += launch_intra_sweeps(P, ctx->pending, ctx->work + 5, ctx->sweep, ctx->nblk, ig,
-                                           sweep_count(ctx->cfg.intra_sweeps), s);
+                                           sweep_count(ctx->cfg.intra_sweeps), ctx->sweep_part,
+                                           std::min(ctx->nblk, kSweepPartCap), s);
     else
       mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
     if (!prev_final_dev) ++ctx->launches;
@@ -949,7 +958,8 @@ constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
 constexpr size_t kNaWdesc = kNaPending + kNaMaxBlocks * 4;      // float4 per block
 constexpr size_t kNaSweep = kNaWdesc + kNaMaxBlocks * 16;       // u32: 2 per block + change flags
 constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // work area (after kMaxSweeps + 1 flags)
-constexpr size_t kNaBytes = kNaWork + ((kWorkWords * 4 + kNaTiles * 16 + 255) / 256) * 256;
+constexpr size_t kNaPart = kNaWork + ((kWorkWords * 4 + kNaTiles * 16 + 255) / 256) * 256;  // sweep statistics
+constexpr size_t kNaBytes = kNaPart + ((sizeof(mptc::SweepPartial) * kSweepPart * kSweepPartCapNoalloc + 255) / 256) * 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
@@ -1023,6 +1033,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
   uint32_t *pend = reinterpret_cast<uint32_t *>(d->scratch + kNaPending);
   float4 *wdesc = reinterpret_cast<float4 *>(d->scratch + kNaWdesc);
   uint32_t *sweep = reinterpret_cast<uint32_t *>(d->scratch + kNaSweep);
+  mptc::SweepPartial *sweep_part = reinterpret_cast<mptc::SweepPartial *>(d->scratch + kNaPart);
   const int bw = width / 4, bh = height / 4, n = (int)nblk;
   const int ntiles = (n + mptc::kScanTile - 1) / mptc::kScanTile;
 
@@ -1055,7 +1066,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
     mptc::pending_scan_kernel<<<ntiles, 256, 0, s>>>(order, done, stb, n, ntiles, tile_state, work + 10, pend,
                                                     work + 5, sweep, sweep + 2 * (size_t)n, sw ? sw + 1 : 0,
                                                     work + 1);
-    launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, sw, s);
+    launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, sw, sweep_part, kSweepPartCapNoalloc, s);
   } else {
     mptc::intra_search_kernel<kIntraThreads><<<d->intra_grid, kIntraThreads, 0, s>>>(P, order, nullptr, n);
   }

@@ -318,7 +318,50 @@ struct ThreadSel : LaneSel {
       mn = SelPick{cand, eps, refit};
     }
   }
+  // Takes in statistics of other positions (the minimum's ties broken by
+  // position, as scan order does).
+  template <class S>
+  __device__ __forceinline__ void merge(const S &o) {
+    if (o.le0_pos < le0_pos) {
+      le0_pos = o.le0_pos;
+      le0 = o.le0;
+    }
+    if (o.neg_key > neg_key) {
+      neg_key = o.neg_key;
+      neg = o.neg;
+    }
+    if (o.min_e < min_e || (o.min_e == min_e && o.min_pos < min_pos)) {
+      min_e = o.min_e;
+      min_pos = o.min_pos;
+      mn = o.mn;
+    }
+  }
 };
+
+// A warp's selection statistics over some of its positions, kept in global
+// memory from one fixed-point sweep to the next (intra_sweep_kernel).
+struct SweepPartial {
+  int le0_pos, neg_key, min_e, min_pos;
+  SelPick le0, neg, mn;
+};
+
+// Reduces the warp's ThreadSel statistics into *dst (lanes holding a
+// statistic write its candidate data; positions are distinct).
+__device__ __forceinline__ void warp_store_partial(const ThreadSel &t, SweepPartial *dst, int lane) {
+  const int le0 = __reduce_min_sync(kFull, t.le0_pos);
+  const int nk = __reduce_max_sync(kFull, t.neg_key);
+  const int me = __reduce_min_sync(kFull, t.min_e);
+  const int mp = __reduce_min_sync(kFull, t.min_e == me ? t.min_pos : 0x7fffffff);
+  if (lane == 0) {
+    dst->le0_pos = le0;
+    dst->neg_key = nk;
+    dst->min_e = me;
+    dst->min_pos = mp;
+  }
+  if (le0 != 0x7fffffff && t.le0_pos == le0) dst->le0 = t.le0;
+  if (nk >= 0 && t.neg_key == nk) dst->neg = t.neg;
+  if (mp != 0x7fffffff && t.min_e == me && t.min_pos == mp) dst->mn = t.mn;
+}
 
 // Completion word of a final block: bit 32 set, the low half the block's
 // index word, which is all a waiting block reads of it.
@@ -1082,18 +1125,23 @@ __device__ __forceinline__ int cached_eval(EvalCache &c, bool use, const BlockTa
 }
 
 // Selection and output of one block of the intra search: the CTA reduces
-// the threads' statistics, then one thread writes the final block and motion
-// code (and, when `publish`, the block's completion word). Returns the
-// block's completion word in that thread and 0 in the others. Ends with a
-// barrier.
+// the threads' statistics, then the thread holding the selected statistic
+// writes the final block and motion code (and, when `publish`, the block's
+// completion word). Returns the block's completion word in that thread and 0
+// in the others. Ends with a barrier.
 template <int THREADS>
 __device__ __forceinline__ uint64_t publish_intra(const SearchParams &P, const ThreadSel &ts, CtaReduce<THREADS> &red,
                                                   int idx, uint64_t stb, int w2, int tid, bool publish) {
   int m, pick;
   const int sel = cta_select<THREADS>(ts, red, w2, m, pick);
   const bool accept = sel >= 0 && m <= P.thr;
+  // the thread whose statistics hold the selected position (its own position,
+  // or, in the later sweeps, statistics merged from the first)
+  const bool holder = pick == 0   ? ts.le0_pos == sel
+                      : pick == 1 ? ts.neg_key >= 0 && 0xFFFF - (ts.neg_key & 0xFFFF) == sel
+                                  : ts.min_e == m && ts.min_pos == sel;
   uint64_t out = 0;
-  if (accept ? tid == sel % THREADS : tid == 0) {
+  if (accept ? holder : tid == 0) {
     uint16_t code = 0xFFFFu;
     uint64_t blk = stb;
     if (accept) {
@@ -1194,13 +1242,20 @@ __global__ void __launch_bounds__(THREADS, 4) intra_search_kernel(SearchParams P
 // something (changed[k] != 0); if the last sweep still changed something, the
 // dataflow kernel recomputes the open blocks exactly. Sweeps have no waits:
 // every open block is independent within a sweep.
+// Positions whose block is final (done) give the same results in every sweep
+// (on the 1080p stream 85% of an open block's positions): the first sweep
+// stores each warp's statistics over them (part, for the first part_cap open
+// blocks), and the later sweeps evaluate only the positions whose block is
+// open, merging the stored statistics in.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, const uint32_t *__restrict__ pending,
+__global__ void __launch_bounds__(THREADS, 3) intra_sweep_kernel(SearchParams P, const uint32_t *__restrict__ pending,
                                                               const uint32_t *__restrict__ n_pending_dev,
                                                               const uint32_t *__restrict__ cur,
                                                               uint32_t *__restrict__ next,
                                                               const uint32_t *__restrict__ changed_in,
-                                                              uint32_t *__restrict__ changed_out) {
+                                                              uint32_t *__restrict__ changed_out,
+                                                              SweepPartial *__restrict__ part, int part_cap,
+                                                              bool first) {
   if (__ldcg(changed_in) == 0u) return;
   __shared__ BlockTab s_tab;
   __shared__ EvalCache s_cache;
@@ -1229,8 +1284,10 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
     const int orig = __ldg(P.orig_err + idx);
     const int sumsq = s_sumsq;
     const PixelGroups pg = load_groups(s_tab);
-    ThreadSel ts;
+    ThreadSel ts, tf;  // all positions; (first sweep) those of final blocks
     int looked = 0, hits = 0;
+    const bool stored = k < part_cap;
+    SweepPartial *wp = part + ((size_t)k * (THREADS / 32) + (tid >> 5));
     for (int base = 0; base < npos; base += THREADS) {
       const int pos = base + tid;
       const int row = pos / w2, col = pos - row * w2;
@@ -1238,14 +1295,19 @@ __global__ void __launch_bounds__(THREADS) intra_sweep_kernel(SearchParams P, co
       if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
         const size_t nidx = (size_t)j * P.bw + i;
         const uint64_t w = __ldcg(P.done + nidx);
+        if (w && !first && stored) continue;  // in the stored statistics
         const uint32_t cand = w ? (uint32_t)w : __ldcg(cur + nidx);
         uint32_t eps = 0;
         int refit = 0;
         const int e = cached_eval(s_cache, cache.on, s_tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq,
                                   eps, refit, looked, hits);
         ts.add(pos, row, e, cand, eps, refit);
+        if (w) tf.add(pos, row, e, cand, eps, refit);
       }
     }
+    if (first && stored) warp_store_partial(tf, wp, lane);
+    // after the lane's own positions, which add() expects in scan order
+    if (!first && stored && lane == 0) ts.merge(*wp);
     const uint64_t w = publish_intra(P, ts, red, idx, stb, w2, tid, false);
     cache.update(__syncthreads_count(looked > 0), __syncthreads_count(hits > 0));
     if (w != 0) {  // the thread that wrote the result
