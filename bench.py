@@ -42,7 +42,7 @@ C_CAND, C_DXT = 600, 1500
 # DRAM bytes (read + write) per launch of the search kernels on the 1080p
 # stream, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum);
 # the summaries under profiles/ give the commands.
-NCU_TRAFFIC = {"inter_search": 10_906_368 + 96_768, "intra_search_kernel": 9_363_968 + 185_856}
+NCU_TRAFFIC = {"inter_search": 10_906_368 + 96_768, "intra_search_kernel": 9_365_248 + 382_464}
 
 
 def algo_bytes(kernel: str, n: int) -> int:

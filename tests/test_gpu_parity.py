@@ -233,6 +233,17 @@ def test_gpu_rejects_bad_arguments(torch_cuda):
     enc = Encoder(32, 32)
     with pytest.raises(MptcError):  # an inter frame needs a previous frame
         enc.encode_frame_host(np.zeros((32, 32, 3), np.uint8), is_intra=False)
+    with pytest.raises(MptcError):  # the same for a run that starts with one
+        enc.encode_stream_host(np.zeros((2, 32, 32, 3), np.uint8), is_intra=[False, False])
+    torch = torch_cuda
+    z = torch.zeros((2, 32, 32, 3), dtype=torch.uint8, device="cuda")
+    outs = (torch.zeros((2, 64), dtype=torch.int64, device="cuda"), torch.zeros((2, 128), dtype=torch.uint8, device="cuda"),
+            torch.zeros((2, 64), dtype=torch.int32, device="cuda"), torch.zeros(2, dtype=torch.int32, device="cuda"))
+    with pytest.raises(MptcError):
+        enc.encode_stream_device(z, *outs, is_intra=[False, True])
+    enc.encode_stream_device(z[:0], *(o[:0] for o in outs), is_intra=[])  # an empty run does nothing
+    enc.encode_stream_device(z, *outs, is_intra=[True, False])
+    assert (outs[0].cpu().numpy() != 0).any()
     enc.close()
 
 
