@@ -30,7 +30,7 @@ constexpr int kSweepPartCapNoalloc = 4096;      // the same for mptc_encode_fram
 constexpr int kWorkWords = 16;      // counters and flags at the start of the per-frame work area
 constexpr int kRing = 24;           // host stream calls: device frame slots
 constexpr int kStbRing = 8;         // stream calls: stb encodes of inter frames done ahead
-constexpr int kLaneIntraShare = 5;  // stream calls: intra lane CTAs = kLaneIntraShare/8 of the SM count
+constexpr int kLaneIntraShare = 4;  // stream calls: intra lane CTAs = kLaneIntraShare/8 of the SM count
 // The per-frame work area: kWorkWords words, then two u64 tile states per scan tile.
 size_t work_bytes(int ntiles) { return (kWorkWords + 4 * (size_t)ntiles) * sizeof(uint32_t); }
 
@@ -643,7 +643,7 @@ mptc_status lane_init(mptc_ctx *ctx) {
     return fail(ctx, MPTC_ECUDA, std::string("stream call: ") + cudaGetErrorString(e));
   }
   b->timing = ctx->timing;
-  // five eighths of the SMs: the overlapped inter frames keep the rest
+  // half the SMs: the overlapped inter frames keep the other half
   b->intra_cap = std::max(1, ctx->sm_count * kLaneIntraShare / 8);
   ctx->lane_b = b;
   return MPTC_OK;
