@@ -34,13 +34,29 @@ def _noalloc(lib, cfg, w, h, rgb, prev, stb, fin, mot, uni, nu, stream):
         ctypes.c_void_p(stream.cuda_stream))
 
 
-@pytest.mark.parametrize("w,h,sa,thr", [(256, 192, 8, 5), (1920, 1080, 8, 5)])
-def test_noalloc_matches_encode_frame_two_calls(torch_cuda, w, h, sa, thr):
+def _noisy_pair(w, h):
+    """Two frames of noise with a drifting gradient band: nearly every block
+    stays open after the inter search (more open blocks than the no-alloc
+    scratch keeps sweep statistics for)."""
+    rng = np.random.default_rng(77)
+    frames = rng.integers(0, 256, size=(2, h, w, 3), dtype=np.uint8)
+    yy, xx = np.mgrid[0:h, 0:w // 4]
+    for k in range(2):
+        g = (xx * 2 + yy + 3 * k) % 256
+        frames[k, :, : w // 4, 0] = g
+        frames[k, :, : w // 4, 1] = 255 - g
+        frames[k, :, : w // 4, 2] = g // 2
+    return frames
+
+
+@pytest.mark.parametrize("w,h,sa,thr,content", [(256, 192, 8, 5, "stream"), (1920, 1080, 8, 5, "stream"),
+                                                (512, 512, 8, 5, "noise")])
+def test_noalloc_matches_encode_frame_two_calls(torch_cuda, w, h, sa, thr, content):
     torch = torch_cuda
     from mptc_gb300._lib import MPTC_OK, Config, lib
     from mptc_gb300.encoder import Encoder
 
-    frames = StreamSpec(w, h, 2, seed=321).generate()
+    frames = StreamSpec(w, h, 2, seed=321).generate() if content == "stream" else _noisy_pair(w, h)
     dev = torch.device("cuda")
     n = (w // 4) * (h // 4)
     stream = torch.cuda.current_stream()
@@ -81,6 +97,11 @@ def test_noalloc_matches_encode_frame_two_calls(torch_cuda, w, h, sa, thr):
             np.testing.assert_array_equal(g[key].cpu().numpy(), r[key].cpu().numpy(),
                                           err_msg=f"call {k}: {key}")
         np.testing.assert_array_equal(g["uni"][:cnt].cpu().numpy(), r["uni"][:cnt].cpu().numpy())
+    if content == "noise":  # both against the oracle on the inter frame
+        import oracle
+        ref_o = oracle.encode_stream(frames, sa, thr, 16, threads=8)
+        np.testing.assert_array_equal(got[1]["fin"].cpu().numpy().view(np.uint64), ref_o[1].final)
+        np.testing.assert_array_equal(got[1]["mot"].cpu().numpy(), ref_o[1].motion)
 
 
 def test_noalloc_rejects_oversize_frame(torch_cuda):
