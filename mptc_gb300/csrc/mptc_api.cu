@@ -59,7 +59,7 @@ struct mptc_ctx {
   uint32_t *order = nullptr;       // blocks in wavefront order
   uint32_t *pending = nullptr;     // pending blocks of the current frame, wavefront order
   float4 *wdesc = nullptr;         // refit weight sums of the previous frame's blocks
-  uint32_t *sweep = nullptr;       // intra sweeps: 2 estimate buffers of n words + kMaxSweeps + 1 change flags
+  uint32_t *sweep = nullptr;       // intra sweeps: 3 estimate buffers of n words + kMaxSweeps + 1 change flags
   mptc::SweepPartial *sweep_part = nullptr;  // intra sweeps: stored statistics, kSweepPart per open block
   uint64_t *stb = nullptr;         // stb blocks (encode_frame / host path)
   int32_t *orig_err = nullptr;
@@ -276,7 +276,7 @@ namespace {
 // Sweeps to run for a configuration's intra_sweeps value.
 int sweep_count(int32_t cfg) { return cfg == 0 ? kSweeps : (cfg < 0 ? 0 : std::min(cfg, kMaxSweeps)); }
 
-// sweep: 2 * n estimate words followed by kMaxSweeps + 1 change flags; the
+// sweep: 3 * n estimate words followed by kMaxSweeps + 1 change flags; the
 // pending scan has set the first estimates and flags. Returns the number of
 // kernels launched.
 // part: kSweepPart statistics per open block for the first part_cap open
@@ -288,10 +288,13 @@ int launch_intra_sweeps(const mptc::SearchParams &P, const uint32_t *pending, co
     mptc::intra_search_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, -1);
     return 1;
   }
-  uint32_t *est[2] = {sweep, sweep + n}, *changed = sweep + 2 * (size_t)n;
+  // three estimate buffers: sweep k reads E[k % 3] and, for its skip test,
+  // E[(k + 2) % 3] (the estimates sweep k-1 read), and writes E[(k + 1) % 3]
+  uint32_t *est[3] = {sweep, sweep + n, sweep + 2 * (size_t)n}, *changed = sweep + 3 * (size_t)n;
   for (int k = 0; k < sweeps; ++k)
     mptc::intra_sweep_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(
-        P, pending, n_pending, est[k & 1], est[(k + 1) & 1], changed + k, changed + k + 1, part, part_cap, k == 0);
+        P, pending, n_pending, est[k % 3], est[(k + 2) % 3], est[(k + 1) % 3], changed + k, changed + k + 1, part,
+        part_cap, k == 0);
   mptc::intra_search_kernel<kIntraThreads><<<grid, kIntraThreads, 0, s>>>(P, pending, n_pending, -1,
                                                                           changed + sweeps);
   return sweeps + 1;
@@ -383,7 +386,7 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
       dalloc(&ctx->final_dev[0], n) || dalloc(&ctx->final_dev[1], n) || dalloc(&ctx->motion_dev, 2 * n) ||
       dalloc(&ctx->unique_dev, n) || dalloc(&ctx->n_unique_dev, 1) || dalloc(&ctx->order, n) ||
-      dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 2 * n + kMaxSweeps + 1) ||
+      dalloc(&ctx->pending, n) || dalloc(&ctx->wdesc, n) || dalloc(&ctx->sweep, 3 * n + kMaxSweeps + 1) ||
       dalloc(&ctx->sweep_part, (size_t)kSweepPart * std::min(ctx->nblk, kSweepPartCap)))
     return bad(MPTC_ENOMEM);
   ctx->tile_state = reinterpret_cast<uint64_t *>(ctx->work + kWorkWords);
@@ -507,7 +510,7 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     const int sw = sweep_count(ctx->cfg.intra_sweeps);
     mptc::pending_scan_kernel<<<ctx->ntiles, 256, 0, s>>>(
         ctx->order, ctx->done, stb_dev, ctx->nblk, ctx->ntiles, ctx->tile_state, ctx->work + 10, ctx->pending,
-        ctx->work + 5, ctx->sweep, ctx->sweep + 2 * (size_t)ctx->nblk, sw ? sw + 1 : 0, ctx->work + 1);
+        ctx->work + 5, ctx->sweep, ctx->sweep + 3 * (size_t)ctx->nblk, sw ? sw + 1 : 0, ctx->work + 1);
   }
   {
     KernelTimer t(ctx, prev_final_dev ? K_PENDING : K_INTRA, s);
@@ -956,8 +959,8 @@ constexpr size_t kNaOrig = kNaStb + kNaMaxBlocks * 8;           // i32 per block
 constexpr size_t kNaOrder = kNaOrig + kNaMaxBlocks * 4;         // u32 per block
 constexpr size_t kNaPending = kNaOrder + kNaMaxBlocks * 4;      // u32 per block
 constexpr size_t kNaWdesc = kNaPending + kNaMaxBlocks * 4;      // float4 per block
-constexpr size_t kNaSweep = kNaWdesc + kNaMaxBlocks * 16;       // u32: 2 per block + change flags
-constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 8 + 256;   // work area (after kMaxSweeps + 1 flags)
+constexpr size_t kNaSweep = kNaWdesc + kNaMaxBlocks * 16;       // u32: 3 per block + change flags
+constexpr size_t kNaWork = kNaSweep + kNaMaxBlocks * 12 + 256;  // work area (after kMaxSweeps + 1 flags)
 constexpr size_t kNaPart = kNaWork + ((kWorkWords * 4 + kNaTiles * 16 + 255) / 256) * 256;  // sweep statistics
 constexpr size_t kNaBytes = kNaPart + ((sizeof(mptc::SweepPartial) * kSweepPart * kSweepPartCapNoalloc + 255) / 256) * 256;
 
@@ -1064,7 +1067,7 @@ extern "C" mptc_status mptc_encode_frame_noalloc(const mptc_config *cfg, int32_t
     launch_inter_search(P, kSearchWarps, work, pend, d->sm_count, s);
     const int sw = sweep_count(cfg->intra_sweeps);
     mptc::pending_scan_kernel<<<ntiles, 256, 0, s>>>(order, done, stb, n, ntiles, tile_state, work + 10, pend,
-                                                    work + 5, sweep, sweep + 2 * (size_t)n, sw ? sw + 1 : 0,
+                                                    work + 5, sweep, sweep + 3 * (size_t)n, sw ? sw + 1 : 0,
                                                     work + 1);
     launch_intra_sweeps(P, pend, work + 5, sweep, n, d->intra_grid, sw, sweep_part, kSweepPartCapNoalloc, s);
   } else {

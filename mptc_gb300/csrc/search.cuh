@@ -1246,11 +1246,14 @@ __global__ void __launch_bounds__(THREADS, 4) intra_search_kernel(SearchParams P
 // (on the 1080p stream 85% of an open block's positions): the first sweep
 // stores each warp's statistics over them (part, for the first part_cap open
 // blocks), and the later sweeps evaluate only the positions whose block is
-// open, merging the stored statistics in.
+// open, merging the stored statistics in. A later sweep also skips a block
+// whose open window blocks all kept the estimates the previous sweep read
+// (cur against before): its result, already written, cannot change.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS, 3) intra_sweep_kernel(SearchParams P, const uint32_t *__restrict__ pending,
                                                               const uint32_t *__restrict__ n_pending_dev,
                                                               const uint32_t *__restrict__ cur,
+                                                              const uint32_t *__restrict__ before,
                                                               uint32_t *__restrict__ next,
                                                               const uint32_t *__restrict__ changed_in,
                                                               uint32_t *__restrict__ changed_out,
@@ -1273,6 +1276,21 @@ __global__ void __launch_bounds__(THREADS, 3) intra_sweep_kernel(SearchParams P,
   for (int k = blockIdx.x; k < n_pend; k += gridDim.x) {
     const int idx = (int)__ldcg(pending + k);
     const int by = idx / P.bw, bx = idx - by * P.bw;
+    if (!first) {  // any open window block with a new estimate?
+      bool moved = false;
+      for (int pos = tid; pos < npos; pos += THREADS) {
+        const int row = pos / w2, col = pos - row * w2;
+        const int j = by - row, i = bx + P.sa - 1 - col;
+        if (i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) {
+          const size_t nidx = (size_t)j * P.bw + i;
+          if (__ldcg(P.done + nidx) == 0ull && __ldcg(cur + nidx) != __ldcg(before + nidx)) moved = true;
+        }
+      }
+      if (!__syncthreads_or(moved)) {
+        if (tid == 0) next[idx] = __ldcg(cur + idx);
+        continue;
+      }
+    }
     const uint64_t stb = __ldg(P.stb + idx);
     const uint32_t own = (uint32_t)(stb >> 32);
     eval_cache_reset(s_cache, own);
