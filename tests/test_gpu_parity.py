@@ -192,6 +192,32 @@ def test_gpu_stream_host_matches_frame_host(torch_cuda, pinned):
     enc.close()
 
 
+def test_gpu_stream_host_ring_wraps(torch_cuda):
+    """A pinned host run longer than the device frame ring (24 slots), with
+    intra frames every 5th frame on the second lane: every frame matches the
+    per-frame host call."""
+    torch = torch_cuda
+    from mptc_gb300.encoder import Encoder, StreamOutput
+    nf = 31
+    frames = StreamSpec(128, 64, nf, seed=29, n_squares=2, square_size=24, speed_min=1,
+                        speed_max=4).generate()
+    ref = gpu_stream(frames, 4, 5, 5)
+    enc = Encoder(128, 64, 4, 5, 5)
+    n = enc.nblk
+    src = torch.from_numpy(frames).pin_memory().numpy()
+    out = StreamOutput(torch.zeros((nf, n), dtype=torch.int64).pin_memory().numpy().view(np.uint64),
+                       torch.zeros((nf, 2 * n), dtype=torch.uint8).pin_memory().numpy(),
+                       torch.zeros((nf, n), dtype=torch.int32).pin_memory().numpy().view(np.uint32),
+                       torch.zeros(nf, dtype=torch.int32).pin_memory().numpy().view(np.uint32))
+    enc.encode_stream_host(src, out=out)
+    for k in range(nf):
+        o = out.frame(k)
+        np.testing.assert_array_equal(o.final, ref[k][1], err_msg=f"frame {k} final")
+        np.testing.assert_array_equal(o.motion, ref[k][2], err_msg=f"frame {k} motion")
+        np.testing.assert_array_equal(o.unique, ref[k][3], err_msg=f"frame {k} unique")
+    enc.close()
+
+
 def test_gpu_stream_device_matches_frame_host(torch_cuda):
     """mptc_encode_stream_device (intra frames on the second lane, concurrent
     with the inter frames before them) gives the per-frame results, across
