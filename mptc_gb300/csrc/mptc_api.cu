@@ -705,9 +705,9 @@ mptc_status ring_init(mptc_ctx *ctx) {
 
 }  // namespace
 
-mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, int32_t n_frames,
-                                    const int32_t *is_intra, uint64_t *final_host, uint8_t *motion_host,
-                                    uint32_t *unique_host, uint32_t *n_unique_host, void *stream) {
+static mptc_status encode_stream_host_run(mptc_ctx *ctx, const uint8_t *frames_host, int32_t n_frames,
+                                          const int32_t *is_intra, uint64_t *final_host, uint8_t *motion_host,
+                                          uint32_t *unique_host, uint32_t *n_unique_host, void *stream) {
   if (!ctx) return MPTC_EINVAL;
   if (n_frames < 0 || (n_frames > 0 && (!frames_host || !is_intra || !final_host || !motion_host || !unique_host ||
                                         !n_unique_host)))
@@ -792,9 +792,9 @@ mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, i
   return MPTC_OK;
 }
 
-mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, int32_t n_frames,
-                                      const int32_t *is_intra, uint64_t *final_dev, uint8_t *motion_dev,
-                                      uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream) {
+static mptc_status encode_stream_device_run(mptc_ctx *ctx, const uint8_t *frames_dev, int32_t n_frames,
+                                            const int32_t *is_intra, uint64_t *final_dev, uint8_t *motion_dev,
+                                            uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream) {
   if (!ctx) return MPTC_EINVAL;
   if (n_frames < 0 || (n_frames > 0 && (!frames_dev || !is_intra || !final_dev || !motion_dev || !unique_dev ||
                                         !n_unique_dev)))
@@ -860,6 +860,32 @@ mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, 
   MPTC_CUDA(cudaStreamSynchronize(s));
   if (*h & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side dependency wait expired");
   return MPTC_OK;
+}
+
+// After a failed run, waits for every stream of the stream calls: their
+// copies and kernels may still use the caller's buffers.
+static void drain_run(mptc_ctx *ctx, void *stream) {
+  cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  for (cudaStream_t t : {ctx->lane_s, ctx->stb_s, ctx->ring.cin, ctx->ring.cout})
+    if (t) cudaStreamSynchronize(t);
+}
+
+mptc_status mptc_encode_stream_host(mptc_ctx *ctx, const uint8_t *frames_host, int32_t n_frames,
+                                    const int32_t *is_intra, uint64_t *final_host, uint8_t *motion_host,
+                                    uint32_t *unique_host, uint32_t *n_unique_host, void *stream) {
+  const mptc_status st = encode_stream_host_run(ctx, frames_host, n_frames, is_intra, final_host, motion_host,
+                                                unique_host, n_unique_host, stream);
+  if (st != MPTC_OK && ctx) drain_run(ctx, stream);
+  return st;
+}
+
+mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, int32_t n_frames,
+                                      const int32_t *is_intra, uint64_t *final_dev, uint8_t *motion_dev,
+                                      uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream) {
+  const mptc_status st = encode_stream_device_run(ctx, frames_dev, n_frames, is_intra, final_dev, motion_dev,
+                                                  unique_dev, n_unique_dev, stream);
+  if (st != MPTC_OK && ctx) drain_run(ctx, stream);
+  return st;
 }
 
 mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k) {
