@@ -159,7 +159,8 @@ def run_reference(args, rank: int) -> None:
 
 
 def workload_config() -> dict:
-    return {"workload": "1080p MPTC encode, 120-frame synthetic stream (config-1 generator at 1920x1080)",
+    return {"workload": "1080p MPTC encode, 120-frame synthetic stream (moving squares over periodic "
+                        "gradients, seeded, 1920x1080)",
             "width": W, "height": H, "frames_per_step": FRAMES, "search_area": SA,
             "err_threshold": THR, "intra_interval": II, "search": "exhaustive (bit-exact plain path)",
             "l2": "inputs larger than L2: 120 frames x 6.2 MB resident, each read once per step",
