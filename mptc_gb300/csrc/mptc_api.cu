@@ -622,29 +622,29 @@ mptc_status lane_init(mptc_ctx *ctx) {
   if (!ctx->run_status && cudaMalloc(&ctx->run_status, sizeof(uint32_t)) != cudaSuccess)
     return fail(ctx, MPTC_ENOMEM, "stream call: status word");
   if (ctx->lane_b) return MPTC_OK;
-  mptc_ctx *b = nullptr;
-  const mptc_status st = mptc_ctx_create(&ctx->cfg, ctx->width, ctx->height, &b);
-  if (st != MPTC_OK) return fail(ctx, st, "stream call: second lane context");
   // the intra lane's stream has the highest priority: its latency-bound
-  // dataflow gets SM slots ahead of the inter kernels it overlaps
+  // dataflow gets SM slots ahead of the inter kernels it overlaps. Each
+  // resource is created only if an earlier, failed call has not made it.
   int prio_low = 0, prio_high = 0;
   cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
-  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->lane_s, cudaStreamNonBlocking, prio_high);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_start, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_done, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stb_s, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !ctx->lane_s) e = cudaStreamCreateWithPriority(&ctx->lane_s, cudaStreamNonBlocking, prio_high);
+  if (e == cudaSuccess && !ctx->lane_start) e = cudaEventCreateWithFlags(&ctx->lane_start, cudaEventDisableTiming);
+  if (e == cudaSuccess && !ctx->lane_done) e = cudaEventCreateWithFlags(&ctx->lane_done, cudaEventDisableTiming);
+  if (e == cudaSuccess && !ctx->stb_s) e = cudaStreamCreateWithFlags(&ctx->stb_s, cudaStreamNonBlocking);
   const size_t n = (size_t)ctx->nblk, per = ((n * 12 + 255) & ~(size_t)255) + 256;
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->stb_mem, per * kStbRing);
+  if (e == cudaSuccess && !ctx->stb_mem) e = cudaMalloc(&ctx->stb_mem, per * kStbRing);
   for (int i = 0; i < kStbRing && e == cudaSuccess; ++i) {
     ctx->stb_slot[i] = reinterpret_cast<uint64_t *>(ctx->stb_mem + per * i);
     ctx->orig_slot[i] = reinterpret_cast<int32_t *>(ctx->stb_mem + per * i + n * 8);
-    e = cudaEventCreateWithFlags(&ctx->stb_done[i], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stb_free[i], cudaEventDisableTiming);
+    if (!ctx->stb_done[i]) e = cudaEventCreateWithFlags(&ctx->stb_done[i], cudaEventDisableTiming);
+    if (e == cudaSuccess && !ctx->stb_free[i]) e = cudaEventCreateWithFlags(&ctx->stb_free[i], cudaEventDisableTiming);
   }
-  if (e != cudaSuccess) {
-    mptc_ctx_destroy(b);
-    return fail(ctx, MPTC_ECUDA, std::string("stream call: ") + cudaGetErrorString(e));
-  }
+  if (e != cudaSuccess)
+    return fail(ctx, e == cudaErrorMemoryAllocation ? MPTC_ENOMEM : MPTC_ECUDA,
+                std::string("stream call: ") + cudaGetErrorString(e));
+  mptc_ctx *b = nullptr;
+  const mptc_status st = mptc_ctx_create(&ctx->cfg, ctx->width, ctx->height, &b);
+  if (st != MPTC_OK) return fail(ctx, st, "stream call: second lane context");
   b->timing = ctx->timing;
   // half the SMs: the overlapped inter frames keep the other half
   b->intra_cap = std::max(1, ctx->sm_count * kLaneIntraShare / 8);
@@ -677,7 +677,8 @@ mptc_status ring_init(mptc_ctx *ctx) {
   const size_t n = (size_t)ctx->nblk;
   auto up256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t per = up256(n * 48) + up256(n * 8) + up256(n * 2) + up256(n * 4) + 256;
-  cudaError_t e = cudaMalloc(&r.mem, per * kRing);
+  // each resource is created only if an earlier, failed call has not made it
+  cudaError_t e = r.mem ? cudaSuccess : cudaMalloc(&r.mem, per * kRing);
   if (e == cudaSuccess) {
     for (int i = 0; i < kRing; ++i) {
       unsigned char *q = r.mem + per * i;
@@ -692,11 +693,11 @@ mptc_status ring_init(mptc_ctx *ctx) {
       r.n_unique[i] = reinterpret_cast<uint32_t *>(q);
     }
   }
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r.cin, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r.cout, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !r.cin) e = cudaStreamCreateWithFlags(&r.cin, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !r.cout) e = cudaStreamCreateWithFlags(&r.cout, cudaStreamNonBlocking);
   for (int i = 0; i < kRing && e == cudaSuccess; ++i)
     for (cudaEvent_t *ev : {&r.up[i], &r.enc[i], &r.down[i]})
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+      if (e == cudaSuccess && !*ev) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e != cudaSuccess) return fail(ctx, e == cudaErrorMemoryAllocation ? MPTC_ENOMEM : MPTC_ECUDA,
                                     std::string("encode_stream_host: ") + cudaGetErrorString(e));
   r.ready = true;
