@@ -12,6 +12,7 @@ import ctypes
 import numpy as np
 
 from ._lib import Config, check, lib
+from .encoder import dev_ptr
 
 
 class BatchEncoder:
@@ -49,7 +50,14 @@ class BatchEncoder:
 
     def upload(self, i: int, frame, stream=None) -> None:
         """frame: (H, W, 3) uint8 numpy array or CUDA tensor."""
-        ptr = frame.data_ptr() if hasattr(frame, "data_ptr") else np.ascontiguousarray(frame).ctypes.data
+        w, h = self.sizes[i]
+        if tuple(frame.shape) != (h, w, 3):
+            raise ValueError(f"frame: shape {tuple(frame.shape)}, expected ({h}, {w}, 3)")
+        if getattr(frame, "is_cuda", False):
+            ptr = dev_ptr(frame, "frame", 1, h * w * 3)
+        else:
+            frame = np.ascontiguousarray(frame.numpy() if hasattr(frame, "numpy") else frame, dtype=np.uint8)
+            ptr = frame.ctypes.data
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
         check(lib().mptc_batch_upload(self._b, i, ptr, s))
 

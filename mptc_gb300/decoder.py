@@ -14,6 +14,7 @@ import ctypes
 import numpy as np
 
 from ._lib import MptcError, lib
+from .encoder import dev_ptr
 from .stream import StreamReader
 
 
@@ -24,8 +25,9 @@ def _stream_ptr(stream) -> ctypes.c_void_p:
 def endpoint_coefficients(width: int, height: int, blocks_dev, coeff_dev, stream=None) -> None:
     """blocks_dev: torch CUDA tensor of width/4*height/4 u64 (int64) blocks;
     coeff_dev: torch CUDA uint8 tensor of 6 * blocks bytes."""
-    rc = lib().mptc_endpoint_coefficients(width, height, blocks_dev.data_ptr(), coeff_dev.data_ptr(),
-                                          _stream_ptr(stream))
+    n = (width // 4) * (height // 4)
+    rc = lib().mptc_endpoint_coefficients(width, height, dev_ptr(blocks_dev, "blocks", 8, n),
+                                          dev_ptr(coeff_dev, "coeff", 1, 6 * n), _stream_ptr(stream))
     if rc != 0:
         raise MptcError(rc, f"endpoint_coefficients {width}x{height}")
 
@@ -56,6 +58,13 @@ class Decoder:
         after next is decoded)."""
         import torch
         n_unique = int(unique.size if isinstance(unique, np.ndarray) else unique.numel())
+        n = self.blocks
+        for name, a, want in (("motion", motion, 2 * n), ("coeff", coeff, 6 * n)):
+            size = a.size if isinstance(a, np.ndarray) else a.numel()
+            if size != want:
+                raise ValueError(f"{name}: {size} bytes given, {want} expected")
+        if n_unique > n:
+            raise ValueError(f"unique: {n_unique} entries given, at most {n} expected")
         s = stream if stream is not None else torch.cuda.current_stream()
         with torch.cuda.stream(s):  # staging copies ordered with the decode kernels
             for dst, src in ((self._motion, motion), (self._coeff, coeff)):

@@ -15,6 +15,35 @@ import numpy as np
 from ._lib import Config, FrameStats, KernelTime, check, lib
 
 
+def dev_ptr(t, name: str, itemsize: int, count: int) -> int:
+    """The device pointer of a tensor argument, after checking it: the C ABI
+    takes plain pointers and cannot see a buffer's size, so a short, strided
+    or mistyped tensor would be read or written past its end on the device.
+    Requires an integer tensor of `itemsize`-byte elements, contiguous, with
+    at least `count` elements, on a CUDA device."""
+    if t.is_floating_point() or t.is_complex() or t.element_size() != itemsize:
+        raise ValueError(f"{name}: {t.dtype} given, an integer type of {itemsize} bytes expected")
+    if not t.is_contiguous():
+        raise ValueError(f"{name}: not contiguous")
+    if t.numel() < count:
+        raise ValueError(f"{name}: {t.numel()} elements given, at least {count} expected")
+    if not t.is_cuda:
+        raise ValueError(f"{name}: not a CUDA tensor")
+    return t.data_ptr()
+
+
+def host_ptr(a: np.ndarray, name: str, dtype, count: int) -> int:
+    """The same checks for a host output array: exact dtype, C-contiguous,
+    writable, at least `count` elements."""
+    if a.dtype != np.dtype(dtype):
+        raise ValueError(f"{name}: {a.dtype} given, {np.dtype(dtype)} expected")
+    if not a.flags.c_contiguous or not a.flags.writeable:
+        raise ValueError(f"{name}: not a writable C-contiguous array")
+    if a.size < count:
+        raise ValueError(f"{name}: {a.size} elements given, at least {count} expected")
+    return a.ctypes.data
+
+
 @dataclass
 class FrameOutput:
     final: np.ndarray    # u64 per block (PhysicalDXTBlock)
@@ -67,13 +96,21 @@ class Encoder:
         return self._ctx
 
     # -- device API ---------------------------------------------------------
+    def _frame_ptrs(self, final, motion, unique, n_unique, frames: int = 1):
+        n = self.nblk
+        return (dev_ptr(final, "final", 8, frames * n), dev_ptr(motion, "motion", 1, frames * 2 * n),
+                dev_ptr(unique, "unique", 4, frames * n), dev_ptr(n_unique, "n_unique", 4, frames))
+
     def encode_frame_device(self, rgb, prev_final, stb, final, motion, unique, n_unique, stream=None):
-        """All arguments are torch CUDA tensors (prev_final may be None)."""
+        """All arguments are torch CUDA tensors (prev_final and stb may be None):
+        rgb (height, width, 3) uint8, prev_final/stb/final nblk int64, motion
+        2*nblk uint8, unique nblk int32, n_unique one int32."""
+        n = self.nblk
+        outs = self._frame_ptrs(final, motion, unique, n_unique)
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
-        check(lib().mptc_encode_frame(self._ctx, rgb.data_ptr(),
-                                      prev_final.data_ptr() if prev_final is not None else None,
-                                      stb.data_ptr() if stb is not None else None, final.data_ptr(),
-                                      motion.data_ptr(), unique.data_ptr(), n_unique.data_ptr(), s),
+        check(lib().mptc_encode_frame(self._ctx, dev_ptr(rgb, "rgb", 1, 48 * n),
+                                      dev_ptr(prev_final, "prev_final", 8, n) if prev_final is not None else None,
+                                      dev_ptr(stb, "stb", 8, n) if stb is not None else None, *outs, s),
               self._ctx)
 
     def encode_stream_device(self, frames, final, motion, unique, n_unique, is_intra=None, stream=None) -> None:
@@ -84,26 +121,31 @@ class Encoder:
         lane, concurrently with the inter frames before them. is_intra: a flag
         per frame, or None for the reference's schedule."""
         n = frames.shape[0]
+        if tuple(frames.shape[1:]) != (self.height, self.width, 3):
+            raise ValueError(f"frames: shape {tuple(frames.shape)}, expected (n, {self.height}, {self.width}, 3)")
+        src = dev_ptr(frames, "frames", 1, n * 48 * self.nblk)
+        outs = self._frame_ptrs(final, motion, unique, n_unique, n)
         flags = np.array([self._intra_flag(None if is_intra is None else is_intra[k]) for k in range(n)],
                          dtype=np.int32)
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
-        check(lib().mptc_encode_stream_device(self._ctx, frames.data_ptr(), n, flags.ctypes.data,
-                                              final.data_ptr(), motion.data_ptr(), unique.data_ptr(),
-                                              n_unique.data_ptr(), s), self._ctx)
+        check(lib().mptc_encode_stream_device(self._ctx, src, n, flags.ctypes.data, *outs, s), self._ctx)
 
     def dxt1_encode_device(self, rgb, stb, orig_err, stream=None):
+        n = self.nblk
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
-        check(lib().mptc_dxt1_encode(self._ctx, rgb.data_ptr(), stb.data_ptr(),
-                                     orig_err.data_ptr() if orig_err is not None else None, s),
+        check(lib().mptc_dxt1_encode(self._ctx, dev_ptr(rgb, "rgb", 1, 48 * n), dev_ptr(stb, "stb", 8, n),
+                                     dev_ptr(orig_err, "orig_err", 4, n) if orig_err is not None else None, s),
               self._ctx)
 
     def reencode_device(self, rgb, stb, orig_err, prev_final, final, motion, unique, n_unique,
                         stream=None):
+        n = self.nblk
+        outs = self._frame_ptrs(final, motion, unique, n_unique)
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
-        check(lib().mptc_reencode(self._ctx, rgb.data_ptr(), stb.data_ptr(), orig_err.data_ptr(),
-                                  prev_final.data_ptr() if prev_final is not None else None,
-                                  final.data_ptr(), motion.data_ptr(), unique.data_ptr(),
-                                  n_unique.data_ptr(), s), self._ctx)
+        check(lib().mptc_reencode(self._ctx, dev_ptr(rgb, "rgb", 1, 48 * n), dev_ptr(stb, "stb", 8, n),
+                                  dev_ptr(orig_err, "orig_err", 4, n),
+                                  dev_ptr(prev_final, "prev_final", 8, n) if prev_final is not None else None,
+                                  *outs, s), self._ctx)
 
     def stats(self, stream=None) -> FrameStats:
         st = FrameStats()
@@ -155,18 +197,17 @@ class Encoder:
         With pinned frames and outputs the uploads and downloads overlap the
         encode; otherwise the frames go one by one."""
         f = np.ascontiguousarray(frames, dtype=np.uint8)
-        assert f.ndim == 4 and f.shape[1:] == (self.height, self.width, 3)
-        n = f.shape[0]
+        if f.ndim != 4 or f.shape[1:] != (self.height, self.width, 3):
+            raise ValueError(f"frames: shape {f.shape}, expected (n, {self.height}, {self.width}, 3)")
+        n, nb = f.shape[0], self.nblk
+        if out is None:
+            out = StreamOutput(np.empty((n, nb), np.uint64), np.empty((n, 2 * nb), np.uint8),
+                               np.empty((n, nb), np.uint32), np.empty(n, np.uint32))
+        ptrs = (host_ptr(out.final, "final", np.uint64, n * nb), host_ptr(out.motion, "motion", np.uint8, n * 2 * nb),
+                host_ptr(out.unique, "unique", np.uint32, n * nb), host_ptr(out.n_unique, "n_unique", np.uint32, n))
         flags = np.array([self._intra_flag(None if is_intra is None else is_intra[k]) for k in range(n)],
                          dtype=np.int32)
-        if out is None:
-            out = StreamOutput(np.empty((n, self.nblk), np.uint64), np.empty((n, 2 * self.nblk), np.uint8),
-                               np.empty((n, self.nblk), np.uint32), np.empty(n, np.uint32))
-        assert out.final.shape[0] >= n and out.final.flags.c_contiguous and out.motion.flags.c_contiguous
-        assert out.unique.flags.c_contiguous and out.n_unique.flags.c_contiguous
-        check(lib().mptc_encode_stream_host(self._ctx, f.ctypes.data, n, flags.ctypes.data,
-                                            out.final.ctypes.data, out.motion.ctypes.data,
-                                            out.unique.ctypes.data, out.n_unique.ctypes.data, None),
+        check(lib().mptc_encode_stream_host(self._ctx, f.ctypes.data, n, flags.ctypes.data, *ptrs, None),
               self._ctx)
         return out
 
@@ -175,17 +216,19 @@ class Encoder:
         """One frame from host memory; successive calls form a stream. With
         is_intra=None the reference's intra-interval schedule is applied
         (frame 1 intra, then every intra_interval-th, codec/codec.cpp:1462-1469)."""
-        is_intra = self._intra_flag(is_intra)
         f = np.ascontiguousarray(frame, dtype=np.uint8)
-        assert f.shape == (self.height, self.width, 3)
+        if f.shape != (self.height, self.width, 3):
+            raise ValueError(f"frame: shape {f.shape}, expected ({self.height}, {self.width}, 3)")
+        nb = self.nblk
         if out is None:
-            out = FrameOutput(np.empty(self.nblk, np.uint64), np.empty(2 * self.nblk, np.uint8),
-                              np.empty(self.nblk, np.uint32),
-                              np.empty(self.nblk, np.uint64) if want_stb else None)
+            out = FrameOutput(np.empty(nb, np.uint64), np.empty(2 * nb, np.uint8), np.empty(nb, np.uint32),
+                              np.empty(nb, np.uint64) if want_stb else None)
+        ptrs = (host_ptr(out.final, "final", np.uint64, nb), host_ptr(out.motion, "motion", np.uint8, 2 * nb),
+                host_ptr(out.unique, "unique", np.uint32, nb))
+        stb = host_ptr(out.stb, "stb", np.uint64, nb) if out.stb is not None else None
+        is_intra = self._intra_flag(is_intra)
         nu = ctypes.c_uint32(0)
-        check(lib().mptc_encode_frame_host(self._ctx, f.ctypes.data, int(bool(is_intra)),
-                                           out.stb.ctypes.data if out.stb is not None else None,
-                                           out.final.ctypes.data, out.motion.ctypes.data,
-                                           out.unique.ctypes.data, ctypes.byref(nu), None),
+        check(lib().mptc_encode_frame_host(self._ctx, f.ctypes.data, int(bool(is_intra)), stb, *ptrs,
+                                           ctypes.byref(nu), None),
               self._ctx)
         return FrameOutput(out.final, out.motion, out.unique[: nu.value], out.stb)

@@ -14,6 +14,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from ._lib import check, lib
+from .encoder import dev_ptr
 
 LAYERS = [(64, 256), (256, 256), (256, 64), (32, 128), (128, 64)]
 
@@ -24,6 +25,16 @@ def param_slices():
         out.append(((o, o + i * n, (i, n)), (o + i * n, o + i * n + n, (n,))))
         o += i * n + n
     return out, o
+
+
+def _example_ptrs(rgb, stb, blocks, cands):
+    """Checked device pointers of a training batch: the frame's pixels and
+    stb blocks, B block indices and B x C candidate words (4-byte integers)."""
+    if cands.dim() != 2 or blocks.numel() != cands.shape[0]:
+        raise ValueError(f"blocks {tuple(blocks.shape)} and cands {tuple(cands.shape)} do not match (B, B x C)")
+    B, C = cands.shape
+    return (dev_ptr(rgb, "rgb", 1, 48), dev_ptr(stb, "stb", 8, 1), dev_ptr(blocks, "blocks", 4, B),
+            dev_ptr(cands, "cands", 4, B * C))
 
 
 class ProposalModel:
@@ -55,7 +66,8 @@ class ProposalModel:
 
     def set_params(self, p: np.ndarray) -> None:
         p = np.ascontiguousarray(p, dtype=np.float32)
-        assert p.size == self.n_params
+        if p.size != self.n_params:
+            raise ValueError(f"params: {p.size} values given, {self.n_params} expected")
         check(lib().mptc_model_set_params(self._m, p.ctypes.data))
 
     def grads(self, rgb, width, stb, blocks, cands):
@@ -63,16 +75,18 @@ class ProposalModel:
         g = np.empty(self.n_params, np.float32)
         loss = ctypes.c_float(0)
         B, C = cands.shape
-        check(lib().mptc_model_grads(self._m, rgb.data_ptr(), width, stb.data_ptr(), blocks.data_ptr(),
-                                     cands.data_ptr(), B, C, g.ctypes.data, ctypes.byref(loss), None))
+        rgb_p, stb_p, blk_p, cand_p = _example_ptrs(rgb, stb, blocks, cands)
+        check(lib().mptc_model_grads(self._m, rgb_p, width, stb_p, blk_p, cand_p, B, C, g.ctypes.data,
+                                     ctypes.byref(loss), None))
         return float(loss.value), g
 
     def train_step(self, rgb, width, stb, blocks, cands, lr=1e-3, weight_decay=1e-4, stream=None) -> float:
         loss = ctypes.c_float(0)
         B, C = cands.shape
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
-        check(lib().mptc_model_train_step(self._m, rgb.data_ptr(), width, stb.data_ptr(), blocks.data_ptr(),
-                                          cands.data_ptr(), B, C, lr, weight_decay, ctypes.byref(loss), s))
+        rgb_p, stb_p, blk_p, cand_p = _example_ptrs(rgb, stb, blocks, cands)
+        check(lib().mptc_model_train_step(self._m, rgb_p, width, stb_p, blk_p, cand_p, B, C, lr, weight_decay,
+                                          ctypes.byref(loss), s))
         return float(loss.value)
 
     def embed(self, rgb, width, stb, blocks, n_blocks, out_blocks, words=None, word_stride=1, n_words=0,

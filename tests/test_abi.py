@@ -65,3 +65,34 @@ def test_default_intra_schedule_matches_reference_loop():
         flags = [enc._intra_flag(None) for _ in range(70)]
         assert flags == bench.intra_schedule(70, interval)
         assert enc._intra_flag(True) is True and enc._intra_flag(False) is False
+
+
+def test_buffer_checks_before_the_abi():
+    """The Python wrappers check every buffer before its pointer crosses the
+    C ABI (which cannot see sizes): type, contiguity, length, then device."""
+    import numpy as np
+    import torch
+
+    from mptc_gb300.encoder import dev_ptr, host_ptr
+    with pytest.raises(ValueError, match="integer type of 4 bytes"):
+        dev_ptr(torch.zeros(8, dtype=torch.float32), "unique", 4, 8)
+    with pytest.raises(ValueError, match="integer type of 8 bytes"):
+        dev_ptr(torch.zeros(8, dtype=torch.int32), "final", 8, 8)
+    with pytest.raises(ValueError, match="not contiguous"):
+        dev_ptr(torch.zeros((8, 8), dtype=torch.int32)[:, 0], "unique", 4, 8)
+    with pytest.raises(ValueError, match="at least 9 expected"):
+        dev_ptr(torch.zeros(8, dtype=torch.int32), "unique", 4, 9)
+    with pytest.raises(ValueError, match="not a CUDA tensor"):
+        dev_ptr(torch.zeros(8, dtype=torch.int32), "unique", 4, 8)
+    a = np.zeros(8, np.uint32)
+    assert host_ptr(a, "unique", np.uint32, 8) == a.ctypes.data
+    with pytest.raises(ValueError, match="uint64 expected"):
+        host_ptr(a, "final", np.uint64, 4)
+    with pytest.raises(ValueError, match="at least 9 expected"):
+        host_ptr(a, "unique", np.uint32, 9)
+    with pytest.raises(ValueError, match="C-contiguous"):
+        host_ptr(np.zeros((8, 8), np.uint32)[:, 0], "unique", np.uint32, 8)
+    ro = np.zeros(8, np.uint32)
+    ro.flags.writeable = False
+    with pytest.raises(ValueError, match="C-contiguous"):
+        host_ptr(ro, "unique", np.uint32, 8)

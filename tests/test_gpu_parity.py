@@ -267,6 +267,10 @@ def test_gpu_rejects_bad_arguments(torch_cuda):
             torch.zeros((2, 64), dtype=torch.int32, device="cuda"), torch.zeros(2, dtype=torch.int32, device="cuda"))
     with pytest.raises(MptcError):
         enc.encode_stream_device(z, *outs, is_intra=[False, True])
+    with pytest.raises(ValueError):  # one frame's final blocks for a run of two
+        enc.encode_stream_device(z, outs[0][:1], *outs[1:], is_intra=[True, False])
+    with pytest.raises(ValueError):  # 4-byte words where the final blocks are 8
+        enc.encode_stream_device(z, outs[2], outs[1], outs[2], outs[3], is_intra=[True, False])
     enc.encode_stream_device(z[:0], *(o[:0] for o in outs), is_intra=[])  # an empty run does nothing
     enc.encode_stream_device(z, *outs, is_intra=[True, False])
     assert (outs[0].cpu().numpy() != 0).any()
