@@ -38,7 +38,9 @@ extern "C" {
 typedef struct mptc_stream_writer mptc_stream_writer;
 
 /* `total_frames` is the number of frames the caller will add (it fixes the
- * header's group count, codec/codec.cpp:1357). */
+ * header's group count, codec/codec.cpp:1357). Frames are at most 2^30
+ * pixels. If host memory runs out while a frame is added, the call returns
+ * MPTC_ENOMEM and every later add or finish call MPTC_ESTATE. */
 mptc_status mptc_stream_writer_create(int32_t width, int32_t height, int32_t search_area,
                                       int32_t unique_interval, int32_t total_frames,
                                       mptc_stream_writer **out_writer);

@@ -58,7 +58,7 @@ mptc_status mptc_stream_reader_open(const uint8_t *data, uint64_t size, mptc_str
   in.max_compressed_ep_y = get_u32(data + 26);
   in.max_compressed_ep_c = get_u32(data + 30);
   if (in.width <= 0 || in.height <= 0 || in.width % 256 || in.height % 256 || in.unique_interval < 1 ||
-      in.search_area < 1 || in.search_area > 63)
+      in.search_area < 1 || in.search_area > 63 || (int64_t)in.width * in.height > (int64_t)1 << 30)
     return MPTC_EINVAL;
   in.frames = in.groups * (uint32_t)in.unique_interval;
   mptc_stream_reader *r = new (std::nothrow) mptc_stream_reader();
@@ -98,7 +98,11 @@ mptc_status mptc_stream_reader_next(mptc_stream_reader *r, uint8_t *motion, uint
     const uint8_t *pc;
     if (!r->take_u32(&psz) || !r->take(psz, &pc) || !r->take_u32(&count)) return MPTC_EINVAL;
     if (count > 4 * n * (size_t)r->info.unique_interval) return MPTC_EINVAL;
-    r->palette.assign(count, 0);
+    try {
+      r->palette.assign(count, 0);
+    } catch (...) {
+      return MPTC_ENOMEM;
+    }
     if (!mptc_host::decode_bytes(pc, psz, r->palette.data(), count)) return MPTC_EINVAL;
     r->palette_used = 0;
   }
@@ -113,15 +117,20 @@ mptc_status mptc_stream_reader_next(mptc_stream_reader *r, uint8_t *motion, uint
   uint8_t *dst[5] = {motion, coeff, coeff + n, coeff + 3 * n, coeff + 4 * n};
   const size_t len[5] = {2 * n, n, 2 * n, n, 2 * n};
   bool ok[5];
+  // parts 1..4 on threads when the frame is large (parts whose thread could
+  // not be started decode here), part 0 on this thread
+  std::thread t[4];
+  int started = 0;
   if (n >= kParallelBlocks) {
-    std::thread t[4];
-    for (int k = 1; k < 5; ++k)
-      t[k - 1] = std::thread([&, k] { ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]); });
-    ok[0] = mptc_host::decode_bytes(code[0], csz[0], dst[0], len[0]);
-    for (auto &th : t) th.join();
-  } else {
-    for (int k = 0; k < 5; ++k) ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]);
+    try {
+      for (int k = 1; k < 5; ++k, ++started)
+        t[k - 1] = std::thread([&, k] { ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]); });
+    } catch (...) {
+    }
   }
+  for (int k = 1 + started; k < 5; ++k) ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]);
+  ok[0] = mptc_host::decode_bytes(code[0], csz[0], dst[0], len[0]);
+  for (int i = 0; i < started; ++i) t[i].join();
   for (bool b : ok)
     if (!b) return MPTC_EINVAL;
   std::memcpy(unique, r->palette.data() + r->palette_used, 4 * (size_t)nu);

@@ -97,6 +97,7 @@ struct mptc_stream_writer {
   uint32_t group_frames = 0;
   uint32_t max_unique = 0, max_palette = 0, max_motion = 0, max_ep_y = 0, max_ep_c = 0;
   uint32_t last_motion = 0, last_ep[4] = {0, 0, 0, 0};
+  bool failed = false;  // an allocation failed part way through a frame: the stream is unusable
 };
 
 namespace {
@@ -137,14 +138,34 @@ void append_frame(mptc_stream_writer *w, const uint8_t *coeff, const uint8_t *mo
   const uint8_t *src[5] = {motion, coeff, coeff + n, coeff + 3 * n, coeff + 4 * n};
   const size_t len[5] = {2 * n, n, 2 * n, n, 2 * n};
   std::vector<uint8_t> z[5];
+  // parts 1..4 on threads when the frame is large (parts whose thread could
+  // not be started code here), part 0 on this thread; an allocation failure
+  // on a thread is reported after the join
+  std::thread t[4];
+  bool thread_ok[5] = {true, true, true, true, true};
+  int started = 0;
   if (n >= kParallelBlocks) {
-    std::thread t[4];
-    for (int k = 1; k < 5; ++k) t[k - 1] = std::thread([&, k] { z[k] = code_bytes(src[k], len[k]); });
-    z[0] = code_bytes(src[0], len[0]);
-    for (auto &th : t) th.join();
-  } else {
-    for (int k = 0; k < 5; ++k) z[k] = code_bytes(src[k], len[k]);
+    try {
+      for (int k = 1; k < 5; ++k, ++started)
+        t[k - 1] = std::thread([&, k] {
+          try {
+            z[k] = code_bytes(src[k], len[k]);
+          } catch (...) {
+            thread_ok[k] = false;
+          }
+        });
+    } catch (...) {
+    }
   }
+  try {
+    for (int k = 1 + started; k < 5; ++k) z[k] = code_bytes(src[k], len[k]);
+    z[0] = code_bytes(src[0], len[0]);
+  } catch (...) {
+    thread_ok[0] = false;
+  }
+  for (int i = 0; i < started; ++i) t[i].join();
+  for (bool b : thread_ok)
+    if (!b) throw std::bad_alloc();
   std::vector<uint8_t> &rec = w->group_records;
   put_u32(rec, n_unique);
   for (int k = 0; k < 5; ++k) {
@@ -181,7 +202,8 @@ extern "C" {
 mptc_status mptc_stream_writer_create(int32_t width, int32_t height, int32_t search_area, int32_t unique_interval,
                                       int32_t total_frames, mptc_stream_writer **out) {
   if (!out || width <= 0 || height <= 0 || (width % 256) || (height % 256) || unique_interval <= 0 ||
-      unique_interval > 255 || total_frames < 0 || search_area < 1 || search_area > 63)
+      unique_interval > 255 || total_frames < 0 || search_area < 1 || search_area > 63 ||
+      (int64_t)width * height > (int64_t)1 << 30)
     return MPTC_EINVAL;
   mptc_stream_writer *w = new (std::nothrow) mptc_stream_writer();
   if (!w) return MPTC_ENOMEM;
@@ -193,12 +215,17 @@ mptc_status mptc_stream_writer_create(int32_t width, int32_t height, int32_t sea
   w->unique_interval = unique_interval;
   w->total_frames = total_frames;
   // header, codec/codec.cpp:1354-1367; the five maxima are patched at the end
-  put_u32(w->stream, (uint32_t)height);
-  put_u32(w->stream, (uint32_t)width);
-  w->stream.push_back((uint8_t)unique_interval);
-  w->stream.push_back((uint8_t)search_area);
-  put_u32(w->stream, (uint32_t)(total_frames / unique_interval));
-  for (int k = 0; k < 5; ++k) put_u32(w->stream, 0);
+  try {
+    put_u32(w->stream, (uint32_t)height);
+    put_u32(w->stream, (uint32_t)width);
+    w->stream.push_back((uint8_t)unique_interval);
+    w->stream.push_back((uint8_t)search_area);
+    put_u32(w->stream, (uint32_t)(total_frames / unique_interval));
+    for (int k = 0; k < 5; ++k) put_u32(w->stream, 0);
+  } catch (...) {
+    delete w;
+    return MPTC_ENOMEM;
+  }
   *out = w;
   return MPTC_OK;
 }
@@ -213,8 +240,14 @@ mptc_status mptc_stream_writer_add_frame(mptc_stream_writer *w, const uint64_t *
                                          const uint32_t *unique, uint32_t n_unique) {
   if (!w || !blocks || !motion || (n_unique && !unique)) return MPTC_EINVAL;
   if (n_unique > (size_t)w->bw * w->bh) return MPTC_EINVAL;
-  const std::vector<uint8_t> coeff = endpoint_coefficients(blocks, w->bw, w->bh);
-  append_frame(w, coeff.data(), motion, unique, n_unique);
+  if (w->failed) return MPTC_ESTATE;
+  try {
+    const std::vector<uint8_t> coeff = endpoint_coefficients(blocks, w->bw, w->bh);
+    append_frame(w, coeff.data(), motion, unique, n_unique);
+  } catch (...) {
+    w->failed = true;
+    return MPTC_ENOMEM;
+  }
   return MPTC_OK;
 }
 
@@ -223,12 +256,19 @@ mptc_status mptc_stream_writer_add_frame_coefficients(mptc_stream_writer *w, con
                                                       uint32_t n_unique) {
   if (!w || !coeff || !motion || (n_unique && !unique)) return MPTC_EINVAL;
   if (n_unique > (size_t)w->bw * w->bh) return MPTC_EINVAL;
-  append_frame(w, coeff, motion, unique, n_unique);
+  if (w->failed) return MPTC_ESTATE;
+  try {
+    append_frame(w, coeff, motion, unique, n_unique);
+  } catch (...) {
+    w->failed = true;
+    return MPTC_ENOMEM;
+  }
   return MPTC_OK;
 }
 
 mptc_status mptc_stream_writer_finish(mptc_stream_writer *w, uint8_t *out, uint64_t *size) {
   if (!w || !size) return MPTC_EINVAL;
+  if (w->failed) return MPTC_ESTATE;
   // the five maxima at byte 14 (codec/codec.cpp:1514-1520)
   const uint32_t mx[5] = {w->max_unique, w->max_palette, w->max_motion, w->max_ep_y, w->max_ep_c};
   for (int k = 0; k < 5; ++k)

@@ -91,7 +91,8 @@ def test_constant_input_codes_small_and_deterministic():
 
 @pytest.mark.parametrize("w,h,sa,ui,n", [(255, 256, 8, 1, 1), (256, 320, 8, 1, 1), (256, 256, 0, 1, 1),
                                           (256, 256, 64, 1, 1), (256, 256, 8, 0, 1),
-                                          (256, 256, 8, 256, 1), (256, 256, 8, 1, -1)])
+                                          (256, 256, 8, 256, 1), (256, 256, 8, 1, -1),
+                                          (32768, 65536, 8, 1, 1)])  # above 2^30 pixels
 def test_writer_rejects_bad_parameters(w, h, sa, ui, n):
     with pytest.raises(MptcError):
         StreamWriter(w, h, sa, ui, n)
@@ -157,6 +158,10 @@ def test_reader_rejects_truncated_and_bad_streams():
     bad[9] = 0  # search area 0
     with pytest.raises(MptcError):
         StreamReader(bytes(bad))
+    huge = bytearray(data)
+    huge[0:8] = (65536).to_bytes(4, "little") + (32768).to_bytes(4, "little")  # 2^31 pixels
+    with pytest.raises(MptcError):
+        StreamReader(bytes(huge))
     rd = StreamReader(data[: len(data) // 2])
     with pytest.raises(MptcError):
         for _ in rd:
