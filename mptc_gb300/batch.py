@@ -11,8 +11,7 @@ import ctypes
 
 import numpy as np
 
-from ._lib import Config, check, lib
-from .encoder import dev_ptr
+from ._lib import Config, check, dev_ptr, lib
 
 
 class BatchEncoder:

@@ -13,8 +13,7 @@ import ctypes
 
 import numpy as np
 
-from ._lib import MptcError, lib
-from .encoder import dev_ptr
+from ._lib import MptcError, dev_ptr, lib
 from .stream import StreamReader
 
 

@@ -12,36 +12,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import Config, FrameStats, KernelTime, check, lib
-
-
-def dev_ptr(t, name: str, itemsize: int, count: int) -> int:
-    """The device pointer of a tensor argument, after checking it: the C ABI
-    takes plain pointers and cannot see a buffer's size, so a short, strided
-    or mistyped tensor would be read or written past its end on the device.
-    Requires an integer tensor of `itemsize`-byte elements, contiguous, with
-    at least `count` elements, on a CUDA device."""
-    if t.is_floating_point() or t.is_complex() or t.element_size() != itemsize:
-        raise ValueError(f"{name}: {t.dtype} given, an integer type of {itemsize} bytes expected")
-    if not t.is_contiguous():
-        raise ValueError(f"{name}: not contiguous")
-    if t.numel() < count:
-        raise ValueError(f"{name}: {t.numel()} elements given, at least {count} expected")
-    if not t.is_cuda:
-        raise ValueError(f"{name}: not a CUDA tensor")
-    return t.data_ptr()
-
-
-def host_ptr(a: np.ndarray, name: str, dtype, count: int) -> int:
-    """The same checks for a host output array: exact dtype, C-contiguous,
-    writable, at least `count` elements."""
-    if a.dtype != np.dtype(dtype):
-        raise ValueError(f"{name}: {a.dtype} given, {np.dtype(dtype)} expected")
-    if not a.flags.c_contiguous or not a.flags.writeable:
-        raise ValueError(f"{name}: not a writable C-contiguous array")
-    if a.size < count:
-        raise ValueError(f"{name}: {a.size} elements given, at least {count} expected")
-    return a.ctypes.data
+from ._lib import Config, FrameStats, KernelTime, check, dev_ptr, host_ptr, lib
 
 
 @dataclass

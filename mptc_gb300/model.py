@@ -13,8 +13,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import check, lib
-from .encoder import dev_ptr
+from ._lib import check, dev_ptr, lib
 
 LAYERS = [(64, 256), (256, 256), (256, 64), (32, 128), (128, 64)]
 

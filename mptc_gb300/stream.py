@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from ._lib import MptcError
+from ._lib import MptcError, host_ptr
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 HOST_LIB_PATH = os.path.join(_HERE, "libmptc_host.so")
@@ -165,9 +165,10 @@ class StreamReader:
         motion = np.empty(2 * n, np.uint8) if motion is None else motion
         coeff = np.empty(6 * n, np.uint8) if coeff is None else coeff
         unique = np.empty(n, np.uint32) if unique is None else unique
+        ptrs = (host_ptr(motion, "motion", np.uint8, 2 * n), host_ptr(coeff, "coeff", np.uint8, 6 * n),
+                host_ptr(unique, "unique", np.uint32, n))
         nu = ctypes.c_uint32()
-        rc = host_lib().mptc_stream_reader_next(self._h, motion.ctypes.data, coeff.ctypes.data,
-                                                unique.ctypes.data, ctypes.byref(nu))
+        rc = host_lib().mptc_stream_reader_next(self._h, *ptrs, ctypes.byref(nu))
         if rc == 5:  # MPTC_ESTATE: no frames left
             return None
         _check(rc, "stream frame")

@@ -73,7 +73,7 @@ def test_buffer_checks_before_the_abi():
     import numpy as np
     import torch
 
-    from mptc_gb300.encoder import dev_ptr, host_ptr
+    from mptc_gb300._lib import dev_ptr, host_ptr
     with pytest.raises(ValueError, match="integer type of 4 bytes"):
         dev_ptr(torch.zeros(8, dtype=torch.float32), "unique", 4, 8)
     with pytest.raises(ValueError, match="integer type of 8 bytes"):
