@@ -96,3 +96,17 @@ def test_buffer_checks_before_the_abi():
     ro.flags.writeable = False
     with pytest.raises(ValueError, match="C-contiguous"):
         host_ptr(ro, "unique", np.uint32, 8)
+
+
+def test_product_path_never_reaches_the_oracle():
+    """The package (Python bindings, CUDA sources, host C++) and the public
+    headers name nothing under oracle/: the oracle is test infrastructure, and
+    the product path has no CPU fallback through it."""
+    pkg = os.path.join(ROOT, "mptc_gb300")
+    files = [os.path.join(d, f) for d, _, fs in os.walk(pkg) for f in fs
+             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp", ".c")) and "__pycache__" not in d]
+    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    assert len(files) > 20
+    for path in files:
+        text = open(path, encoding="utf-8").read()
+        assert not re.search(r"\boracle\b|mptc_oracle|libmptc_oracle", text), path
