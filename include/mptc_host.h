@@ -89,7 +89,7 @@ typedef struct mptc_stream_info {
 typedef struct mptc_stream_reader mptc_stream_reader;
 
 /* Copies `size` bytes of stream; checks the header (sizes multiples of 256
- * pixels, search area 1..63, unique interval >= 1). */
+ * pixels, at most 2^30 pixels, search area 1..63, unique interval >= 1). */
 mptc_status mptc_stream_reader_open(const uint8_t *data, uint64_t size, mptc_stream_reader **out_reader);
 mptc_status mptc_stream_reader_destroy(mptc_stream_reader *reader);
 mptc_status mptc_stream_reader_info(const mptc_stream_reader *reader, mptc_stream_info *info);
