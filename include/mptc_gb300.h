@@ -13,7 +13,10 @@
  * `_dev` pointers are device memory, `_host` pointers host memory; `stream` is
  * a cudaStream_t passed as void* (NULL = legacy default stream). Frame width
  * and height must be multiples of 4 (the reference reads past the frame
- * otherwise, codec/dxt_image.cpp:128-139).
+ * otherwise, codec/dxt_image.cpp:128-139). A context, batch, model or decoder
+ * is used by one host thread at a time; separate ones may be used from
+ * separate threads at once (the shared per-device tables are uploaded under a
+ * lock), except mptc_encode_frame_noalloc, whose calls share one scratch area.
  *
  * Layouts (little-endian, raster order of 4x4 blocks, blocks_wide = width/4):
  *   block  u64 = ep1 | ep2 << 16 | interp << 32   (PhysicalDXTBlock, dxt_image.h:16-23)
