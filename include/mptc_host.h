@@ -60,6 +60,22 @@ mptc_status mptc_stream_writer_add_frame_coefficients(mptc_stream_writer *writer
                                                       const uint8_t *motion, const uint32_t *unique_palette,
                                                       uint32_t n_unique);
 
+/* A run of frames in one call, in the layout of mptc_encode_stream_host's
+ * outputs: frame f's blocks at final_blocks + f * blocks, its motion codes at
+ * motion + 2 * f * blocks, its palette at unique_palette + f * blocks with
+ * n_unique[f] entries. The frames' endpoint transforms and coded parts are
+ * computed on all the host's cores and appended in frame order: the bytes are
+ * those of n_frames mptc_stream_writer_add_frame calls. */
+mptc_status mptc_stream_writer_add_frames(mptc_stream_writer *writer, int32_t n_frames,
+                                          const uint64_t *final_blocks, const uint8_t *motion,
+                                          const uint32_t *unique_palette, const uint32_t *n_unique);
+
+/* The same with the endpoint images already transformed: frame f's six
+ * coefficient planes at coeff + 6 * f * blocks. */
+mptc_status mptc_stream_writer_add_frames_coefficients(mptc_stream_writer *writer, int32_t n_frames,
+                                                       const uint8_t *coeff, const uint8_t *motion,
+                                                       const uint32_t *unique_palette, const uint32_t *n_unique);
+
 /* Finishes the stream: *size receives its byte count; if `out` is not NULL
  * (room for *size bytes when called with out == NULL first) the bytes are
  * copied there. */

@@ -6,8 +6,11 @@
 #include "arith_coder.h"
 
 #include <algorithm>
+#include <array>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <thread>
 #include <vector>
@@ -128,44 +131,47 @@ std::vector<uint8_t> endpoint_coefficients(const uint64_t *blocks, int bw, int b
   return out;
 }
 
-// Codes one frame's parts and appends its record to the open group; closes
-// the group after unique_interval frames (codec/codec.cpp:1115-1158, :1471-1505).
-// The five parts (motion codes, Y1, Co1|Cg1, Y2, Co2|Cg2) use independent
-// coders and are coded concurrently on large frames.
-void append_frame(mptc_stream_writer *w, const uint8_t *coeff, const uint8_t *motion, const uint32_t *unique,
-                  uint32_t n_unique) {
-  const size_t n = (size_t)w->bw * w->bh;
+// Runs job(i) for i in [0, count) on up to `threads` threads, the calling
+// thread included (jobs of threads that could not be started run on the
+// others). Returns false if a job threw (an allocation failed).
+bool parallel_for(size_t count, size_t threads, const std::function<void(size_t)> &job) {
+  std::atomic<size_t> next{0};
+  std::atomic<bool> ok{true};
+  auto worker = [&] {
+    for (size_t i; (i = next.fetch_add(1)) < count;) {
+      try {
+        job(i);
+      } catch (...) {
+        ok = false;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  const size_t extra = std::min(threads, count) > 1 ? std::min(threads, count) - 1 : 0;
+  try {
+    pool.reserve(extra);
+    for (size_t t = 0; t < extra; ++t) pool.emplace_back(worker);
+  } catch (...) {
+  }
+  worker();
+  for (std::thread &t : pool) t.join();
+  return ok;
+}
+
+// The five independently coded parts of a frame record: motion codes, Y1,
+// Co1|Cg1, Y2, Co2|Cg2 (codec/codec.cpp:1140-1155, :860-899). Each part has
+// its own coder and model, so parts and frames code independently.
+using FrameCode = std::array<std::vector<uint8_t>, 5>;
+
+std::vector<uint8_t> code_part(const uint8_t *coeff, const uint8_t *motion, size_t n, int k) {
   const uint8_t *src[5] = {motion, coeff, coeff + n, coeff + 3 * n, coeff + 4 * n};
   const size_t len[5] = {2 * n, n, 2 * n, n, 2 * n};
-  std::vector<uint8_t> z[5];
-  // parts 1..4 on threads when the frame is large (parts whose thread could
-  // not be started code here), part 0 on this thread; an allocation failure
-  // on a thread is reported after the join
-  std::thread t[4];
-  bool thread_ok[5] = {true, true, true, true, true};
-  int started = 0;
-  if (n >= kParallelBlocks) {
-    try {
-      for (int k = 1; k < 5; ++k, ++started)
-        t[k - 1] = std::thread([&, k] {
-          try {
-            z[k] = code_bytes(src[k], len[k]);
-          } catch (...) {
-            thread_ok[k] = false;
-          }
-        });
-    } catch (...) {
-    }
-  }
-  try {
-    for (int k = 1 + started; k < 5; ++k) z[k] = code_bytes(src[k], len[k]);
-    z[0] = code_bytes(src[0], len[0]);
-  } catch (...) {
-    thread_ok[0] = false;
-  }
-  for (int i = 0; i < started; ++i) t[i].join();
-  for (bool b : thread_ok)
-    if (!b) throw std::bad_alloc();
+  return code_bytes(src[k], len[k]);
+}
+
+// Appends a coded frame's record to the open group and closes the group after
+// unique_interval frames (codec/codec.cpp:1115-1158, :1471-1505).
+void append_record(mptc_stream_writer *w, const FrameCode &z, const uint32_t *unique, uint32_t n_unique) {
   std::vector<uint8_t> &rec = w->group_records;
   put_u32(rec, n_unique);
   for (int k = 0; k < 5; ++k) {
@@ -192,6 +198,46 @@ void append_frame(mptc_stream_writer *w, const uint8_t *coeff, const uint8_t *mo
     w->group_records.clear();
     w->group_palette.clear();
     w->group_frames = 0;
+  }
+}
+
+size_t host_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
+
+// One frame: its five parts concurrently when the frame is large.
+void append_frame(mptc_stream_writer *w, const uint8_t *coeff, const uint8_t *motion, const uint32_t *unique,
+                  uint32_t n_unique) {
+  const size_t n = (size_t)w->bw * w->bh;
+  FrameCode z;
+  if (!parallel_for(5, n >= kParallelBlocks ? 5 : 1, [&](size_t k) { z[k] = code_part(coeff, motion, n, (int)k); }))
+    throw std::bad_alloc();
+  append_record(w, z, unique, n_unique);
+}
+
+// A run of frames (frame f's arrays at blocks + f n, coeff + 6 f n, motion +
+// 2 f n, unique + f n): chunks of frames whose endpoint transforms (when
+// `blocks` is given) and parts are coded by all the host's cores, then
+// appended in frame order, so the bytes are those of frame-by-frame calls.
+void append_frames(mptc_stream_writer *w, size_t n_frames, const uint64_t *blocks, const uint8_t *coeff,
+                   const uint8_t *motion, const uint32_t *unique, const uint32_t *n_unique) {
+  const size_t n = (size_t)w->bw * w->bh, threads = host_threads(), chunk = 2 * threads;
+  std::vector<std::vector<uint8_t>> cf;
+  std::vector<FrameCode> z;
+  for (size_t f0 = 0; f0 < n_frames; f0 += chunk) {
+    const size_t m = std::min(chunk, n_frames - f0);
+    if (blocks) {
+      cf.assign(m, {});
+      if (!parallel_for(m, threads, [&](size_t i) { cf[i] = endpoint_coefficients(blocks + (f0 + i) * n, w->bw, w->bh); }))
+        throw std::bad_alloc();
+    }
+    z.assign(m, FrameCode{});
+    if (!parallel_for(5 * m, threads, [&](size_t j) {
+          const size_t i = j / 5;
+          const uint8_t *c = blocks ? cf[i].data() : coeff + (f0 + i) * 6 * n;
+          z[i][j % 5] = code_part(c, motion + (f0 + i) * 2 * n, n, (int)(j % 5));
+        }))
+      throw std::bad_alloc();
+    for (size_t i = 0; i < m; ++i)
+      append_record(w, z[i], n_unique[f0 + i] ? unique + (f0 + i) * n : nullptr, n_unique[f0 + i]);
   }
 }
 
@@ -264,6 +310,35 @@ mptc_status mptc_stream_writer_add_frame_coefficients(mptc_stream_writer *w, con
     return MPTC_ENOMEM;
   }
   return MPTC_OK;
+}
+
+// Shared checks and error handling of the two run calls.
+static mptc_status add_frames(mptc_stream_writer *w, int32_t n_frames, const uint64_t *blocks, const uint8_t *coeff,
+                              const uint8_t *motion, const uint32_t *unique, const uint32_t *n_unique) {
+  if (!w || n_frames < 0 || (n_frames > 0 && ((!blocks && !coeff) || !motion || !n_unique))) return MPTC_EINVAL;
+  const size_t n = (size_t)w->bw * w->bh;
+  for (int32_t f = 0; f < n_frames; ++f)
+    if (n_unique[f] > n || (n_unique[f] && !unique)) return MPTC_EINVAL;
+  if (w->failed) return MPTC_ESTATE;
+  try {
+    append_frames(w, (size_t)n_frames, blocks, coeff, motion, unique, n_unique);
+  } catch (...) {
+    w->failed = true;
+    return MPTC_ENOMEM;
+  }
+  return MPTC_OK;
+}
+
+mptc_status mptc_stream_writer_add_frames(mptc_stream_writer *w, int32_t n_frames, const uint64_t *blocks,
+                                          const uint8_t *motion, const uint32_t *unique, const uint32_t *n_unique) {
+  return add_frames(w, n_frames, blocks, nullptr, motion, unique, n_unique);
+}
+
+mptc_status mptc_stream_writer_add_frames_coefficients(mptc_stream_writer *w, int32_t n_frames,
+                                                       const uint8_t *coeff, const uint8_t *motion,
+                                                       const uint32_t *unique, const uint32_t *n_unique) {
+  if (!coeff && n_frames > 0) return MPTC_EINVAL;
+  return add_frames(w, n_frames, nullptr, coeff, motion, unique, n_unique);
 }
 
 mptc_status mptc_stream_writer_finish(mptc_stream_writer *w, uint8_t *out, uint64_t *size) {

@@ -22,7 +22,8 @@ HOST_LIB_PATH = os.path.join(_HERE, "libmptc_host.so")
 
 HOST_EXPORTED = [
     "mptc_stream_writer_create", "mptc_stream_writer_destroy", "mptc_stream_writer_add_frame",
-    "mptc_stream_writer_add_frame_coefficients", "mptc_stream_writer_finish",
+    "mptc_stream_writer_add_frame_coefficients", "mptc_stream_writer_add_frames",
+    "mptc_stream_writer_add_frames_coefficients", "mptc_stream_writer_finish",
     "mptc_stream_writer_frame_sizes", "mptc_stream_reader_open", "mptc_stream_reader_destroy",
     "mptc_stream_reader_info", "mptc_stream_reader_next",
 ]
@@ -53,6 +54,8 @@ def host_lib() -> ctypes.CDLL:
         L.mptc_stream_writer_finish.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_uint64)]
         L.mptc_stream_writer_frame_sizes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), vp]
         L.mptc_stream_writer_add_frame_coefficients.argtypes = [vp, vp, vp, vp, ctypes.c_uint32]
+        L.mptc_stream_writer_add_frames.argtypes = [vp, i32, vp, vp, vp, vp]
+        L.mptc_stream_writer_add_frames_coefficients.argtypes = [vp, i32, vp, vp, vp, vp]
         L.mptc_stream_reader_open.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(vp)]
         L.mptc_stream_reader_destroy.argtypes = [vp]
         L.mptc_stream_reader_info.argtypes = [vp, ctypes.POINTER(StreamInfo)]
@@ -101,6 +104,30 @@ class StreamWriter:
             self._h, coeff.ctypes.data, motion.ctypes.data, unique.ctypes.data if unique.size else None,
             unique.size), "add_frame_coefficients")
 
+    def add_frames(self, final: np.ndarray, motion: np.ndarray, unique: np.ndarray, n_unique: np.ndarray,
+                   coefficients: bool = False) -> None:
+        """A run of F frames in one call, coded on all host cores: final (F,
+        blocks) u64 (or, with coefficients=True, (F, 6 * blocks) u8 coefficient
+        planes), motion (F, 2 * blocks) u8, unique (F, blocks) u32 with frame
+        f's palette in unique[f, :n_unique[f]], n_unique (F,) u32 — the
+        layout of Encoder.encode_stream_host's StreamOutput."""
+        f = int(np.shape(n_unique)[0])
+        n = self.blocks
+        nu = np.ascontiguousarray(n_unique, dtype=np.uint32).reshape(-1)
+        if coefficients:
+            src = np.ascontiguousarray(final, dtype=np.uint8)
+            src_ptr = host_ptr(src.reshape(-1), "coeff", np.uint8, 6 * n * f)
+        else:
+            src = np.ascontiguousarray(final, dtype=np.uint64)
+            src_ptr = host_ptr(src.reshape(-1), "final", np.uint64, n * f)
+        mot = np.ascontiguousarray(motion, dtype=np.uint8)
+        uni = np.ascontiguousarray(unique, dtype=np.uint32)
+        ptrs = (host_ptr(mot.reshape(-1), "motion", np.uint8, 2 * n * f),
+                host_ptr(uni.reshape(-1), "unique", np.uint32, n * f), nu.ctypes.data)
+        call = (host_lib().mptc_stream_writer_add_frames_coefficients if coefficients
+                else host_lib().mptc_stream_writer_add_frames)
+        _check(call(self._h, f, src_ptr, *ptrs), "add_frames")
+
     def frame_sizes(self) -> tuple[int, list[int]]:
         """(motion bytes, [Y1, C1, Y2, C2] endpoint bytes) of the last frame."""
         mb = ctypes.c_uint32()
@@ -130,15 +157,22 @@ class StreamWriter:
 
 def write_stream(frames, width: int, height: int, search_area: int, unique_interval: int) -> bytes:
     """Stream bytes of encoded frames: each item has ``final``, ``motion`` and
-    ``unique`` arrays (or is a (final, motion, unique) tuple)."""
-    frames = list(frames)
+    ``unique`` arrays (or is a (final, motion, unique) tuple). The frames are
+    coded in one add_frames call (all host cores)."""
+    frames = [f if isinstance(f, tuple) else (f.final, f.motion, f.unique) for f in frames]
     w = StreamWriter(width, height, search_area, unique_interval, len(frames))
     try:
-        for f in frames:
-            if isinstance(f, tuple):
-                w.add_frame(*f)
-            else:
-                w.add_frame(f.final, f.motion, f.unique)
+        if frames:
+            n = w.blocks
+            final = np.stack([np.asarray(f[0], np.uint64).reshape(-1) for f in frames])
+            motion = np.stack([np.asarray(f[1], np.uint8).reshape(-1) for f in frames])
+            n_unique = np.array([np.size(f[2]) for f in frames], np.uint32)
+            if final.shape[1] != n or motion.shape[1] != 2 * n or (n_unique > n).any():
+                raise ValueError(f"frame arrays do not match {n} blocks")
+            unique = np.zeros((len(frames), n), np.uint32)
+            for k, f in enumerate(frames):
+                unique[k, : n_unique[k]] = np.asarray(f[2], np.uint32).reshape(-1)
+            w.add_frames(final, motion, unique, n_unique)
         return w.finish()
     finally:
         w.close()

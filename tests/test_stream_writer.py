@@ -195,3 +195,52 @@ def test_arithmetic_coder_round_trip_on_skewed_and_uniform_bytes():
         np.testing.assert_array_equal(c, c2)
         np.testing.assert_array_equal(u, u2)
     rd.close()
+
+
+def test_add_frames_matches_frame_by_frame_and_coefficients():
+    """One add_frames call (frames coded on all host cores) writes the bytes of
+    frame-by-frame add_frame calls, including a trailing partial group; the
+    coefficient form, fed the planes the reader decodes, writes them again."""
+    from mptc_gb300.stream import StreamReader
+    w_, h_, nf, ui = 256, 512, 7, 3
+    frames = StreamSpec(w_, h_, nf, seed=77, n_squares=3, square_size=48).generate()
+    res = oracle.encode_stream(frames, 6, 5, 4, threads=os.cpu_count() or 1, want_psnr=False)
+    one = StreamWriter(w_, h_, 6, ui, nf)
+    for r in res:
+        one.add_frame(r.final, r.motion, r.unique)
+    ref = one.finish()
+    one.close()
+    n = (w_ // 4) * (h_ // 4)
+    fin = np.stack([r.final for r in res])
+    mot = np.stack([r.motion for r in res])
+    nu = np.array([len(r.unique) for r in res], np.uint32)
+    uni = np.zeros((nf, n), np.uint32)
+    for k, r in enumerate(res):
+        uni[k, : nu[k]] = r.unique
+    run = StreamWriter(w_, h_, 6, ui, nf)
+    run.add_frames(fin[:2], mot[:2], uni[:2], nu[:2])  # two calls: the group spans them
+    run.add_frames(fin[2:], mot[2:], uni[2:], nu[2:])
+    assert run.finish() == ref
+    run.close()
+    parts = list(StreamReader(ref))
+    assert len(parts) == 6  # the trailing partial group is not written, as in the reference
+    coeff = np.stack([p[1] for p in parts])
+    cw = StreamWriter(w_, h_, 6, ui, 6)
+    cw.add_frames(coeff, mot[:6], uni[:6], nu[:6], coefficients=True)
+    data = cw.finish()
+    cw.close()
+    assert data == ref  # same group count (6 // 3 == 7 // 3) and the same records
+
+
+def test_add_frames_rejects_bad_runs():
+    n = (256 // 4) * (256 // 4)
+    w = StreamWriter(256, 256, 8, 2, 2)
+    fin, mot = np.zeros((2, n), np.uint64), np.full((2, 2 * n), 255, np.uint8)
+    uni = np.zeros((2, n), np.uint32)
+    with pytest.raises(MptcError):  # a palette longer than the frame
+        w.add_frames(fin, mot, uni, np.array([n + 1, 0], np.uint32))
+    with pytest.raises(ValueError):  # one frame's motion codes for a run of two
+        w.add_frames(fin, mot[:1], uni, np.array([0, 0], np.uint32))
+    w.add_frames(fin, mot, uni, np.array([n, n], np.uint32))
+    assert len(w.finish()) > 34
+    w.close()
