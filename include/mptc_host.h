@@ -117,6 +117,16 @@ mptc_status mptc_stream_reader_info(const mptc_stream_reader *reader, mptc_strea
 mptc_status mptc_stream_reader_next(mptc_stream_reader *reader, uint8_t *motion, uint8_t *coeff,
                                     uint32_t *unique_palette, uint32_t *n_unique);
 
+/* Up to max_frames next frames in one call, their parts decoded on all the
+ * host's cores: frame f's motion codes at motion + 2 * f * blocks, its
+ * coefficient planes at coeff + 6 * f * blocks, its palette slice at
+ * unique_palette + f * blocks (n_unique[f] entries); *n_read frames were
+ * read (fewer than max_frames at the end of the stream). MPTC_ESTATE when no
+ * frame is left; MPTC_EINVAL on a truncated or inconsistent stream. */
+mptc_status mptc_stream_reader_next_frames(mptc_stream_reader *reader, int32_t max_frames, uint8_t *motion,
+                                           uint8_t *coeff, uint32_t *unique_palette, uint32_t *n_unique,
+                                           int32_t *n_read);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,6 +5,7 @@
 // palette. The five parts of a frame decode concurrently on large frames.
 #include "../../include/mptc_host.h"
 #include "arith_coder.h"
+#include "parallel.h"
 
 #include <cstring>
 #include <new>
@@ -87,9 +88,19 @@ mptc_status mptc_stream_reader_info(const mptc_stream_reader *r, mptc_stream_inf
   return MPTC_OK;
 }
 
-mptc_status mptc_stream_reader_next(mptc_stream_reader *r, uint8_t *motion, uint8_t *coeff, uint32_t *unique,
-                                    uint32_t *n_unique) {
-  if (!r || !motion || !coeff || !unique || !n_unique) return MPTC_EINVAL;
+}  // extern "C"
+
+namespace {
+
+// One frame record parsed: its five coded parts, not yet decoded.
+struct FrameParts {
+  const uint8_t *code[5];
+  uint32_t size[5];
+};
+
+// Reads the next frame's record (and its group's palette first, at a group
+// start), copies the frame's palette slice to `unique`; the parts stay coded.
+mptc_status parse_frame(mptc_stream_reader *r, FrameParts *fp, uint32_t *unique, uint32_t *n_unique) {
   if (r->frame >= r->info.frames) return MPTC_ESTATE;
   const size_t n = r->nblk;
   if (r->frame % (uint32_t)r->info.unique_interval == 0) {
@@ -108,35 +119,73 @@ mptc_status mptc_stream_reader_next(mptc_stream_reader *r, uint8_t *motion, uint
   }
   // frame record: [u32 n_unique][u32 size][motion] then 4 x [u32 size][part] (decoder.cpp:361-401)
   uint32_t nu;
-  const uint8_t *code[5];
-  uint32_t csz[5];
   if (!r->take_u32(&nu)) return MPTC_EINVAL;
   for (int k = 0; k < 5; ++k)
-    if (!r->take_u32(&csz[k]) || !r->take(csz[k], &code[k])) return MPTC_EINVAL;
+    if (!r->take_u32(&fp->size[k]) || !r->take(fp->size[k], &fp->code[k])) return MPTC_EINVAL;
   if (nu > n || 4 * (size_t)nu > r->palette.size() - r->palette_used) return MPTC_EINVAL;
-  uint8_t *dst[5] = {motion, coeff, coeff + n, coeff + 3 * n, coeff + 4 * n};
-  const size_t len[5] = {2 * n, n, 2 * n, n, 2 * n};
-  bool ok[5];
-  // parts 1..4 on threads when the frame is large (parts whose thread could
-  // not be started decode here), part 0 on this thread
-  std::thread t[4];
-  int started = 0;
-  if (n >= kParallelBlocks) {
-    try {
-      for (int k = 1; k < 5; ++k, ++started)
-        t[k - 1] = std::thread([&, k] { ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]); });
-    } catch (...) {
-    }
-  }
-  for (int k = 1 + started; k < 5; ++k) ok[k] = mptc_host::decode_bytes(code[k], csz[k], dst[k], len[k]);
-  ok[0] = mptc_host::decode_bytes(code[0], csz[0], dst[0], len[0]);
-  for (int i = 0; i < started; ++i) t[i].join();
-  for (bool b : ok)
-    if (!b) return MPTC_EINVAL;
   std::memcpy(unique, r->palette.data() + r->palette_used, 4 * (size_t)nu);
   r->palette_used += 4 * (size_t)nu;
   *n_unique = nu;
   ++r->frame;
+  return MPTC_OK;
+}
+
+// Decodes part k of a parsed frame into the frame's motion / coefficient buffers.
+bool decode_part(const FrameParts &fp, size_t n, int k, uint8_t *motion, uint8_t *coeff) {
+  uint8_t *dst[5] = {motion, coeff, coeff + n, coeff + 3 * n, coeff + 4 * n};
+  const size_t len[5] = {2 * n, n, 2 * n, n, 2 * n};
+  return mptc_host::decode_bytes(fp.code[k], fp.size[k], dst[k], len[k]);
+}
+
+}  // namespace
+
+extern "C" {
+
+mptc_status mptc_stream_reader_next(mptc_stream_reader *r, uint8_t *motion, uint8_t *coeff, uint32_t *unique,
+                                    uint32_t *n_unique) {
+  if (!r || !motion || !coeff || !unique || !n_unique) return MPTC_EINVAL;
+  FrameParts fp;
+  uint32_t nu = 0;
+  const mptc_status st = parse_frame(r, &fp, unique, &nu);
+  if (st != MPTC_OK) return st;
+  // the five parts on five threads when the frame is large
+  const size_t n = r->nblk;
+  if (!mptc_host::parallel_for(5, n >= kParallelBlocks ? 5 : 1,
+                               [&](size_t k) { return decode_part(fp, n, (int)k, motion, coeff); }))
+    return MPTC_EINVAL;
+  *n_unique = nu;
+  return MPTC_OK;
+}
+
+mptc_status mptc_stream_reader_next_frames(mptc_stream_reader *r, int32_t max_frames, uint8_t *motion, uint8_t *coeff,
+                                           uint32_t *unique, uint32_t *n_unique, int32_t *n_read) {
+  if (!r || max_frames < 0 || !n_read || (max_frames > 0 && (!motion || !coeff || !unique || !n_unique)))
+    return MPTC_EINVAL;
+  *n_read = 0;
+  const size_t n = r->nblk;
+  std::vector<FrameParts> parts;
+  try {
+    parts.reserve((size_t)max_frames);
+  } catch (...) {
+    return MPTC_ENOMEM;
+  }
+  // records are parsed in order (their sizes locate the next one), then every
+  // part of every parsed frame is decoded on all the host's cores
+  while ((int32_t)parts.size() < max_frames) {
+    const size_t f = parts.size();
+    FrameParts fp;
+    const mptc_status st = parse_frame(r, &fp, unique + f * n, &n_unique[f]);
+    if (st == MPTC_ESTATE) break;
+    if (st != MPTC_OK) return st;
+    parts.push_back(fp);
+  }
+  if (parts.empty() && max_frames > 0) return MPTC_ESTATE;
+  if (!mptc_host::parallel_for(5 * parts.size(), mptc_host::host_threads(), [&](size_t j) {
+        const size_t f = j / 5;
+        return decode_part(parts[f], n, (int)(j % 5), motion + 2 * f * n, coeff + 6 * f * n);
+      }))
+    return MPTC_EINVAL;
+  *n_read = (int32_t)parts.size();
   return MPTC_OK;
 }
 

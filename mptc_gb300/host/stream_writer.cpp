@@ -4,13 +4,12 @@
 // reference encoder's stream. The arithmetic coder is in arith_coder.h.
 #include "../../include/mptc_host.h"
 #include "arith_coder.h"
+#include "parallel.h"
 
 #include <algorithm>
 #include <array>
-#include <atomic>
 #include <cstdint>
 #include <cstring>
-#include <functional>
 #include <new>
 #include <thread>
 #include <vector>
@@ -18,6 +17,8 @@
 namespace {
 
 using mptc_host::code_bytes;
+using mptc_host::host_threads;
+using mptc_host::parallel_for;
 
 constexpr size_t kParallelBlocks = 16384;  // frames this large code their parts concurrently
 
@@ -131,33 +132,6 @@ std::vector<uint8_t> endpoint_coefficients(const uint64_t *blocks, int bw, int b
   return out;
 }
 
-// Runs job(i) for i in [0, count) on up to `threads` threads, the calling
-// thread included (jobs of threads that could not be started run on the
-// others). Returns false if a job threw (an allocation failed).
-bool parallel_for(size_t count, size_t threads, const std::function<void(size_t)> &job) {
-  std::atomic<size_t> next{0};
-  std::atomic<bool> ok{true};
-  auto worker = [&] {
-    for (size_t i; (i = next.fetch_add(1)) < count;) {
-      try {
-        job(i);
-      } catch (...) {
-        ok = false;
-      }
-    }
-  };
-  std::vector<std::thread> pool;
-  const size_t extra = std::min(threads, count) > 1 ? std::min(threads, count) - 1 : 0;
-  try {
-    pool.reserve(extra);
-    for (size_t t = 0; t < extra; ++t) pool.emplace_back(worker);
-  } catch (...) {
-  }
-  worker();
-  for (std::thread &t : pool) t.join();
-  return ok;
-}
-
 // The five independently coded parts of a frame record: motion codes, Y1,
 // Co1|Cg1, Y2, Co2|Cg2 (codec/codec.cpp:1140-1155, :860-899). Each part has
 // its own coder and model, so parts and frames code independently.
@@ -201,14 +175,15 @@ void append_record(mptc_stream_writer *w, const FrameCode &z, const uint32_t *un
   }
 }
 
-size_t host_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
-
 // One frame: its five parts concurrently when the frame is large.
 void append_frame(mptc_stream_writer *w, const uint8_t *coeff, const uint8_t *motion, const uint32_t *unique,
                   uint32_t n_unique) {
   const size_t n = (size_t)w->bw * w->bh;
   FrameCode z;
-  if (!parallel_for(5, n >= kParallelBlocks ? 5 : 1, [&](size_t k) { z[k] = code_part(coeff, motion, n, (int)k); }))
+  if (!parallel_for(5, n >= kParallelBlocks ? 5 : 1, [&](size_t k) {
+        z[k] = code_part(coeff, motion, n, (int)k);
+        return true;
+      }))
     throw std::bad_alloc();
   append_record(w, z, unique, n_unique);
 }
@@ -226,7 +201,10 @@ void append_frames(mptc_stream_writer *w, size_t n_frames, const uint64_t *block
     const size_t m = std::min(chunk, n_frames - f0);
     if (blocks) {
       cf.assign(m, {});
-      if (!parallel_for(m, threads, [&](size_t i) { cf[i] = endpoint_coefficients(blocks + (f0 + i) * n, w->bw, w->bh); }))
+      if (!parallel_for(m, threads, [&](size_t i) {
+            cf[i] = endpoint_coefficients(blocks + (f0 + i) * n, w->bw, w->bh);
+            return true;
+          }))
         throw std::bad_alloc();
     }
     z.assign(m, FrameCode{});
@@ -234,6 +212,7 @@ void append_frames(mptc_stream_writer *w, size_t n_frames, const uint64_t *block
           const size_t i = j / 5;
           const uint8_t *c = blocks ? cf[i].data() : coeff + (f0 + i) * 6 * n;
           z[i][j % 5] = code_part(c, motion + (f0 + i) * 2 * n, n, (int)(j % 5));
+          return true;
         }))
       throw std::bad_alloc();
     for (size_t i = 0; i < m; ++i)

@@ -25,7 +25,7 @@ HOST_EXPORTED = [
     "mptc_stream_writer_add_frame_coefficients", "mptc_stream_writer_add_frames",
     "mptc_stream_writer_add_frames_coefficients", "mptc_stream_writer_finish",
     "mptc_stream_writer_frame_sizes", "mptc_stream_reader_open", "mptc_stream_reader_destroy",
-    "mptc_stream_reader_info", "mptc_stream_reader_next",
+    "mptc_stream_reader_info", "mptc_stream_reader_next", "mptc_stream_reader_next_frames",
 ]
 
 
@@ -60,6 +60,7 @@ def host_lib() -> ctypes.CDLL:
         L.mptc_stream_reader_destroy.argtypes = [vp]
         L.mptc_stream_reader_info.argtypes = [vp, ctypes.POINTER(StreamInfo)]
         L.mptc_stream_reader_next.argtypes = [vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
+        L.mptc_stream_reader_next_frames.argtypes = [vp, i32, vp, vp, vp, vp, ctypes.POINTER(i32)]
         _HOST = L
     return _HOST
 
@@ -207,6 +208,25 @@ class StreamReader:
             return None
         _check(rc, "stream frame")
         return motion, coeff, unique[: nu.value]
+
+    def next_frames(self, max_frames: int):
+        """Up to max_frames next frames, their parts decoded on all host cores:
+        (motion (F, 2n) u8, coeff (F, 6n) u8, unique (F, n) u32, n_unique (F,)
+        u32) with F frames read (0 at the end of the stream)."""
+        n = self.blocks
+        motion = np.empty((max_frames, 2 * n), np.uint8)
+        coeff = np.empty((max_frames, 6 * n), np.uint8)
+        unique = np.empty((max_frames, n), np.uint32)
+        nu = np.zeros(max_frames, np.uint32)
+        got = ctypes.c_int32(0)
+        rc = host_lib().mptc_stream_reader_next_frames(self._h, max_frames, motion.ctypes.data, coeff.ctypes.data,
+                                                       unique.ctypes.data, nu.ctypes.data, ctypes.byref(got))
+        if rc == 5:  # MPTC_ESTATE: no frames left
+            got.value = 0
+        else:
+            _check(rc, "stream frames")
+        f = got.value
+        return motion[:f], coeff[:f], unique[:f], nu[:f]
 
     def __iter__(self):
         while True:

@@ -244,3 +244,30 @@ def test_add_frames_rejects_bad_runs():
     w.add_frames(fin, mot, uni, np.array([n, n], np.uint32))
     assert len(w.finish()) > 34
     w.close()
+
+
+def test_reader_next_frames_matches_next_frame():
+    """The reader's run call (parts of many frames decoded on all host cores)
+    returns what frame-by-frame reads return, stops at the end of the stream,
+    and rejects a truncated stream."""
+    from mptc_gb300.stream import StreamReader
+    case = STREAMS[2]
+    _, _, data = _oracle_stream(case)
+    one = list(StreamReader(data))
+    rd = StreamReader(data)
+    got = []
+    while True:
+        mot, coeff, uni, nu = rd.next_frames(3)
+        if len(nu) == 0:
+            break
+        got += [(mot[f], coeff[f], uni[f, : nu[f]]) for f in range(len(nu))]
+    rd.close()
+    assert len(got) == len(one) > 3
+    for a, b in zip(got, one):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
+    rd = StreamReader(data[: len(data) // 2])
+    with pytest.raises(MptcError):
+        for _ in range(len(one)):
+            rd.next_frames(len(one))
+    rd.close()
