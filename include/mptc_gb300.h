@@ -164,7 +164,10 @@ mptc_status mptc_encode_stream_device(mptc_ctx *ctx, const uint8_t *frames_dev, 
  * Frames larger than MPTC_NOALLOC_MAX_BLOCKS blocks are rejected with
  * MPTC_EINVAL. The first call on a device sets that device up (looks up the
  * scratch array's device address and uploads the stb tables); make that first
- * call before any stream capture. All calls share the one scratch array, so
+ * call before any stream capture. The set-up is kept for the life of the
+ * process: cudaDeviceReset on a device that has made a call is not supported
+ * (the saved scratch address and tables would be stale afterwards). All calls
+ * share the one scratch array, so
  * calls that overlap on the GPU (on different streams, or from several host
  * threads) race and corrupt each other's results: serialise them. Outputs and
  * their layouts are those of mptc_encode_frame; stb_dev may be NULL. If a

@@ -65,7 +65,12 @@ mptc_status mptc_stream_writer_add_frame_coefficients(mptc_stream_writer *writer
  * motion + 2 * f * blocks, its palette at unique_palette + f * blocks with
  * n_unique[f] entries. The frames' endpoint transforms and coded parts are
  * computed on all the host's cores and appended in frame order: the bytes are
- * those of n_frames mptc_stream_writer_add_frame calls. */
+ * those of n_frames mptc_stream_writer_add_frame calls. The run is coded in
+ * chunks of 2 x (host threads) frames; if host memory runs out part way, the
+ * call returns MPTC_ENOMEM after the earlier chunks' records were appended,
+ * and the writer is unusable from then on (every later add or finish call
+ * returns MPTC_ESTATE), as after a failed single-frame call. The host threads
+ * are the hardware threads, or MPTC_HOST_THREADS from the environment. */
 mptc_status mptc_stream_writer_add_frames(mptc_stream_writer *writer, int32_t n_frames,
                                           const uint64_t *final_blocks, const uint8_t *motion,
                                           const uint32_t *unique_palette, const uint32_t *n_unique);
@@ -122,7 +127,11 @@ mptc_status mptc_stream_reader_next(mptc_stream_reader *reader, uint8_t *motion,
  * coefficient planes at coeff + 6 * f * blocks, its palette slice at
  * unique_palette + f * blocks (n_unique[f] entries); *n_read frames were
  * read (fewer than max_frames at the end of the stream). MPTC_ESTATE when no
- * frame is left; MPTC_EINVAL on a truncated or inconsistent stream. */
+ * frame is left; MPTC_EINVAL on a truncated or inconsistent stream. The call
+ * parses all the records it reads before decoding their parts, so an error in
+ * any of them (or in decoding any part) returns MPTC_EINVAL with *n_read = 0
+ * after the reader has moved past the parsed records: the frames of that call
+ * are lost and the reader is unusable from then on (destroy it). */
 mptc_status mptc_stream_reader_next_frames(mptc_stream_reader *reader, int32_t max_frames, uint8_t *motion,
                                            uint8_t *coeff, uint32_t *unique_palette, uint32_t *n_unique,
                                            int32_t *n_read);

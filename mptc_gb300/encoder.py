@@ -15,6 +15,21 @@ import numpy as np
 from ._lib import Config, FrameStats, KernelTime, check, dev_ptr, host_ptr, lib
 
 
+def intra_schedule(n: int, interval: int) -> list[bool]:
+    """Intra flags of n frames: the first frame intra, then every interval-th
+    (CompressMultiUnique's set_intra / intra_num loop, codec/codec.cpp:1462-1469)."""
+    out, num, nxt = [], 1, True
+    for _ in range(n):
+        out.append(nxt)
+        if num <= interval:
+            nxt = False
+            if num == interval:
+                nxt, num = True, 1
+            else:
+                num += 1
+    return out
+
+
 @dataclass
 class FrameOutput:
     final: np.ndarray    # u64 per block (PhysicalDXTBlock)

@@ -3,6 +3,7 @@
 #pragma once
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstddef>
 #include <functional>
 #include <thread>
@@ -10,7 +11,17 @@
 
 namespace mptc_host {
 
-inline size_t host_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
+// Threads of the host coder: the host's hardware threads, or the positive
+// integer in the environment variable MPTC_HOST_THREADS when it is set (a
+// caller that shares the host with other work, or a test that wants small
+// chunks).
+inline size_t host_threads() {
+  if (const char *e = std::getenv("MPTC_HOST_THREADS")) {
+    const long v = std::strtol(e, nullptr, 10);
+    if (v > 0) return (size_t)std::min(v, 4096L);
+  }
+  return std::max(1u, std::thread::hardware_concurrency());
+}
 
 // Runs job(i) for i in [0, count) on up to `threads` threads, the calling
 // thread included (jobs of threads that could not be started run on the

@@ -156,22 +156,29 @@ class StreamWriter:
             pass
 
 
-def write_stream(frames, width: int, height: int, search_area: int, unique_interval: int) -> bytes:
+def write_stream(frames, width: int, height: int, search_area: int, unique_interval: int,
+                 chunk_frames: int | None = None) -> bytes:
     """Stream bytes of encoded frames: each item has ``final``, ``motion`` and
     ``unique`` arrays (or is a (final, motion, unique) tuple). The frames are
-    coded in one add_frames call (all host cores)."""
+    coded in add_frames calls of ``chunk_frames`` frames each (default: twice
+    the host's cores, the writer's own chunk), so that only one chunk's
+    stacked arrays are held at a time; the bytes do not depend on the chunk."""
     frames = [f if isinstance(f, tuple) else (f.final, f.motion, f.unique) for f in frames]
     w = StreamWriter(width, height, search_area, unique_interval, len(frames))
+    step = chunk_frames if chunk_frames is not None else 2 * (os.cpu_count() or 1)
+    if step < 1:
+        raise ValueError("chunk_frames must be positive")
     try:
-        if frames:
-            n = w.blocks
-            final = np.stack([np.asarray(f[0], np.uint64).reshape(-1) for f in frames])
-            motion = np.stack([np.asarray(f[1], np.uint8).reshape(-1) for f in frames])
-            n_unique = np.array([np.size(f[2]) for f in frames], np.uint32)
+        n = w.blocks
+        for c0 in range(0, len(frames), step):
+            part = frames[c0:c0 + step]
+            final = np.stack([np.asarray(f[0], np.uint64).reshape(-1) for f in part])
+            motion = np.stack([np.asarray(f[1], np.uint8).reshape(-1) for f in part])
+            n_unique = np.array([np.size(f[2]) for f in part], np.uint32)
             if final.shape[1] != n or motion.shape[1] != 2 * n or (n_unique > n).any():
                 raise ValueError(f"frame arrays do not match {n} blocks")
-            unique = np.zeros((len(frames), n), np.uint32)
-            for k, f in enumerate(frames):
+            unique = np.zeros((len(part), n), np.uint32)
+            for k, f in enumerate(part):
                 unique[k, : n_unique[k]] = np.asarray(f[2], np.uint32).reshape(-1)
             w.add_frames(final, motion, unique, n_unique)
         return w.finish()

@@ -101,3 +101,19 @@ def mixed_batch(frames: int = 30) -> list[StreamSpec]:
 
 def uhd_streams() -> list[StreamSpec]:
     return [replace(UHD2160, seed=1000 + s) for s in range(4)]
+
+
+def pad_edge(frames: np.ndarray, multiple: int) -> np.ndarray:
+    """Frames (..., H, W, 3) padded on the right and bottom to multiples of
+    `multiple` pixels by repeating the last column and row. The reference's
+    stream writer needs frame sizes that are multiples of 256 pixels (its
+    endpoint wavelet works on 64x64-block tiles, codec/image_processing.h:293-294)
+    and its block gather needs widths that are multiples of 4
+    (codec/dxt_image.cpp:128-139)."""
+    h, w = frames.shape[-3], frames.shape[-2]
+    ph = (h + multiple - 1) // multiple * multiple - h
+    pw = (w + multiple - 1) // multiple * multiple - w
+    if ph == 0 and pw == 0:
+        return frames
+    widths = [(0, 0)] * (frames.ndim - 3) + [(0, ph), (0, pw), (0, 0)]
+    return np.pad(frames, widths, mode="edge")

@@ -9,22 +9,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .encoder import Encoder
+from .encoder import Encoder, intra_schedule
 from .model import ProposalModel, sample_examples
-
-
-def intra_flags(n: int, interval: int) -> list[bool]:
-    """Frame 1 intra, then every interval-th (the reference's schedule)."""
-    out, num, nxt = [], 1, True
-    for _ in range(n):
-        out.append(nxt)
-        if num <= interval:
-            nxt = False
-            if num == interval:
-                nxt, num = True, 1
-            else:
-                num += 1
-    return out
 
 
 def train_proposal(torch, frames_dev, search_area=8, err_threshold=5, intra_interval=16, steps=400,
@@ -35,7 +21,7 @@ def train_proposal(torch, frames_dev, search_area=8, err_threshold=5, intra_inte
     n = bw * bh
     dev = frames_dev.device
     enc = Encoder(W, H, search_area, err_threshold, intra_interval)
-    flags = intra_flags(T, intra_interval)
+    flags = intra_schedule(T, intra_interval)
     fin = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(2)]
     mot = torch.empty(2 * n, dtype=torch.uint8, device=dev)
     uni = torch.empty(n, dtype=torch.int32, device=dev)

@@ -41,6 +41,8 @@ def lib():
                                            i32]
         L.mo_frame_psnr.argtypes = [vp, i32, i32, vp, vp]
         L.mo_frame_psnr.restype = ctypes.c_double
+        L.mo_decoded_sse.argtypes = [vp, i32, i32, vp]
+        L.mo_decoded_sse.restype = ctypes.c_uint64
         _LIB = L
     return _LIB
 
@@ -76,6 +78,15 @@ def refit(px48: np.ndarray, interp: int):
     valid = ctypes.c_int(0)
     err = lib().mo_refit(_ptr(a), ctypes.c_uint32(interp), _ptr(e1), _ptr(e2), ctypes.byref(valid))
     return int(err), e1, e2, bool(valid.value)
+
+
+def decoded_sse(frame: np.ndarray, blocks: np.ndarray) -> int:
+    """Squared error of a frame against its decoded DXT1 blocks (u64 each)."""
+    h, w, _ = frame.shape
+    f = np.ascontiguousarray(frame, dtype=np.uint8)
+    b = np.ascontiguousarray(blocks, dtype=np.uint64)
+    assert b.size == (h // 4) * (w // 4)
+    return int(lib().mo_decoded_sse(_ptr(f), w, h, _ptr(b)))
 
 
 @dataclass

@@ -728,3 +728,31 @@ double mo_frame_psnr(const uint8_t *rgb, int width, int height, const uint64_t *
   mse /= (double)(width * height);
   return 10.0 * log10((3.0 * 255.0 * 255.0) / mse);
 }
+
+/* Squared error of a frame against what a DXT1 decoder shows for its physical
+ * blocks: every block's palette is PhysicalToLogical's (codec/dxt_image.cpp:198-227:
+ * Decode565 of both endpoints, LerpChannels 1/3 and 2/3 when ep1 > ep2, else
+ * the midpoint and black), whatever 8-bit endpoints a refit kept in the
+ * encoder's logical blocks. This is the quantity DXTImage::PSNR
+ * (:363-383) measures when every logical block is PhysicalToLogical of its
+ * physical block, as after the constructor (:419-434). */
+uint64_t mo_decoded_sse(const uint8_t *rgb, int width, int height, const uint64_t *blocks) {
+  const int bw = width >> 2, bh = height >> 2;
+  uint64_t sse = 0;
+  for (int by = 0; by < bh; ++by) {
+    for (int bx = 0; bx < bw; ++bx) {
+      const uint64_t b = blocks[(size_t)by * bw + bx];
+      uint8_t pal[4][3], px[48];
+      block_palette(b, pal);
+      gather_block(rgb, width, bx, by, px);
+      for (int i = 0; i < 16; ++i) {
+        const int k = (int)((b >> (32 + 2 * i)) & 3);
+        for (int c = 0; c < 3; ++c) {
+          const int d = (int)px[3 * i + c] - (int)pal[k][c];
+          sse += (uint64_t)(d * d);
+        }
+      }
+    }
+  }
+  return sse;
+}

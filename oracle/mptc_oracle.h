@@ -61,6 +61,10 @@ int mo_reencode_frame_mt(const uint8_t *rgb, int width, int height, const uint64
 double mo_frame_psnr(const uint8_t *rgb, int width, int height, const uint64_t *final_blocks,
                      const uint64_t *stb_blocks);
 
+/* Squared error of the frame against the decoded DXT1 blocks (RGB565 endpoints
+ * expanded, PhysicalToLogical palettes), summed over every pixel and channel. */
+uint64_t mo_decoded_sse(const uint8_t *rgb, int width, int height, const uint64_t *blocks);
+
 #ifdef __cplusplus
 }
 #endif

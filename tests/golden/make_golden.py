@@ -18,9 +18,17 @@ synthetic streams and on adversarial block patterns, and records:
                        (``GetFrame`` via ``oracle/_ref/decoder_harness``)
                        rebuilds from each stream, which pin the GPU decoder.
 
+``configs.json`` (``--configs``) holds the same per-frame records for the
+measured workloads at their full sizes: all 120 frames of the 1080p stream,
+all 64 frames of the 720p stream with its scene cut (and its whole MPTC stream,
+edge-padded to 1280x768), one stream of each resolution of the mixed batch,
+and the 2160p stress stream at the largest search area (63); the reference
+runs of these take most of an hour on one core each, so they run side by side.
+
 Usage (needs the reference sources; run from the repository root):
     make -C oracle/ref REF=<path to MPTC>
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # golden.json + adversarial fixtures
+    python tests/golden/make_golden.py --configs  # configs.json
 """
 from __future__ import annotations
 
@@ -38,7 +46,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 
-from mptc_gb300.synth import HD720, FHD1080, SMOKE_256, StreamSpec  # noqa: E402
+from mptc_gb300.synth import (HD720, FHD1080, SMOKE_256, StreamSpec, mixed_batch, pad_edge,  # noqa: E402
+                              uhd_streams)
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "hotpath_harness")
 ENCODER = os.path.join(ROOT, "oracle", "_ref", "mptc_encoder")
@@ -68,6 +77,28 @@ STREAM_CASES = [
     ("stream256_sa4_thr0_ii4_ui3_tail", SMOKE_256, 0, 8, 4, 0, 4, 3),
     ("stream512x256_sa2_thr20_ii2_ui1", StreamSpec(512, 256, 4, seed=21, n_squares=3), 0, 4, 2, 20, 2, 1),
     ("stream256x512_sa16_thr5_ii8_ui4", StreamSpec(256, 512, 8, seed=22, cut_every=3), 0, 8, 16, 5, 8, 4),
+]
+
+
+# The measured workloads at full size: (name, spec, first frame, frame count,
+# search_area, threshold, intra_interval).
+def config_cases():
+    mixed = mixed_batch()
+    return [
+        ("fhd1080_120f_sa8_thr5", FHD1080, 0, 120, 8, 5, 16),
+        ("hd720_64f_sa8_thr5", HD720, 0, 64, 8, 5, 16),
+        ("mixed_856x480_s1000", mixed[0], 0, 4, 8, 5, 16),
+        ("mixed_1280x720_s1009", mixed[9], 0, 4, 8, 5, 16),
+        ("mixed_1920x1080_s1018", mixed[18], 0, 4, 8, 5, 16),
+        ("mixed_2560x1440_s1027", mixed[27], 0, 4, 8, 5, 16),
+        ("uhd2160_sa63_thr5", uhd_streams()[0], 0, 2, 63, 5, 16),
+    ]
+
+
+# Whole streams of the measured workloads, frames edge-padded to 256-pixel
+# multiples: (name, spec, frame count, sa, thr, intra interval, unique interval).
+CONFIG_STREAMS = [
+    ("hd720_pad1280x768_64f_sa8_thr5_ii16_ui8", HD720, 64, 8, 5, 16, 8),
 ]
 
 
@@ -258,5 +289,49 @@ def main() -> None:
         json.dump(golden, f, indent=1)
 
 
+def _config_case(case):
+    name, spec, first, count, sa, thr, ii = case
+    frames = spec.generate(first, count)
+    res = run_reference(frames, sa, thr, ii)
+    return dict(name=name, spec=spec.__dict__, first=first, count=count, search_area=sa,
+                threshold=thr, intra_interval=ii, input_sha=[sha(f) for f in frames],
+                frames=[frame_record(r) for r in res])
+
+
+def _config_stream(case):
+    name, spec, count, sa, thr, ii, ui = case
+    frames = pad_edge(spec.generate(0, count), 256)
+    data = run_reference_stream(frames, sa, thr, ii, ui)
+    n_dec = (count // ui - 1) * ui + 1
+    decoded = run_reference_decoder(data, n_dec)
+    return dict(name=name, spec=spec.__dict__, count=count, pad=256, search_area=sa, threshold=thr,
+                intra_interval=ii, unique_interval=ui, width=int(frames.shape[2]),
+                height=int(frames.shape[1]), input_sha=[sha(f) for f in frames], size=len(data),
+                sha=hashlib.sha256(data).hexdigest(), decoded=[sha(b) for b in decoded])
+
+
+def main_configs() -> None:
+    import multiprocessing as mp
+    if not os.path.exists(HARNESS):
+        sys.exit(f"{HARNESS} missing: build it with make -C oracle/ref")
+    cases = config_cases()
+    # longest first, so that the pool's last worker is not the slowest case
+    order = sorted(range(len(cases)), key=lambda i: -cases[i][3] * cases[i][1].width * cases[i][1].height
+                   * cases[i][4] ** 2)
+    with mp.get_context("spawn").Pool(min(len(cases) + 1, os.cpu_count() or 1)) as pool:
+        streams = [pool.apply_async(_config_stream, (c,)) for c in CONFIG_STREAMS]
+        jobs = {i: pool.apply_async(_config_case, (cases[i],)) for i in order}
+        out = {"generator": "mptc_gb300/csrc/synth_frames.c",
+               "cases": [jobs[i].get() for i in range(len(cases))],
+               "streams": [j.get() for j in streams]}
+    for c in out["cases"]:
+        print(c["name"], [(fr["n_inter"], fr["n_intra"], fr["n_unique"]) for fr in c["frames"]][:4])
+    with open(os.path.join(OUT_DIR, "configs.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 if __name__ == "__main__":
-    main()
+    if "--configs" in sys.argv[1:]:
+        main_configs()
+    else:
+        main()

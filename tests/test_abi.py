@@ -54,16 +54,14 @@ def test_version_and_arch_need_no_gpu():
 def test_default_intra_schedule_matches_reference_loop():
     """The encoder's default intra flags (used by the per-frame and the stream
     calls) follow the reference's schedule: the first frame intra, then every
-    intra_interval-th (codec/codec.cpp:1462-1469), as bench.intra_schedule
-    and the oracle's stream loop do."""
-    from mptc_gb300.encoder import Encoder
-
-    import bench
+    intra_interval-th (codec/codec.cpp:1462-1469), as intra_schedule (used by
+    the bench and the training loop) and the oracle's stream loop do."""
+    from mptc_gb300.encoder import Encoder, intra_schedule
     for interval in (1, 2, 5, 16):
         enc = Encoder.__new__(Encoder)  # the schedule state only: no context
         enc.intra_interval, enc._intra_num, enc._next_intra = interval, 1, True
         flags = [enc._intra_flag(None) for _ in range(70)]
-        assert flags == bench.intra_schedule(70, interval)
+        assert flags == intra_schedule(70, interval)
         assert enc._intra_flag(True) is True and enc._intra_flag(False) is False
 
 

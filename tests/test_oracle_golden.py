@@ -66,3 +66,43 @@ def test_oracle_threaded_equals_single_thread():
 def test_oracle_rejects_bad_sizes():
     with pytest.raises(ValueError):
         oracle.dxt1_encode(np.zeros((6, 8, 3), np.uint8))
+
+
+def _decoded_sse_numpy(frame, blocks):
+    """Plain numpy restatement: Decode565 (codec/dxt_image.cpp:43-61) and the
+    PhysicalToLogical palette (:198-227) of every block, squared error."""
+    h, w, _ = frame.shape
+    b = blocks.astype(np.uint64)
+    e = [(b >> np.uint64(s)) & np.uint64(0xFFFF) for s in (0, 16)]
+    e = [x.astype(np.int64) for x in e]
+
+    def dec(v):
+        r, g, bl = v >> 11, (v >> 5) & 63, v & 31
+        return np.stack([(r << 3) | (r >> 2), (g << 2) | (g >> 4), (bl << 3) | (bl >> 2)], -1)
+    c0, c1 = dec(e[0]), dec(e[1])
+    four = (e[0] > e[1])[:, None]
+    c2 = np.where(four, (2 * c0 + c1) // 3, (c0 + c1) // 2)
+    c3 = np.where(four, (c0 + 2 * c1) // 3, 0)
+    pal = np.stack([c0, c1, c2, c3], 1)  # (n, 4, 3)
+    idx = np.stack([((b >> np.uint64(32 + 2 * i)) & np.uint64(3)).astype(np.int64) for i in range(16)], 1)
+    px = frame.astype(np.int64).reshape(h // 4, 4, w // 4, 4, 3).transpose(0, 2, 1, 3, 4).reshape(-1, 16, 3)
+    dec_px = np.take_along_axis(pal, idx[:, :, None].repeat(3, 2), 1)
+    return int(((px - dec_px) ** 2).sum())
+
+
+def test_oracle_decoded_sse():
+    """The decoded-block squared error (the quantity the learned proposal's
+    PSNR gate compares) equals a numpy restatement on an encoded stream, and on
+    a frame where no block is accepted (every block keeps its stb block, so the
+    logical palettes are PhysicalToLogical's) it gives the PSNR of the pinned
+    DXTImage::PSNR restatement."""
+    frames = StreamSpec(96, 64, 3, seed=31).generate()
+    for r, f in zip(oracle.encode_stream(frames, 4, 5, 16, threads=4), frames):
+        assert oracle.decoded_sse(f, r.final) == _decoded_sse_numpy(f, r.final)
+        assert oracle.decoded_sse(f, r.stb) == _decoded_sse_numpy(f, r.stb)
+    f = frames[1]
+    stb = oracle.dxt1_encode(f)
+    r = oracle.reencode(f, stb, None, 4, -(1 << 20))
+    assert np.array_equal(r.final, stb)
+    mse = oracle.decoded_sse(f, r.final) / (f.shape[0] * f.shape[1])
+    assert abs(10.0 * np.log10(3.0 * 255.0 ** 2 / mse) - r.psnr) <= 1e-9 * r.psnr

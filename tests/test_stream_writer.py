@@ -232,6 +232,35 @@ def test_add_frames_matches_frame_by_frame_and_coefficients():
     assert data == ref  # same group count (6 // 3 == 7 // 3) and the same records
 
 
+def test_add_frames_chunk_boundaries_inside_one_call(monkeypatch):
+    """With one host thread the writer codes runs in chunks of 2 frames, so one
+    add_frames call of 7 frames crosses three chunk boundaries, two of them
+    inside a unique group; the bytes equal frame-by-frame calls. write_stream
+    in chunks of 2 and 5 frames writes them too."""
+    from mptc_gb300.stream import write_stream
+    w_, h_, nf, ui = 256, 256, 7, 3
+    frames = StreamSpec(w_, h_, nf, seed=78, n_squares=2, square_size=40).generate()
+    res = oracle.encode_stream(frames, 4, 5, 4, threads=os.cpu_count() or 1, want_psnr=False)
+    one = StreamWriter(w_, h_, 4, ui, nf)
+    for r in res:
+        one.add_frame(r.final, r.motion, r.unique)
+    ref = one.finish()
+    one.close()
+    n = (w_ // 4) * (h_ // 4)
+    nu = np.array([len(r.unique) for r in res], np.uint32)
+    uni = np.zeros((nf, n), np.uint32)
+    for k, r in enumerate(res):
+        uni[k, : nu[k]] = r.unique
+    monkeypatch.setenv("MPTC_HOST_THREADS", "1")
+    run = StreamWriter(w_, h_, 4, ui, nf)
+    run.add_frames(np.stack([r.final for r in res]), np.stack([r.motion for r in res]), uni, nu)
+    assert run.finish() == ref
+    run.close()
+    monkeypatch.delenv("MPTC_HOST_THREADS")
+    for chunk in (2, 5):
+        assert write_stream(res, w_, h_, 4, ui, chunk_frames=chunk) == ref
+
+
 def test_add_frames_rejects_bad_runs():
     n = (256 // 4) * (256 // 4)
     w = StreamWriter(256, 256, 8, 2, 2)
