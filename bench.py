@@ -405,6 +405,9 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
                                               "152 SMs x 128 lanes at the clock seen",
                                     timing_note="CUDA-event launch times of the same step, run after the timed region, where the "
                                                 "intra frames of the second lane overlap the inter frames")
+    if rank == 0 and world == 1 and not args.no_learned and nf == FRAMES:
+        line["learned"] = learned_comparison(args, torch, dev, frames_dev, value, log)
+    if rank == 0:
         print(json.dumps(line), flush=True)
     enc.close()
 
@@ -570,155 +573,168 @@ def psnr_db(sse_list, W_, H_):
     return float(np.mean([10.0 * np.log10(3.0 * 255.0 ** 2 / (s / (W_ * H_))) for s in sse_list]))
 
 
-def run_learned(args, rank: int, world: int, dist) -> None:
-    """Learned proposal vs exhaustive search on the 1080p stream: trains on 200
-    separate seeded frames with the library's kernels, then times both forms
-    (single stream, or --batch S concurrent streams) and compares decoded
-    PSNR and the motion/palette code length on the same 120 frames, and the
-    bytes of whole MPTC streams of the first 32 frames (edge-padded to
-    256-pixel multiples, decoded back bit-exactly on the GPU)."""
-    import torch
+def time_stream_call(torch, enc, frames_dev, sched, steps, warmup):
+    """Frames/s of mptc_encode_stream_device over the frames (outputs in HBM)."""
+    nf = frames_dev.shape[0]
+    n = enc.nblk
+    dev = frames_dev.device
+    fin = torch.empty((nf, n), dtype=torch.int64, device=dev)
+    mot = torch.empty((nf, 2 * n), dtype=torch.uint8, device=dev)
+    uni = torch.empty((nf, n), dtype=torch.int32, device=dev)
+    nu = torch.empty(nf, dtype=torch.int32, device=dev)
+    s = torch.cuda.current_stream()
+    for _ in range(warmup):
+        enc.encode_stream_device(frames_dev, fin, mot, uni, nu, is_intra=sched, stream=s)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        enc.encode_stream_device(frames_dev, fin, mot, uni, nu, is_intra=sched, stream=s)
+    e1.record(s)
+    torch.cuda.synchronize()
+    enc.stats(s)  # raises on a device-side timeout
+    return nf * steps / (e0.elapsed_time(e1) * 1e-3)
 
+
+def time_batch(torch, frames_dev, S, model, topk, steps, warmup):
+    """S concurrent streams of the 1080p stream (stream k from frame offset 15k,
+    its intra frames at phase 16k/S) through the batched encoder; frames/s of
+    all streams together."""
     from mptc_gb300.batch import BatchEncoder
-    from mptc_gb300.encoder import Encoder
-    from mptc_gb300.synth import FHD1080, FHD1080_TRAIN
-    from mptc_gb300.training import train_proposal
+    nf = frames_dev.shape[0]
+    b = BatchEncoder([(W, H)] * S, SA, THR, II)
+    if model is not None:
+        b.set_model(model, topk)
+    offsets = [(15 * k) % nf for k in range(S)]
+    phases = [(II * k) // S for k in range(S)]
+    s = torch.cuda.current_stream()
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
+    def flags(f):
+        return [f == 0 or (f - phases[k]) % II == 0 for k in range(S)]
+
+    def step():
+        for f in range(nf):
+            for k in range(S):
+                b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
+            b.encode(flags(f), s)
+    for f in range(2):
+        for k in range(S):
+            b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
+        b.encode(flags(f), s)
+    tuned = b.autotune(flags(2), s)
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    b.fetch(0)
+    b.close()
+    return S * nf * steps / (e0.elapsed_time(e1) * 1e-3), tuned
+
+
+def learned_comparison(args, torch, dev, frames_dev, plain_fps, log):
+    """The learned proposal against the exhaustive search on the 1080p stream:
+    trains on 200 separate seeded 1080p frames with the library's kernels, then
+    measures the learned form single-stream and batched beside the plain form,
+    the decoded PSNR and motion/palette code length of the same 120 frames, and
+    the bytes of whole MPTC streams of the first 32 frames (edge-padded to
+    256-pixel multiples, decoded back bit-exactly on the GPU)."""
+    from mptc_gb300.encoder import Encoder
+    from mptc_gb300.synth import FHD1080_TRAIN
+    from mptc_gb300.training import train_proposal
     t0 = time.time()
     train_dev = torch.from_numpy(FHD1080_TRAIN.generate()).to(dev)
-    log(f"[rank {rank}] training frames in {time.time() - t0:.1f}s")
-    t0 = time.time()
-    model, losses = train_proposal(torch, train_dev, SA, THR, II, steps=args.train_steps, batch=4096, cands=16,
-                                   lr=1e-3, log=log if rank == 0 else None)
-    torch.cuda.synchronize()
-    train_s = time.time() - t0
+    gen_s = time.time() - t0
+    model, losses, tinfo = train_proposal(torch, train_dev, SA, THR, II, steps=args.train_steps, batch=4096,
+                                          cands=32, lr=1e-3, log=log)
     del train_dev
-    nf = args.frames
-    frames_dev = torch.from_numpy(FHD1080.generate(0, nf)).to(dev)
+    torch.cuda.empty_cache()
+    nf = frames_dev.shape[0]
     sched = intra_schedule(nf, II)
-    # quality: the same stream through both forms
+    K = args.topk
     plain_enc = Encoder(W, H, SA, THR, II)
     learned_enc = Encoder(W, H, SA, THR, II)
-    learned_enc.set_model(model, args.topk)
+    learned_enc.set_model(model, K)
     qp = encode_stream_quality(torch, plain_enc, frames_dev, sched, W, H)
     ql = encode_stream_quality(torch, learned_enc, frames_dev, sched, W, H)
-    # bitrate: whole MPTC streams of the first frames, padded to 256-pixel multiples
     ns, UI = min(nf, 32), 8
     padded = pad_to_tiles(torch, frames_dev[:ns])
     pw, ph = padded.shape[2], padded.shape[1]
     enc_p = Encoder(pw, ph, SA, THR, II)
     bytes_p, exact_p = stream_size(torch, enc_p, padded, sched, UI)
-    enc_p.set_model(model, args.topk)
+    enc_p.set_model(model, K)
     bytes_l, exact_l = stream_size(torch, enc_p, padded, sched, UI)
     enc_p.close()
     del padded
-    n = (W // 4) * (H // 4)
-    inter_blocks = sum(1 for f in sched if not f) * n
-
-    def time_single(enc):
-        fin = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(2)]
-        stb = torch.empty(n, dtype=torch.int64, device=dev)
-        mot = torch.empty(2 * n, dtype=torch.uint8, device=dev)
-        uni = torch.empty(n, dtype=torch.int32, device=dev)
-        nu = torch.zeros(1, dtype=torch.int32, device=dev)
-        s = torch.cuda.current_stream()
-
-        def step():
-            for f in range(nf):
-                prev = None if sched[f] else fin[(f - 1) % 2]
-                enc.encode_frame_device(frames_dev[f], prev, stb, fin[f % 2], mot, uni, nu, s)
-        for _ in range(args.warmup):
-            step()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(s)
-        for _ in range(args.steps):
-            step()
-        e1.record(s)
-        torch.cuda.synchronize()
-        return nf * args.steps / (e0.elapsed_time(e1) * 1e-3)
-
-    def time_batch(S, with_model):
-        b = BatchEncoder([(W, H)] * S, SA, THR, II)
-        if with_model:
-            b.set_model(model, args.topk)
-        offsets = [(15 * k) % nf for k in range(S)]
-        phases = [(II * k) // S for k in range(S)]
-        s = torch.cuda.current_stream()
-
-        def flags(f):
-            return [f == 0 or (f - phases[k]) % II == 0 for k in range(S)]
-
-        def step():
-            for f in range(nf):
-                for k in range(S):
-                    b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
-                b.encode(flags(f), s)
-        for f in range(2):
-            for k in range(S):
-                b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
-            b.encode(flags(f), s)
-        b.autotune(flags(2), s)
-        for _ in range(args.warmup):
-            step()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(s)
-        for _ in range(args.steps):
-            step()
-        e1.record(s)
-        torch.cuda.synchronize()
-        b.fetch(0)
-        b.close()
-        return S * nf * args.steps / (e0.elapsed_time(e1) * 1e-3)
-
-    clk = ClockSampler(local)
-    plain_fps = time_single(plain_enc)
-    learned_fps = time_single(learned_enc)
-    S = args.batch
-    plain_b = time_batch(S, False) if S > 0 else None
-    learned_b = time_batch(S, True) if S > 0 else None
-    clocks = clk.stop()
-    value = learned_b if S > 0 else learned_fps
-    base = plain_fps
-    bits_p, bits_l = sum(qp["bits"]), sum(ql["bits"])
-    if rank == 0:
-        cfg = workload_config()
-        cfg.update({"workload": ("learned proposal + batching" if S > 0 else "learned proposal") +
-                                f" on the 1080p stream ({S or 1} stream(s) x {nf} frames); top-K {args.topk}",
-                    "search": f"learned top-{args.topk} proposals, exact test, exhaustive fallback",
-                    "streams_per_gpu": S or 1,
-                    "train": {"frames": 200, "steps": args.train_steps, "batch_blocks": 4096,
-                              "candidates_per_block": 16, "optimizer": "AdamW lr 1e-3",
-                              "loss_first": round(losses[0], 4), "loss_last": round(losses[-1], 4),
-                              "seconds": round(train_s, 1)}})
-        line = dict(metric=METRIC, value=round(value, 3), unit="frames/s", n_gpus=world, steps=args.steps,
-                    warmup=args.warmup, ms_per_step=round(1000.0 * nf * (S or 1) / value, 3),
-                    higher_is_better=True, scaling="weak", vs_baseline=None, dtype="bf16+fp32+int32",
-                    data="synthetic", config=cfg, clocks=clocks,
-                    comparison={"plain_single_fps": round(plain_fps, 2), "learned_single_fps": round(learned_fps, 2),
-                                "plain_batched_fps": round(plain_b, 2) if plain_b else None,
-                                "learned_batched_fps": round(learned_b, 2) if learned_b else None,
-                                "speedup_vs_plain_single": round(value / base, 3),
-                                "psnr_plain_db": round(psnr_db(qp["sse"], W, H), 4),
-                                "psnr_learned_db": round(psnr_db(ql["sse"], W, H), 4),
-                                "psnr_delta_db": round(psnr_db(ql["sse"], W, H) - psnr_db(qp["sse"], W, H), 4),
-                                "motion_palette_bits_plain": int(bits_p), "motion_palette_bits_learned": int(bits_l),
-                                "motion_palette_bits_delta": round(bits_l / bits_p - 1.0, 5),
-                                "stream_frames": ns, "stream_padding": f"{W}x{H} edge-replicated to {pw}x{ph}",
-                                "stream_bytes_plain": bytes_p, "stream_bytes_learned": bytes_l,
-                                "stream_bytes_delta": round(bytes_l / bytes_p - 1.0, 5),
-                                "streams_decode_exactly": bool(exact_p and exact_l),
-                                "unique_blocks_plain": int(sum(qp["unique"])),
-                                "unique_blocks_learned": int(sum(ql["unique"])),
-                                "fallback_rate": round(ql["fallback"] / max(1, inter_blocks), 4)})
-        print(json.dumps(line), flush=True)
+    steps, warm = max(1, min(args.steps, 3)), max(1, min(args.warmup, 2))
+    learned_fps = time_stream_call(torch, learned_enc, frames_dev, sched, steps, warm)
+    S = args.batch if args.batch > 0 else 8
+    plain_b, tuned_p = time_batch(torch, frames_dev, S, None, K, steps, warm)
+    learned_b, tuned_l = time_batch(torch, frames_dev, S, model, K, steps, warm)
     plain_enc.close()
     learned_enc.close()
     model.close()
+    inter_blocks = sum(1 for f in sched if not f) * (W // 4) * (H // 4)
+    psnr_p, psnr_l = psnr_db(qp["sse"], W, H), psnr_db(ql["sse"], W, H)
+    bits_p, bits_l = sum(qp["bits"]), sum(ql["bits"])
+    return {
+        "method": f"top-{K} distinct window words scored by f(block).g(word) on the tensor cores, exact test of the "
+                  "K with the reference's selection rule, exhaustive search of the blocks none passes",
+        "topk": K, "streams_batched": S,
+        "plain_single_fps": round(plain_fps, 2), "learned_single_fps": round(learned_fps, 2),
+        "plain_batched_fps": round(plain_b, 2), "learned_batched_fps": round(learned_b, 2),
+        "speedup_learned_batched_vs_plain_single": round(learned_b / plain_fps, 3),
+        "speedup_learned_vs_plain_single_stream": round(learned_fps / plain_fps, 3),
+        "psnr_plain_db": round(psnr_p, 4), "psnr_learned_db": round(psnr_l, 4),
+        "psnr_delta_db": round(psnr_l - psnr_p, 4),
+        "motion_palette_bits_delta": round(bits_l / bits_p - 1.0, 5),
+        "stream_frames": ns, "stream_padding": f"{W}x{H} edge-replicated to {pw}x{ph}",
+        "stream_bytes_plain": bytes_p, "stream_bytes_learned": bytes_l,
+        "stream_bytes_delta": round(bytes_l / bytes_p - 1.0, 5),
+        "streams_decode_exactly": bool(exact_p and exact_l),
+        "fallback_rate": round(ql["fallback"] / max(1, inter_blocks), 4),
+        "gates": {"psnr_loss_le_0.1db": bool(psnr_p - psnr_l <= 0.1),
+                  "bytes_increase_le_2pct": bool(bytes_l <= 1.02 * bytes_p)},
+        "autotune": {"plain": tuned_p, "learned": tuned_l},
+        "train": {**tinfo, "frames_generated_s": round(gen_s, 1), "loss_first": round(losses[0], 4),
+                  "loss_last": round(float(np.mean(losses[-50:])), 4), "optimizer": "AdamW lr 1e-3 wd 1e-4"},
+    }
+
+
+def run_learned(args, rank: int, world: int, dist) -> None:
+    """Learned proposal + batching as the headline value: the same measurements
+    as the default run's `learned` object, printed as their own line."""
+    import torch
+
+    from mptc_gb300.encoder import Encoder
+    from mptc_gb300.synth import FHD1080
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nf = args.frames
+    frames_dev = torch.from_numpy(FHD1080.generate(0, nf)).to(dev)
+    sched = intra_schedule(nf, II)
+    enc = Encoder(W, H, SA, THR, II)
+    clk = ClockSampler(local)
+    plain_fps = time_stream_call(torch, enc, frames_dev, sched, max(1, min(args.steps, 3)), 2)
+    enc.close()
+    cmp_ = learned_comparison(args, torch, dev, frames_dev, plain_fps, log if rank == 0 else None)
+    clocks = clk.stop()
+    value = cmp_["learned_batched_fps"]
+    if rank == 0:
+        cfg = workload_config()
+        cfg.update({"workload": f"learned proposal + batching on the 1080p stream ({cmp_['streams_batched']} "
+                                f"streams x {nf} frames); top-K {cmp_['topk']}",
+                    "search": cmp_["method"], "streams_per_gpu": cmp_["streams_batched"]})
+        print(json.dumps(dict(metric=METRIC, value=round(value, 3), unit="frames/s", n_gpus=world, steps=args.steps,
+                              warmup=args.warmup, ms_per_step=round(1000.0 * nf * cmp_["streams_batched"] / value, 3),
+                              higher_is_better=True, scaling="weak", vs_baseline=None, dtype="bf16+fp32+int32",
+                              data="synthetic", config=cfg, clocks=clocks, learned=cmp_)), flush=True)
 
 
 def main() -> None:
@@ -733,7 +749,9 @@ def main() -> None:
                     help="S > 0: S concurrent 1080p streams per GPU through the batched encoder")
     ap.add_argument("--learned", action="store_true",
                     help="learned proposal: train on 200 separate seeded frames, then time plain vs learned")
-    ap.add_argument("--train-steps", type=int, default=600)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--no-learned", action="store_true",
+                    help="default run without the learned-proposal comparison")
     ap.add_argument("--topk", type=int, default=8)
     ap.add_argument("--quick", action="store_true",
                     help="device-timed region only: no e2e pass, CPU baseline or ALU probe (profiling)")

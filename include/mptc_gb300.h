@@ -216,14 +216,18 @@ mptc_status mptc_batch_autotune(mptc_batch *batch, const int32_t *is_intra, int3
                                 int32_t *intra_ctas, void *stream);
 
 /* ---- Learned candidate proposal (no counterpart in the reference) -------
- * A block MLP f (54 -> 256 -> 256 -> 64 over the 48 pixel bytes and the stb
- * endpoints) and a candidate MLP g (32 -> 128 -> 64 over an index word's bits)
- * score window candidates by f(block) . g(candidate). With a model attached,
- * the inter search tests only the K best-scored window positions with the
- * exact error (err_diff <= threshold) and falls back to the exhaustive search
- * when none passes; the stream stays a valid MPTC stream but is no longer
- * bit-identical to the reference's. BF16 tensor-core kernels, FP32 accumulate;
- * trained on the GPU with AdamW on (block, accepted candidate) pairs. */
+ * A block MLP f (54 -> 256 -> 256 -> 64 over the 48 pixel bytes, normalised
+ * per channel to the block's range, and the stb endpoints) and a candidate MLP
+ * g (32 -> 128 -> 64 over an index word's bits) score window candidates by
+ * f(block) . g(candidate). With a model attached, the inter search scores
+ * every window position on the tcgen05 tensor cores, tests only the K
+ * best-scored distinct index words exactly, applies the reference's selection
+ * rule to those K positions and accepts under the error threshold; a block
+ * none of whose K proposals passes goes to the exhaustive search. Every
+ * accepted block meets the reference's acceptance rule and the stream stays a
+ * valid MPTC stream, but it is no longer bit-identical to the reference's.
+ * BF16 operands, FP32 accumulate; trained on the GPU with AdamW on
+ * (block, accepted candidate) pairs. */
 typedef struct mptc_model mptc_model;
 int64_t mptc_model_num_params(void);
 mptc_status mptc_model_create(uint64_t seed, mptc_model **out_model);
@@ -251,11 +255,38 @@ mptc_status mptc_model_embed(mptc_model *model, const uint8_t *rgb_dev, int32_t 
 /* Checkpoint / resume: parameters, AdamW moments and step count. */
 mptc_status mptc_model_save(mptc_model *model, const char *path);
 mptc_status mptc_model_load(mptc_model *model, const char *path);
-/* Attaches (k in 1..16) or detaches (model NULL or k <= 0) a model to a
- * context's inter search. Needs search_area <= 12. */
+/* Attaches (k = 4, 8 or 16 proposals per block) or detaches (model NULL or
+ * k <= 0) a model to a context's inter search. Needs search_area <= 8. The
+ * context keeps a pointer: the model must outlive the attachment, and a
+ * training step between frames changes the proposals of later frames. */
 mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k);
+/* The learned proposal's window scoring of one inter frame on its own: the
+ * embeddings of the frame's blocks (rgb_dev, stb_dev) and of the previous
+ * frame's final blocks, then for every block the K best-scored distinct index
+ * words of its inter window (K of the attached model), best first, each at its
+ * first window position in the reference's scan order (row-major from
+ * (bx-sa, by-sa), codec/dxt_image.cpp:731-735); unused slots 0xFFFF.
+ * topk_dev: blocks x 16 u16. Synchronises `stream`. */
+mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev,
+                                   const uint64_t *prev_final_dev, uint16_t *topk_dev, void *stream);
+/* Candidate window rows staged per pipeline stage of the scoring kernel (4 or
+ * 8; the default 8): 8 rows make 256-candidate MMAs, one CTA per SM; 4 rows
+ * 128-candidate MMAs, two CTAs per SM. Results do not depend on it. */
+mptc_status mptc_ctx_set_learned_shape(mptc_ctx *ctx, int32_t rows_per_stage);
 /* Attaches (or detaches) a model to every stream of a batch. */
 mptc_status mptc_batch_set_model(mptc_batch *batch, const mptc_model *model, int32_t k);
+/* Exact err_diff of C candidate index words for each of B blocks of a frame:
+ * the refit, validity and error the inter search computes for a window
+ * candidate (CompressedBlock::RecalculateEndpoints + Error against the block's
+ * stb error, codec/dxt_image.cpp:258-349, as InterBlockSearch uses them,
+ * :739-757). blocks_dev: B block indices; cands_dev: B x C index words;
+ * err_dev: B x C int32, 2^31-1 where the refit would swap the endpoints (the
+ * reference skips such a candidate). The learned proposal's training examples
+ * are labelled with it. */
+mptc_status mptc_candidate_errors(const uint8_t *rgb_dev, int32_t width, int32_t height, const uint64_t *stb_dev,
+                                  const uint32_t *blocks_dev, const uint32_t *cands_dev, int32_t B, int32_t C,
+                                  int32_t *err_dev, void *stream);
+
 /* Squared error between a frame and the decoded DXT1 blocks (RGB565 endpoints
  * expanded as a decoder does), into *sse_dev (device u64). */
 mptc_status mptc_decoded_sse(const uint8_t *rgb_dev, int32_t width, int32_t height, const uint64_t *blocks_dev,

@@ -30,7 +30,8 @@ EXPORTED = [
     "mptc_model_grads", "mptc_model_embed", "mptc_model_save", "mptc_model_load",
     "mptc_ctx_set_model", "mptc_decoded_sse", "mptc_batch_set_model",
     "mptc_endpoint_coefficients", "mptc_decoder_create", "mptc_decoder_destroy", "mptc_decode_frame",
-    "mptc_decoder_check", "mptc_decoder_last_error", "mptc_kernel_launches",
+    "mptc_decoder_check", "mptc_decoder_last_error", "mptc_kernel_launches", "mptc_candidate_errors",
+    "mptc_learned_proposals", "mptc_ctx_set_learned_shape",
 ]
 
 NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
@@ -138,6 +139,9 @@ def lib() -> ctypes.CDLL:
         L.mptc_model_load.argtypes = [vp, ctypes.c_char_p]
         L.mptc_ctx_set_model.argtypes = [vp, vp, i32]
         L.mptc_decoded_sse.argtypes = [vp, i32, i32, vp, vp, vp]
+        L.mptc_learned_proposals.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.mptc_ctx_set_learned_shape.argtypes = [vp, i32]
+        L.mptc_candidate_errors.argtypes = [vp, i32, i32, vp, vp, vp, i32, i32, vp, vp]
         L.mptc_batch_set_model.argtypes = [vp, vp, i32]
         L.mptc_endpoint_coefficients.argtypes = [i32, i32, vp, vp, vp]
         L.mptc_decoder_create.argtypes = [i32, i32, i32, ctypes.POINTER(vp)]

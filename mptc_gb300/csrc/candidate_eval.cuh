@@ -4,13 +4,13 @@
 #pragma once
 #include <cstdint>
 
+#include "status_bits.cuh"
+
 namespace mptc {
 
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kInvalid = 0x7fffffff;  // invalid candidate / no selection (INT_MAX)
 
-// Device status bits (OR-ed into the context's status word).
-constexpr uint32_t kDevTimeout = 1u;
 
 // Staging of the block being searched (one per warp in the inter search, one
 // per CTA in the intra search).

@@ -109,26 +109,19 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
       }
 }
 
-// Block features: 48 pixel bytes / 255 and the stb endpoints (RGB565 ep1, ep2)
-// as 5/6/5-bit values / 31, 63, 31; zero padded to kFeatPad columns.
+// Block features (block_feature_half) of blocks[r] (NULL: block r), n rows of
+// kFeatPad bf16.
 __global__ void block_features_kernel(const uint8_t *__restrict__ rgb, int width, int bw, const uint64_t *__restrict__ stb,
                                       const uint32_t *__restrict__ blocks, int n, __nv_bfloat16 *__restrict__ X) {
-  const int total = n * kFeatPad;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const int r = e / kFeatPad, c = e % kFeatPad;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 2 * n; e += gridDim.x * blockDim.x) {
+    const int r = e >> 1, half = e & 1;
     const int idx = blocks ? (int)blocks[r] : r;
     const int by = idx / bw, bx = idx - by * bw;
-    float v = 0.f;
-    if (c < 48) {
-      const int p = c / 3, ch = c % 3;
-      v = rgb[((size_t)(4 * by + p / 4) * width + 4 * bx + p % 4) * 3 + ch] * (1.0f / 255.0f);
-    } else if (c < 54) {
-      const uint64_t b = stb[idx];
-      const uint32_t ep = (uint32_t)((c < 51 ? b : b >> 16) & 0xFFFF);
-      const int ch = (c - 48) % 3;
-      v = ch == 0 ? (ep >> 11) * (1.0f / 31.0f) : ch == 1 ? ((ep >> 5) & 63) * (1.0f / 63.0f) : (ep & 31) * (1.0f / 31.0f);
-    }
-    X[e] = __float2bfloat16(v);
+    uint32_t f[16];
+    block_feature_half(rgb, width, bx, by, stb[idx], half, f);
+    uint4 *dst = reinterpret_cast<uint4 *>(X + (size_t)r * kFeatPad + 32 * half);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) dst[j] = make_uint4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
   }
 }
 
@@ -154,6 +147,10 @@ __global__ void transpose_bf16_kernel(const float *__restrict__ x, int R, int C,
     const int r = i / C, c = i - r * C;
     y[(size_t)c * R + r] = __float2bfloat16(x[i]);
   }
+}
+
+__global__ void bf16_to_f32_kernel(const __nv_bfloat16 *__restrict__ x, float *__restrict__ y, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = __bfloat162float(x[i]);
 }
 
 __global__ void to_bf16_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ y, int n) {

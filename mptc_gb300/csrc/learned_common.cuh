@@ -6,11 +6,12 @@
 // reference's acceptance rule (err_diff <= threshold) and the stream stays a
 // valid MPTC stream.
 //
-// All matrix products run on the tensor cores through mma.sync m16n8k16 with
-// BF16 operands and FP32 accumulation, in forward, backward and scoring.
+// Inference (embeddings and window scoring, learned_tc.cuh) runs on the
+// tcgen05 tensor cores; the training step's matrix products (learned.cuh) use
+// mma.sync m16n8k16. Both take BF16 operands and accumulate in FP32.
 //
-// This header holds the sizes and the tensor-core helpers shared by the
-// training kernels (learned.cuh) and the scoring kernels (learned_search.cuh).
+// This header holds the sizes, the input features (the same for training and
+// inference) and the mma.sync helpers of the training kernels.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -21,6 +22,67 @@ namespace mptc {
 constexpr int kFeatIn = 54, kFeatPad = 64;  // block features, padded K
 constexpr int kH1 = 256, kH2 = 256, kEmb = 64;
 constexpr int kCandIn = 32, kCandH = 128;
+constexpr int kMaxK = 16;                  // proposals per block
+constexpr uint16_t kNoProposal = 0xFFFFu;  // empty top-K slot
+
+// Block features, half `half` (columns 32*half .. +31) as 16 packed bf16 pairs:
+// 48 pixel channels (p - lo_c) / (hi_c - lo_c) over the block's own channel
+// range (0 for a flat channel), the stb endpoints ep1, ep2 as r/31, g/63,
+// b/31, zero padding to 64.
+__device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ rgb, int width, int bx, int by,
+                                                   uint64_t stb, int half, uint32_t (&out)[16]) {
+  uint32_t w[12];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t *p = reinterpret_cast<const uint32_t *>(rgb + ((size_t)(4 * by + r) * width + 4 * bx) * 3);
+    w[3 * r] = __ldg(p);
+    w[3 * r + 1] = __ldg(p + 1);
+    w[3 * r + 2] = __ldg(p + 2);
+  }
+  auto byte = [&](int i) -> uint32_t { return (w[i >> 2] >> (8 * (i & 3))) & 0xFFu; };
+  uint32_t lo[3] = {255u, 255u, 255u}, hi[3] = {0u, 0u, 0u};
+#pragma unroll
+  for (int i = 0; i < 48; ++i) {
+    const uint32_t v = byte(i);
+    lo[i % 3] = min(lo[i % 3], v);
+    hi[i % 3] = max(hi[i % 3], v);
+  }
+  float inv[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) inv[c] = hi[c] > lo[c] ? 1.0f / (float)(hi[c] - lo[c]) : 0.0f;
+  const uint32_t e1 = (uint32_t)(stb & 0xFFFF), e2 = (uint32_t)((stb >> 16) & 0xFFFF);
+  float f[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const int i = 32 * half + j;
+    float v = 0.f;
+    if (i < 48) {
+      v = (float)(byte(i) - lo[i % 3]) * inv[i % 3];
+    } else if (i < 54) {
+      const uint32_t ep = i < 51 ? e1 : e2;
+      const int ch = (i - 48) % 3;
+      v = ch == 0 ? (float)(ep >> 11) * (1.0f / 31.0f)
+                  : ch == 1 ? (float)((ep >> 5) & 63) * (1.0f / 63.0f) : (float)(ep & 31) * (1.0f / 31.0f);
+    }
+    f[j] = v;
+  }
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const __nv_bfloat162 b = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
+    out[j] = *reinterpret_cast<const uint32_t *>(&b);
+  }
+}
+
+// Word features, half `half`: the 32 bits of an index word as 0/1 (half 0),
+// zero padding (half 1).
+__device__ __forceinline__ void word_feature_half(uint32_t word, int half, uint32_t (&out)[16]) {
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const uint32_t b0 = (word >> (2 * j)) & 1u, b1 = (word >> (2 * j + 1)) & 1u;
+    // bf16 1.0 = 0x3F80
+    out[j] = half ? 0u : (b0 ? 0x3F80u : 0u) | (b1 ? 0x3F800000u : 0u);
+  }
+}
 
 __device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
   return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);

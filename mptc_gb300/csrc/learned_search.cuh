@@ -1,6 +1,5 @@
-// Inference side of the learned proposal for the inter search: tile scoring
-// of every block against its window candidates on the tensor cores, top-K
-// selection, and the inter kernel that tests only the K proposals exactly.
+// Decoded-block squared error of a frame, the PSNR measure that compares the
+// learned proposal's output with the exhaustive search's.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -10,177 +9,6 @@
 #include "search.cuh"
 
 namespace mptc {
-
-constexpr int kMaxK = 16;                  // proposals per block
-constexpr uint16_t kNoProposal = 0xFFFFu;  // empty top-K slot
-
-// Score tile: 16 blocks (8 wide x 2 high) against the union of their inter
-// windows; scores[b, p] = F[b] . G[p] with BF16 mma.sync, FP32 accumulate.
-// Then each block keeps its K best window positions (scan index of the
-// reference's inter loop, rows j = by-sa.., columns i = bx-sa..), best first.
-// F: block embeddings of this frame, G: embeddings of the previous frame's
-// final blocks (both fp32, n x 64).
-constexpr int kTileW = 8, kTileH = 2;
-
-__global__ void __launch_bounds__(128) score_topk_kernel(const float *__restrict__ F, const float *__restrict__ G,
-                                                         int bw, int bh, int sa, int K,
-                                                         uint16_t *__restrict__ topk) {
-  extern __shared__ __align__(16) uint8_t dsm[];
-  const int uw = kTileW + 2 * sa - 1, uh = kTileH + 2 * sa - 1, nu = uw * uh;
-  const int nu8 = (nu + 7) & ~7;
-  __nv_bfloat16 *sG = reinterpret_cast<__nv_bfloat16 *>(dsm);                   // [nu8][64]
-  __nv_bfloat16 *sF = sG + (size_t)nu8 * kEmb;                                   // [16][64]
-  float *sS = reinterpret_cast<float *>(sF + 16 * kEmb);                         // [16][nu8]
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-  const int tx0 = blockIdx.x * kTileW, ty0 = blockIdx.y * kTileH;
-  const int ux0 = tx0 - sa, uy0 = ty0 - sa;  // union window origin
-  for (int e = tid; e < nu8 * kEmb; e += blockDim.x) {
-    const int p = e / kEmb, d = e % kEmb;
-    const int ui = p % uw, uj = p / uw, i = ux0 + ui, j = uy0 + uj;
-    float v = 0.f;
-    if (p < nu && i >= 0 && j >= 0 && i < bw && j < bh) v = G[((size_t)j * bw + i) * kEmb + d];
-    sG[e] = __float2bfloat16(v);
-  }
-  for (int e = tid; e < 16 * kEmb; e += blockDim.x) {
-    const int r = e / kEmb, d = e % kEmb, bx = tx0 + r % kTileW, by = ty0 + r / kTileW;
-    sF[e] = __float2bfloat16(bx < bw && by < bh ? F[((size_t)by * bw + bx) * kEmb + d] : 0.f);
-  }
-  __syncthreads();
-  // A fragments of the 16 x 64 block tile, shared by all n-tiles
-  uint32_t af[4][4];
-#pragma unroll
-  for (int ks = 0; ks < 4; ++ks) {
-    const int c = 16 * ks + 2 * t;
-    af[ks][0] = pack_bf16x2(sF[g * kEmb + c], sF[g * kEmb + c + 1]);
-    af[ks][1] = pack_bf16x2(sF[(g + 8) * kEmb + c], sF[(g + 8) * kEmb + c + 1]);
-    af[ks][2] = pack_bf16x2(sF[g * kEmb + c + 8], sF[g * kEmb + c + 9]);
-    af[ks][3] = pack_bf16x2(sF[(g + 8) * kEmb + c + 8], sF[(g + 8) * kEmb + c + 9]);
-  }
-  for (int nt = warp; nt < nu8 / 8; nt += 4) {
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    const int n = 8 * nt + g;
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-      const int c = 16 * ks + 2 * t;
-      const uint32_t bf[2] = {pack_bf16x2(sG[n * kEmb + c], sG[n * kEmb + c + 1]),
-                              pack_bf16x2(sG[n * kEmb + c + 8], sG[n * kEmb + c + 9])};
-      mma_bf16_16816(acc, af[ks], bf);
-    }
-    sS[g * nu8 + 8 * nt + 2 * t] = acc[0];
-    sS[g * nu8 + 8 * nt + 2 * t + 1] = acc[1];
-    sS[(g + 8) * nu8 + 8 * nt + 2 * t] = acc[2];
-    sS[(g + 8) * nu8 + 8 * nt + 2 * t + 1] = acc[3];
-  }
-  __syncthreads();
-  // top-K per block over its own window: warp w handles blocks w, w+4, ...
-  const int w2 = 2 * sa, npos = w2 * w2;
-  for (int r = warp; r < 16; r += 4) {
-    const int bx = tx0 + r % kTileW, by = ty0 + r / kTileW;
-    if (bx >= bw || by >= bh) continue;
-    const int ox = (r % kTileW), oy = (r / kTileW);  // block window origin inside the union
-    uint16_t *out = topk + ((size_t)by * bw + bx) * kMaxK;
-    uint32_t taken[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per-lane bitmask over its positions (<= 256 per lane)
-    for (int kk = 0; kk < K; ++kk) {
-      float best = -3.0e38f;
-      int bp = 0x7fffffff;
-      for (int pos = lane, q = 0; pos < npos; pos += 32, ++q) {
-        const int row = pos / w2, col = pos - row * w2;
-        const int i = bx - sa + col, j = by - sa + row;
-        if (i < 0 || j < 0 || i >= bw || j >= bh) continue;
-        if (q < 256 && ((taken[q >> 5] >> (q & 31)) & 1u)) continue;
-        const float v = sS[r * nu8 + (oy + row) * uw + (ox + col)];
-        if (v > best || (v == best && pos < bp)) {
-          best = v;
-          bp = pos;
-        }
-      }
-      // warp argmax (highest score, then lowest position)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(kFull, best, o);
-        const int op = __shfl_xor_sync(kFull, bp, o);
-        if (ov > best || (ov == best && op < bp)) {
-          best = ov;
-          bp = op;
-        }
-      }
-      if (lane == 0) out[kk] = bp == 0x7fffffff ? kNoProposal : (uint16_t)bp;
-      if (bp != 0x7fffffff && (bp & 31) == lane) {
-        const int q = bp >> 5;
-        if (q < 256) taken[q >> 5] |= 1u << (q & 31);
-      }
-    }
-    for (int kk = K + lane; kk < kMaxK; kk += 32) out[kk] = kNoProposal;
-  }
-}
-
-// Learned inter search: one warp per block. Lanes 0..K-1 test the K proposed
-// window positions with the exact integer error; the proposal with the
-// smallest err_diff <= 0 (ties: the better-scored) is accepted. When none is,
-// the warp runs the exhaustive inter search with the reference's selection
-// rule. Accepted blocks become final; the others are left for the intra pass.
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) learned_inter_kernel(SearchParams P, const uint16_t *__restrict__ topk,
-                                                                  int K, uint32_t *__restrict__ fallbacks) {
-  __shared__ BlockTab s_tab[WARPS];
-  __shared__ DedupTab s_dd[WARPS];
-  __shared__ uint8_t s_snap5[256], s_snap6[256];
-  build_snap_tables(s_snap5, s_snap6);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  BlockTab &tab = s_tab[warp];
-  const int nblk = P.bw * P.bh, w2 = 2 * P.sa;
-  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
-  for (int idx = blockIdx.x * WARPS + warp; idx < nblk; idx += gridDim.x * WARPS) {
-    const int by = idx / P.bw, bx = idx - by * P.bw;
-    const int sumsq = stage_block(tab, P.rgb, P.width, bx, by, lane);
-    const PixelGroups pg = load_groups(tab);
-    const uint64_t stb = P.stb[idx];
-    const uint32_t own = (uint32_t)(stb >> 32);
-    const int orig = P.orig_err[idx];
-    // proposals
-    int e = kInvalid, refit = 0, pos = -1;
-    uint32_t cand = 0, eps = 0;
-    if (lane < K) {
-      const uint16_t p = topk[(size_t)idx * kMaxK + lane];
-      if (p != kNoProposal) {
-        pos = p;
-        const int row = pos / w2, col = pos - row * w2;
-        const size_t nidx = (size_t)(by - P.sa + row) * P.bw + (bx - P.sa + col);
-        cand = __ldg(prev_hi + 2 * nidx);
-        const float4 d = __ldg(P.wdesc + nidx);
-        const WeightSums ws{d.x, d.y, d.z, d.w};
-        e = eval_candidate(tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
-      }
-    }
-    // A proposal is taken only when it is no worse than the block's own stb
-    // encoding (err_diff <= 0, the outcome the reference's search prefers); the
-    // others go to the exhaustive search, which keeps the decoded quality.
-    const bool pass = e != kInvalid && e <= 0 && e <= P.thr;
-    const int key = pass ? ((e + 0x10000) << 8) | lane : 0x7fffffff;  // min err_diff, then best score
-    const int best = __reduce_min_sync(kFull, key);
-    uint64_t word;
-    if (best != 0x7fffffff) {
-      const int who = best & 0xFF;
-      const int sel_pos = __shfl_sync(kFull, pos, who);
-      const uint32_t sel_cand = __shfl_sync(kFull, cand, who);
-      const uint32_t sel_eps = __shfl_sync(kFull, eps, who);
-      const int sel_refit = __shfl_sync(kFull, refit, who);
-      const uint64_t blk = sel_refit ? ((uint64_t)sel_eps | ((uint64_t)sel_cand << 32)) : stb;
-      if (lane == 0) {
-        const int row = sel_pos / w2, col = sel_pos - row * w2;
-        P.final_blk[idx] = blk;
-        P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
-      }
-      word = done_word(blk);
-    } else {
-      if (lane == 0) atomicAdd(fallbacks, 1u);
-      word = inter_block_search(P, tab, s_dd[warp], pg, s_snap5, s_snap6, idx, bx, by, stb, orig, sumsq, lane);
-    }
-    if (lane == 0) P.done[idx] = word;
-    __syncwarp();
-  }
-}
 
 // Decoded-stream squared error of a frame's final blocks (what a DXT1 decoder
 // shows: RGB565 endpoints expanded, 4-colour if ep1 > ep2, else 3-colour with

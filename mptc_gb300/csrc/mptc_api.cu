@@ -15,6 +15,7 @@
 #include "dxt1_encode.cuh"
 #include "search.cuh"
 #include "learned_search.cuh"
+#include "learned_tc.cuh"
 #include "model_internal.h"
 
 namespace {
@@ -42,12 +43,14 @@ struct mptc_ctx {
   int device = 0, sm_count = 0, intra_grid = 0;
   // launch shapes (tunable): warps per CTA of the inter search, CTA cap of the intra search
   int inter_warps = kSearchWarps, intra_cap = 0;
-  // learned proposal (optional)
+  // learned proposal (optional): K proposals per block, union rows per
+  // scoring stage (4 or 8), bf16 embeddings of this frame's blocks (F) and of
+  // the previous frame's final blocks (G), their TMA tensor maps, top-K lists
   const mptc_model *model = nullptr;
-  int topk_k = 0;
-  float *femb = nullptr, *gemb = nullptr;
+  int topk_k = 0, score_rows = 8;
+  __nv_bfloat16 *femb = nullptr, *gemb = nullptr;
   uint16_t *topk = nullptr;
-  mptc_internal::EmbedWorkspace ews;
+  CUtensorMap tm_f{}, tm_g4{}, tm_g8{};
   // device scratch
   uint64_t *done = nullptr;        // per block completion words
   // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count,
@@ -337,6 +340,104 @@ int launch_inter_search(const mptc::SearchParams &P, int warps, uint32_t *work, 
 
 }  // namespace
 
+namespace {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// Tensor map of an embedding buffer (bf16 [bh][bw][64]) for boxes of
+// box_w x box_h blocks, 128-byte swizzled, zero fill outside the frame.
+bool embedding_map(CUtensorMap *m, void *base, int bw, int bh, int box_w, int box_h) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)mptc::kEmb, (cuuint64_t)bw, (cuuint64_t)bh};
+  const cuuint64_t strides[2] = {(cuuint64_t)mptc::kEmb * 2, (cuuint64_t)bw * mptc::kEmb * 2};
+  const cuuint32_t box[3] = {(cuuint32_t)mptc::kEmb, (cuuint32_t)box_w, (cuuint32_t)box_h};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+// The scoring kernels' shared memory: ROWS = 8 stages use 512 TMEM columns and
+// ask for 120 KB (one CTA per SM); ROWS = 4 use 256 and ask for 80 KB (two).
+template <int ROWS>
+constexpr int score_smem() {
+  return (int)std::max<size_t>(mptc::score_smem_bytes<ROWS>(), ROWS == 8 ? 122880 : 81920);
+}
+
+template <int ROWS, int K>
+cudaError_t score_attr() {
+  return cudaFuncSetAttribute(mptc::score_topk_tc_kernel<ROWS, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              score_smem<ROWS>());
+}
+
+template <int ROWS, int K>
+void launch_score(mptc_ctx *ctx, const CUtensorMap &tg, const mptc::ScoreArgs &sa_, cudaStream_t s) {
+  const int tiles = ((ctx->bw + mptc::kScoreTileW - 1) / mptc::kScoreTileW) *
+                    ((ctx->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
+  const int grid = std::min(tiles, ctx->sm_count * (ROWS == 8 ? 1 : 2));
+  mptc::score_topk_tc_kernel<ROWS, K><<<grid, mptc::kScoreThreads, score_smem<ROWS>(), s>>>(ctx->tm_f, tg, sa_);
+}
+
+template <int K>
+void launch_eval(mptc_ctx *ctx, const mptc::SearchParams &P, cudaStream_t s) {
+  constexpr int WARPS = 4, BPW = 32 / K;
+  const int grid = std::min((ctx->nblk + WARPS * BPW - 1) / (WARPS * BPW), ctx->sm_count * 16);
+  mptc::learned_eval_kernel<K, WARPS><<<grid, WARPS * 32, 0, s>>>(P, ctx->topk, ctx->work + 6, ctx->pending);
+}
+
+// The learned inter search of one frame: g over the previous frame's final
+// words, f over this frame's blocks, window scoring with the top-K distinct
+// proposals, their exact test, and the exhaustive search of the blocks none
+// of whose proposals passed (listed in ctx->pending, counted in work[6]; the
+// list is consumed before the pending scan reuses the buffer). Returns the
+// number of kernels launched.
+int launch_learned_inter(mptc_ctx *ctx, const mptc::SearchParams &P, const uint8_t *rgb, const uint64_t *stb,
+                         const uint64_t *prev, cudaStream_t s) {
+  const int n = ctx->nblk;
+  mptc_internal::model_embed_words(ctx->model, reinterpret_cast<const uint32_t *>(prev) + 1, 2, n, ctx->gemb,
+                                   ctx->work + 1, s);
+  mptc_internal::model_embed_blocks(ctx->model, rgb, ctx->width, stb, nullptr, n, ctx->femb, ctx->work + 1, s);
+  mptc::ScoreArgs a{ctx->bw, ctx->bh, ctx->cfg.search_area, ctx->topk, ctx->work + 1};
+  const bool r8 = ctx->score_rows == 8;
+  const CUtensorMap &tg = r8 ? ctx->tm_g8 : ctx->tm_g4;
+  switch (ctx->topk_k) {
+    case 4:
+      r8 ? launch_score<8, 4>(ctx, tg, a, s) : launch_score<4, 4>(ctx, tg, a, s);
+      launch_eval<4>(ctx, P, s);
+      break;
+    case 16:
+      r8 ? launch_score<8, 16>(ctx, tg, a, s) : launch_score<4, 16>(ctx, tg, a, s);
+      launch_eval<16>(ctx, P, s);
+      break;
+    default:
+      r8 ? launch_score<8, 8>(ctx, tg, a, s) : launch_score<4, 8>(ctx, tg, a, s);
+      launch_eval<8>(ctx, P, s);
+      break;
+  }
+  mptc::inter_list_kernel<4><<<ctx->sm_count * 8, 4 * 32, 0, s>>>(P, ctx->pending, ctx->work + 6);
+  return 5;
+}
+
+}  // namespace
+
 extern "C" {
 
 int32_t mptc_version(void) { return 100; }
@@ -420,7 +521,6 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->femb);
   cudaFree(ctx->gemb);
   cudaFree(ctx->topk);
-  mptc_internal::embed_workspace_free(ctx->ews);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
   if (ctx->lane_b) mptc_ctx_destroy(ctx->lane_b);
@@ -483,20 +583,10 @@ mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t 
     mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
     // weight descriptors, the search (learned: embeddings, scoring, search),
     // pending compaction, sweep init + sweeps + dataflow fallback
-    ctx->launches += 1 + (ctx->model ? mptc_internal::kEmbedLaunches + 2 : 0) + 1;
+    ctx->launches += 2;  // weight descriptors, pending compaction
     KernelTimer t(ctx, K_INTER, s);
     if (ctx->model) {
-      // learned proposal: embeddings, top-K window positions, exact test of the K
-      mptc_status es = mptc_internal::model_embed_frame(ctx->model, ctx->ews, rgb_dev, ctx->width, stb_dev, ctx->nblk,
-                                                        ctx->femb, reinterpret_cast<const uint32_t *>(prev_final_dev) + 1,
-                                                        2, ctx->gemb, s);
-      if (es != MPTC_OK) return fail(ctx, es, "learned proposal: embedding failed");
-      const int sa = ctx->cfg.search_area, uw = mptc::kTileW + 2 * sa - 1, uh = mptc::kTileH + 2 * sa - 1;
-      const int nu8 = (uw * uh + 7) & ~7;
-      const size_t smem = (size_t)nu8 * mptc::kEmb * 2 + 16 * mptc::kEmb * 2 + (size_t)16 * nu8 * 4;
-      dim3 tg((ctx->bw + mptc::kTileW - 1) / mptc::kTileW, (ctx->bh + mptc::kTileH - 1) / mptc::kTileH);
-      mptc::score_topk_kernel<<<tg, 128, smem, s>>>(ctx->femb, ctx->gemb, ctx->bw, ctx->bh, sa, ctx->topk_k, ctx->topk);
-      mptc::learned_inter_kernel<4><<<(ctx->nblk + 3) / 4, 128, 0, s>>>(P, ctx->topk, ctx->topk_k, ctx->work + 6);
+      ctx->launches += launch_learned_inter(ctx, P, rgb_dev, stb_dev, prev_final_dev, s);
     } else {
       ctx->launches += launch_inter_search(P, ctx->inter_warps, ctx->work, ctx->pending, ctx->sm_count, s);
     }
@@ -896,22 +986,83 @@ mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k
     ctx->topk_k = 0;
     return MPTC_OK;
   }
-  if (k > mptc::kMaxK) return fail(ctx, MPTC_EINVAL, "learned proposal: k above 16");
-  if (ctx->cfg.search_area > 12) return fail(ctx, MPTC_EINVAL, "learned proposal: search area above 12");
+  if (k != 4 && k != 8 && k != 16) return fail(ctx, MPTC_EINVAL, "learned proposal: k must be 4, 8 or 16");
+  if (ctx->cfg.search_area > 8) return fail(ctx, MPTC_EINVAL, "learned proposal: search area above 8");
   const size_t n = (size_t)ctx->nblk;
   if (!ctx->femb) {
     if (dalloc(&ctx->femb, n * mptc::kEmb) || dalloc(&ctx->gemb, n * mptc::kEmb) || dalloc(&ctx->topk, n * mptc::kMaxK))
       return fail(ctx, MPTC_ENOMEM, "learned proposal buffers");
-    if (mptc_internal::embed_workspace_alloc(ctx->ews, ctx->nblk) != MPTC_OK)
-      return fail(ctx, MPTC_ENOMEM, "learned proposal workspace");
-    const int sa = ctx->cfg.search_area, uw = mptc::kTileW + 2 * sa - 1, uh = mptc::kTileH + 2 * sa - 1;
-    const int nu8 = (uw * uh + 7) & ~7;
-    const int smem = nu8 * mptc::kEmb * 2 + 16 * mptc::kEmb * 2 + 16 * nu8 * 4;
-    MPTC_CUDA(cudaFuncSetAttribute(mptc::score_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    if (!embedding_map(&ctx->tm_f, ctx->femb, ctx->bw, ctx->bh, mptc::kScoreTileW, mptc::kScoreTileH) ||
+        !embedding_map(&ctx->tm_g4, ctx->gemb, ctx->bw, ctx->bh, 32, 4) ||
+        !embedding_map(&ctx->tm_g8, ctx->gemb, ctx->bw, ctx->bh, 32, 8))
+      return fail(ctx, MPTC_ECUDA, "learned proposal: tensor map encoding failed");
+    MPTC_CUDA((score_attr<8, 4>()));
+    MPTC_CUDA((score_attr<8, 8>()));
+    MPTC_CUDA((score_attr<8, 16>()));
+    MPTC_CUDA((score_attr<4, 4>()));
+    MPTC_CUDA((score_attr<4, 8>()));
+    MPTC_CUDA((score_attr<4, 16>()));
   }
   ctx->model = model;
   ctx->topk_k = k;
   return MPTC_OK;
+}
+
+mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev,
+                                   const uint64_t *prev_final_dev, uint16_t *topk_dev, void *stream) {
+  if (!ctx) return MPTC_EINVAL;
+  if (!ctx->model) return fail(ctx, MPTC_ESTATE, "mptc_learned_proposals: no model attached");
+  if (!rgb_dev || !stb_dev || !prev_final_dev || !topk_dev || !aligned(rgb_dev, 4) || !aligned(stb_dev, 8) ||
+      !aligned(prev_final_dev, 8) || !aligned(topk_dev, 2))
+    return fail(ctx, MPTC_EINVAL, "mptc_learned_proposals: null or misaligned pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int n = ctx->nblk;
+  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, work_bytes(ctx->ntiles), s));
+  mptc_status st = mptc_internal::model_embed_words(ctx->model, reinterpret_cast<const uint32_t *>(prev_final_dev) + 1,
+                                                    2, n, ctx->gemb, ctx->work + 1, s);
+  if (st == MPTC_OK)
+    st = mptc_internal::model_embed_blocks(ctx->model, rgb_dev, ctx->width, stb_dev, nullptr, n, ctx->femb,
+                                           ctx->work + 1, s);
+  if (st != MPTC_OK) return fail(ctx, st, "mptc_learned_proposals: embedding launch failed");
+  mptc::ScoreArgs a{ctx->bw, ctx->bh, ctx->cfg.search_area, ctx->topk, ctx->work + 1};
+  const bool r8 = ctx->score_rows == 8;
+  const CUtensorMap &tg = r8 ? ctx->tm_g8 : ctx->tm_g4;
+  MPTC_CUDA(cudaMemsetAsync(ctx->topk, 0xFF, (size_t)n * mptc::kMaxK * sizeof(uint16_t), s));
+  switch (ctx->topk_k) {
+    case 4: r8 ? launch_score<8, 4>(ctx, tg, a, s) : launch_score<4, 4>(ctx, tg, a, s); break;
+    case 16: r8 ? launch_score<8, 16>(ctx, tg, a, s) : launch_score<4, 16>(ctx, tg, a, s); break;
+    default: r8 ? launch_score<8, 8>(ctx, tg, a, s) : launch_score<4, 8>(ctx, tg, a, s); break;
+  }
+  MPTC_CUDA(cudaGetLastError());
+  MPTC_CUDA(cudaMemcpyAsync(topk_dev, ctx->topk, (size_t)n * mptc::kMaxK * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s));
+  uint32_t status = 0;
+  MPTC_CUDA(cudaMemcpyAsync(&status, ctx->work + 1, 4, cudaMemcpyDeviceToHost, s));
+  MPTC_CUDA(cudaStreamSynchronize(s));
+  if (status & mptc::kDevTimeout) return fail(ctx, MPTC_ETIMEOUT, "device-side wait expired");
+  return MPTC_OK;
+}
+
+mptc_status mptc_ctx_set_learned_shape(mptc_ctx *ctx, int32_t rows_per_stage) {
+  if (!ctx) return MPTC_EINVAL;
+  if (rows_per_stage != 4 && rows_per_stage != 8) return fail(ctx, MPTC_EINVAL, "rows per stage must be 4 or 8");
+  ctx->score_rows = rows_per_stage;
+  return MPTC_OK;
+}
+
+mptc_status mptc_candidate_errors(const uint8_t *rgb_dev, int32_t width, int32_t height, const uint64_t *stb_dev,
+                                  const uint32_t *blocks_dev, const uint32_t *cands_dev, int32_t B, int32_t C,
+                                  int32_t *err_dev, void *stream) {
+  if (!rgb_dev || !stb_dev || !blocks_dev || !cands_dev || !err_dev || width <= 0 || height <= 0 || (width & 3) ||
+      (height & 3) || B < 0 || C < 1 || !aligned(rgb_dev, 4))
+    return MPTC_EINVAL;
+  if (B == 0) return MPTC_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || ensure_tables(dev) != cudaSuccess) return MPTC_ECUDA;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int grid = std::min((B + mptc::kErrWarps - 1) / mptc::kErrWarps, 4096);
+  mptc::candidate_errors_kernel<<<grid, mptc::kErrWarps * 32, 0, s>>>(rgb_dev, width, width / 4, stb_dev, blocks_dev,
+                                                                       cands_dev, B, C, err_dev);
+  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
 mptc_status mptc_decoded_sse(const uint8_t *rgb_dev, int32_t width, int32_t height, const uint64_t *blocks_dev,

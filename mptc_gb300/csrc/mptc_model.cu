@@ -1,6 +1,8 @@
 // Learned proposal model: parameters, training step (forward, sampled softmax
-// cross-entropy, backward, AdamW) and inference embeddings, all on the GPU in
-// the kernels of learned.cuh. C ABI in include/mptc_gb300.h.
+// cross-entropy, backward, AdamW; kernels of learned.cuh), the packed bf16
+// weight image the tensor-core inference kernels stage by TMA, and the
+// launchers of those embedding kernels (learned_tc.cuh). C ABI in
+// include/mptc_gb300.h.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -11,7 +13,10 @@
 #include <vector>
 
 #include "../../include/mptc_gb300.h"
+#include <mutex>
+
 #include "learned.cuh"
+#include "learned_embed.cuh"
 #include "model_internal.h"
 
 namespace {
@@ -67,6 +72,12 @@ struct mptc_model {
   float *df = nullptr, *dgg = nullptr, *dh1 = nullptr, *dh2 = nullptr, *dg1 = nullptr;
   bf16 *dfb = nullptr, *dggb = nullptr, *dh1b = nullptr, *dh2b = nullptr, *dg1b = nullptr;
   float *loss = nullptr;
+  // packed bf16 weight image of the inference kernels (refreshed after every
+  // parameter change) and a bf16 staging buffer for mptc_model_embed
+  uint8_t *img = nullptr;
+  __nv_bfloat16 *emb_tmp = nullptr;
+  int emb_cap = 0;
+  uint32_t *status = nullptr;
 };
 
 namespace {
@@ -180,7 +191,93 @@ mptc_status forward_backward(mptc_model *m, const uint8_t *rgb, int width, int b
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
+// Refreshes the packed bf16 weight image from the fp32 master weights.
+void repack(mptc_model *m, cudaStream_t s) {
+  const uint32_t img_off[5] = {mptc::kImgF1, mptc::kImgF2, mptc::kImgF3, mptc::kImgG1, mptc::kImgG2};
+  for (int l = 0; l < 5; ++l) {
+    const int kpad = (kLayers[l].in + 63) / 64 * 64;
+    mptc::pack_layer_kernel<<<blocks_for((size_t)kpad * kLayers[l].out), 256, 0, s>>>(
+        m->w + kOff.w[l], kLayers[l].in, kLayers[l].out, kpad, m->img + img_off[l]);
+  }
+}
+
+// Dynamic shared memory of the embedding kernels, set once per device. The f
+// kernel needs all but 2 KB of an SM's shared memory (one CTA per SM, its
+// 512 TMEM columns); the g kernel asks for 80 KB so that at most two CTAs
+// (256 TMEM columns each) share an SM.
+constexpr int kMaxDev = 64;
+std::mutex g_attr_mu;
+bool g_attr_done[kMaxDev] = {};
+constexpr size_t kSmemF = mptc::embed_smem_bytes<mptc::NetF>();
+constexpr size_t kSmemG = mptc::embed_smem_bytes<mptc::NetG>() > 81920 ? mptc::embed_smem_bytes<mptc::NetG>() : 81920;
+
+cudaError_t ensure_embed_attrs() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDev) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_attr_mu);
+  if (g_attr_done[dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(mptc::embed_kernel<mptc::NetF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kSmemF);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(mptc::embed_kernel<mptc::NetG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kSmemG);
+  if (e == cudaSuccess) g_attr_done[dev] = true;
+  return e;
+}
+
+int sm_count_now() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
 }  // namespace
+
+namespace mptc_internal {
+
+mptc_status model_embed_blocks(const mptc_model *m, const uint8_t *rgb, int width, const uint64_t *stb,
+                               const uint32_t *blocks, int n, __nv_bfloat16 *F, uint32_t *status, cudaStream_t s) {
+  if (!m || n <= 0) return MPTC_EINVAL;
+  if (ensure_embed_attrs() != cudaSuccess) return MPTC_ECUDA;
+  mptc::EmbedArgs a{};
+  a.rgb = rgb;
+  a.width = width;
+  a.bw = width / 4;
+  a.n = n;
+  a.stb = stb;
+  a.blocks = blocks;
+  a.wimg = m->img;
+  a.b1 = m->w + kOff.b[0];
+  a.b2 = m->w + kOff.b[1];
+  a.b3 = m->w + kOff.b[2];
+  a.out = F;
+  a.status = status ? status : m->status;
+  const int tiles = (n + 127) / 128;
+  mptc::embed_kernel<mptc::NetF, true><<<std::min(tiles, sm_count_now()), mptc::kEmbedThreads, kSmemF, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
+}
+
+mptc_status model_embed_words(const mptc_model *m, const uint32_t *words, int word_stride, int n, __nv_bfloat16 *G,
+                              uint32_t *status, cudaStream_t s) {
+  if (!m || n <= 0) return MPTC_EINVAL;
+  if (ensure_embed_attrs() != cudaSuccess) return MPTC_ECUDA;
+  mptc::EmbedArgs a{};
+  a.n = n;
+  a.words = words;
+  a.word_stride = word_stride;
+  a.wimg = m->img;
+  a.b1 = m->w + kOff.b[3];
+  a.b2 = m->w + kOff.b[4];
+  a.out = G;
+  a.status = status ? status : m->status;
+  const int tiles = (n + 127) / 128;
+  mptc::embed_kernel<mptc::NetG, false><<<std::min(tiles, 2 * sm_count_now()), mptc::kEmbedThreads, kSmemG, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
+}
+
+}  // namespace mptc_internal
 
 extern "C" {
 
@@ -193,7 +290,8 @@ mptc_status mptc_model_create(uint64_t seed, mptc_model **out) {
   if (!m) return MPTC_ENOMEM;
   const size_t n = kOff.total;
   if (dmalloc(&m->w, n) || dmalloc(&m->wb, n) || dmalloc(&m->g, n) || dmalloc(&m->m, n) || dmalloc(&m->v, n) ||
-      dmalloc(&m->loss, 1)) {
+      dmalloc(&m->loss, 1) || dmalloc(&m->img, mptc::kImgBytes) || dmalloc(&m->status, 1) ||
+      cudaMemset(m->img, 0, mptc::kImgBytes) != cudaSuccess || cudaMemset(m->status, 0, 4) != cudaSuccess) {
     mptc_model_destroy(m);
     return MPTC_ENOMEM;
   }
@@ -231,6 +329,9 @@ mptc_status mptc_model_destroy(mptc_model *m) {
   cudaFree(m->m);
   cudaFree(m->v);
   cudaFree(m->loss);
+  cudaFree(m->img);
+  cudaFree(m->emb_tmp);
+  cudaFree(m->status);
   delete m;
   return MPTC_OK;
 }
@@ -240,6 +341,7 @@ mptc_status mptc_model_set_params(mptc_model *m, const float *host) {
   const size_t n = kOff.total;
   if (cudaMemcpy(m->w, host, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return MPTC_ECUDA;
   mptc::to_bf16_kernel<<<blocks_for(n), 256>>>(m->w, m->wb, (int)n);
+  repack(m, nullptr);
   return cudaDeviceSynchronize() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
@@ -282,6 +384,7 @@ mptc_status mptc_model_train_step(mptc_model *m, const uint8_t *rgb_dev, int32_t
   const size_t n = kOff.total;
   mptc::adamw_kernel<<<blocks_for(n), 256, 0, s>>>(m->w, m->wb, m->g, m->m, m->v, (int)n, lr, b1, b2, 1e-8f,
                                                    weight_decay, c1, c2);
+  repack(m, s);
   if (cudaGetLastError() != cudaSuccess) return MPTC_ECUDA;
   if (loss_host) {
     if (cudaMemcpyAsync(loss_host, m->loss, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -330,97 +433,45 @@ mptc_status mptc_model_load(mptc_model *m, const char *path) {
   return MPTC_OK;
 }
 
-// Embeddings for inference and tests: F = f(block features) for `n` blocks
-// (blocks_dev NULL = all blocks of the frame in raster order), G = g(words).
+// Embeddings through the inference kernels (tcgen05, bf16 out) converted to
+// fp32: F = f(block features) for `n_blocks` blocks (blocks_dev NULL = the
+// first n_blocks blocks in raster order), G = g(words).
 mptc_status mptc_model_embed(mptc_model *m, const uint8_t *rgb_dev, int32_t width, const uint64_t *stb_dev,
                              const uint32_t *blocks_dev, int32_t n_blocks, float *emb_blocks_dev,
                              const uint32_t *words_dev, int32_t word_stride, int32_t n_words, float *emb_words_dev,
                              void *stream) {
-  if (!m || (n_blocks > 0 && (!rgb_dev || !stb_dev || !emb_blocks_dev)) || (n_words > 0 && (!words_dev || !emb_words_dev)))
+  if (!m || (n_blocks > 0 && (!rgb_dev || !stb_dev || !emb_blocks_dev || width <= 0 || (width & 3))) ||
+      (n_words > 0 && (!words_dev || !emb_words_dev || word_stride < 1)))
     return MPTC_EINVAL;
-  using namespace mptc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int B = n_blocks > 0 ? n_blocks : 0, BC = n_words > 0 ? n_words : 0;
-  mptc_status st = ensure_ws(m, B > 0 ? B : 1, BC > 0 ? BC : 1);
-  if (st != MPTC_OK) return st;
-  const bf16 *W[5];
-  const float *b[5];
-  for (int l = 0; l < 5; ++l) {
-    W[l] = m->wb + kOff.w[l];
-    b[l] = m->w + kOff.b[l];
+  const int need = std::max(n_blocks, n_words);
+  if (need <= 0) return MPTC_OK;
+  if (need > m->emb_cap) {
+    cudaFree(m->emb_tmp);
+    m->emb_tmp = nullptr;
+    m->emb_cap = 0;
+    if (dmalloc(&m->emb_tmp, (size_t)need * mptc::kEmb)) return MPTC_ENOMEM;
+    m->emb_cap = need;
   }
-  if (B > 0) {
-    block_features_kernel<<<blocks_for((size_t)B * kFeatPad), 256, 0, s>>>(rgb_dev, width, width / 4, stb_dev,
-                                                                           blocks_dev, B, m->x);
-    gemm_fwd(m->x, W[0], b[0], m->h1, m->h1b, B, kFeatPad, kH1, true, s);
-    gemm_fwd(m->h1b, W[1], b[1], m->h2, m->h2b, B, kH1, kH2, true, s);
-    gemm_fwd(m->h2b, W[2], b[2], emb_blocks_dev, nullptr, B, kH2, kEmb, false, s);
+  if (cudaMemsetAsync(m->status, 0, 4, s) != cudaSuccess) return MPTC_ECUDA;
+  mptc_status st = MPTC_OK;
+  if (n_blocks > 0) {
+    st = mptc_internal::model_embed_blocks(m, rgb_dev, width, stb_dev, blocks_dev, n_blocks, m->emb_tmp, nullptr, s);
+    if (st != MPTC_OK) return st;
+    mptc::bf16_to_f32_kernel<<<blocks_for((size_t)n_blocks * mptc::kEmb), 256, 0, s>>>(m->emb_tmp, emb_blocks_dev,
+                                                                                      n_blocks * mptc::kEmb);
   }
-  if (BC > 0) {
-    cand_features_kernel<<<blocks_for((size_t)BC * kCandIn), 256, 0, s>>>(words_dev, word_stride, BC, m->xc);
-    gemm_fwd(m->xc, W[3], b[3], m->g1, m->g1b, BC, kCandIn, kCandH, true, s);
-    gemm_fwd(m->g1b, W[4], b[4], emb_words_dev, nullptr, BC, kCandH, kEmb, false, s);
+  if (n_words > 0) {
+    st = mptc_internal::model_embed_words(m, words_dev, word_stride, n_words, m->emb_tmp, nullptr, s);
+    if (st != MPTC_OK) return st;
+    mptc::bf16_to_f32_kernel<<<blocks_for((size_t)n_words * mptc::kEmb), 256, 0, s>>>(m->emb_tmp, emb_words_dev,
+                                                                                     n_words * mptc::kEmb);
   }
-  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
+  uint32_t flag = 0;
+  if (cudaMemcpyAsync(&flag, m->status, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return MPTC_ECUDA;
+  return flag ? MPTC_ETIMEOUT : (cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA);
 }
 
 }  // extern "C"
-
-namespace mptc_internal {
-
-mptc_status embed_workspace_alloc(EmbedWorkspace &ws, int rows) {
-  using namespace mptc;
-  embed_workspace_free(ws);
-  const size_t r = (size_t)rows;
-  if (dmalloc(&ws.x, r * kFeatPad) || dmalloc(&ws.h1b, r * kH1) || dmalloc(&ws.h2b, r * kH2) ||
-      dmalloc(&ws.h1, r * kH1) || dmalloc(&ws.h2, r * kH2) || dmalloc(&ws.wt, kOff.total)) {
-    embed_workspace_free(ws);
-    return MPTC_ENOMEM;
-  }
-  ws.cap = rows;
-  return MPTC_OK;
-}
-
-void embed_workspace_free(EmbedWorkspace &ws) {
-  cudaFree(ws.x);
-  cudaFree(ws.h1b);
-  cudaFree(ws.h2b);
-  cudaFree(ws.h1);
-  cudaFree(ws.h2);
-  cudaFree(ws.wt);
-  ws = EmbedWorkspace{};
-}
-
-mptc_status model_embed_frame(const mptc_model *m, EmbedWorkspace &ws, const uint8_t *rgb, int width,
-                              const uint64_t *stb, int n, float *F, const uint32_t *words, int word_stride,
-                              float *G, cudaStream_t s) {
-  using namespace mptc;
-  if (!m || n > ws.cap) return MPTC_EINVAL;
-  // transposed bf16 weights ([out x in]) so both GEMM operands load as
-  // contiguous 16-byte vectors along k
-  const bf16 *Wt[5];
-  const float *b[5];
-  for (int l = 0; l < 5; ++l) {
-    const size_t cnt = (size_t)kLayers[l].in * kLayers[l].out;
-    transpose_bf16_kernel<<<blocks_for(cnt), 256, 0, s>>>(m->w + kOff.w[l], kLayers[l].in, kLayers[l].out,
-                                                          ws.wt + kOff.w[l]);
-    Wt[l] = ws.wt + kOff.w[l];
-    b[l] = m->w + kOff.b[l];
-  }
-  auto fwd = [&](const bf16 *x, int l, float *y, bf16 *yb, bool relu) {
-    const int K = kLayers[l].in, N = kLayers[l].out;
-    dim3 grid((N + kGBN - 1) / kGBN, (n + kGBM - 1) / kGBM);
-    gemm_bf16_kernel<false, true><<<grid, 128, 0, s>>>(x, K, Wt[l], K, y, yb, N, b[l], n, N, K, relu ? 1 : 0, 0);
-  };
-  block_features_kernel<<<blocks_for((size_t)n * kFeatPad), 256, 0, s>>>(rgb, width, width / 4, stb, nullptr, n, ws.x);
-  fwd(ws.x, 0, ws.h1, ws.h1b, true);
-  fwd(ws.h1b, 1, ws.h2, ws.h2b, true);
-  fwd(ws.h2b, 2, F, nullptr, false);
-  // candidate MLP: reuse x (n x 32 fits in n x 64) and h1 (n x 128 fits in n x 256)
-  cand_features_kernel<<<blocks_for((size_t)n * kCandIn), 256, 0, s>>>(words, word_stride, n, ws.x);
-  fwd(ws.x, 3, ws.h1, ws.h1b, true);
-  fwd(ws.h1b, 4, G, nullptr, false);
-  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
-}
-
-}  // namespace mptc_internal
