@@ -446,8 +446,8 @@ def run_batch(args, rank: int, world: int, dist) -> None:
         for k in range(S):
             b.upload(k, frames_dev[(f + offsets[k]) % nf], stream)
         b.encode(flags(f), stream)
-    warps, ctas = b.autotune(flags(2), stream)
-    log(f"[rank {rank}] autotune: inter warps/CTA {warps}, intra CTAs/stream {ctas or 'all'}")
+    tuned = b.autotune(flags(2), stream)
+    log(f"[rank {rank}] autotune: {tuned}")
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -470,7 +470,7 @@ def run_batch(args, rank: int, world: int, dist) -> None:
         cfg = workload_config()
         cfg.update({"workload": f"batched 1080p MPTC encode: {S} concurrent streams x {nf} frames",
                     "streams_per_gpu": S, "intra_phase": "stream k: 16k/S",
-                    "autotune": {"inter_warps_per_cta": warps, "intra_ctas_per_stream": ctas or "all"}})
+                    "autotune": tuned})
         print(json.dumps(dict(metric=METRIC, value=round(value, 3), unit="frames/s", n_gpus=world,
                               steps=args.steps, warmup=args.warmup,
                               ms_per_step=round(elapsed_ms / args.steps, 3), higher_is_better=True,
@@ -644,8 +644,8 @@ def learned_comparison(args, torch, dev, frames_dev, plain_fps, log):
     the bytes of whole MPTC streams of the first 32 frames (edge-padded to
     256-pixel multiples, decoded back bit-exactly on the GPU)."""
     from mptc_gb300.encoder import Encoder
-    from mptc_gb300.synth import FHD1080_TRAIN
-    from mptc_gb300.training import train_proposal
+    from mptc_gb300.synth import FHD1080_CALIB, FHD1080_TRAIN
+    from mptc_gb300.training import choose_topk, train_proposal
     t0 = time.time()
     train_dev = torch.from_numpy(FHD1080_TRAIN.generate()).to(dev)
     gen_s = time.time() - t0
@@ -653,9 +653,14 @@ def learned_comparison(args, torch, dev, frames_dev, plain_fps, log):
                                           cands=32, lr=1e-3, log=log)
     del train_dev
     torch.cuda.empty_cache()
+    # K: given, or the fastest that stays within half the PSNR budget on
+    # separate calibration frames, judged by the exhaustive search
+    calib = torch.from_numpy(FHD1080_CALIB.generate()).to(dev)
+    K, k_table = choose_topk(torch, model, calib, SA, THR, II, ks=(args.topk,) if args.topk > 0 else (4, 8, 16),
+                             log=log)
+    del calib
     nf = frames_dev.shape[0]
     sched = intra_schedule(nf, II)
-    K = args.topk
     plain_enc = Encoder(W, H, SA, THR, II)
     learned_enc = Encoder(W, H, SA, THR, II)
     learned_enc.set_model(model, K)
@@ -684,7 +689,9 @@ def learned_comparison(args, torch, dev, frames_dev, plain_fps, log):
     return {
         "method": f"top-{K} distinct window words scored by f(block).g(word) on the tensor cores, exact test of the "
                   "K with the reference's selection rule, exhaustive search of the blocks none passes",
-        "topk": K, "streams_batched": S,
+        "topk": K, "topk_calibration": {str(k): {"psnr_loss_db": v[0], "ms_per_frame": v[1], "fallback": v[2]}
+                                         for k, v in k_table.items()},
+        "streams_batched": S,
         "plain_single_fps": round(plain_fps, 2), "learned_single_fps": round(learned_fps, 2),
         "plain_batched_fps": round(plain_b, 2), "learned_batched_fps": round(learned_b, 2),
         "speedup_learned_batched_vs_plain_single": round(learned_b / plain_fps, 3),
@@ -719,6 +726,24 @@ def run_learned(args, rank: int, world: int, dist) -> None:
     nf = args.frames
     frames_dev = torch.from_numpy(FHD1080.generate(0, nf)).to(dev)
     sched = intra_schedule(nf, II)
+    if args.quick:
+        # profiling: an untrained model of the same shapes, kernel times of the
+        # learned stream call only (no training, quality or batch runs)
+        from mptc_gb300.model import ProposalModel
+        model = ProposalModel(seed=1)
+        enc = Encoder(W, H, SA, THR, II)
+        enc.set_model(model, args.topk or 8)
+        fps = time_stream_call(torch, enc, frames_dev, sched, max(1, args.steps), max(1, args.warmup))
+        enc.set_kernel_timing(True)
+        time_stream_call(torch, enc, frames_dev, sched, 1, 0)
+        enc.set_kernel_timing(False)
+        kt = enc.kernel_times()
+        if rank == 0:
+            print(json.dumps(dict(quick=True, learned=True, frames=nf, value=round(fps, 2), kernels={
+                k: {"launches": v[0], "total_ms": round(v[1], 3)} for k, v in kt.items()})), flush=True)
+        enc.close()
+        model.close()
+        return
     enc = Encoder(W, H, SA, THR, II)
     clk = ClockSampler(local)
     plain_fps = time_stream_call(torch, enc, frames_dev, sched, max(1, min(args.steps, 3)), 2)
@@ -752,7 +777,8 @@ def main() -> None:
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--no-learned", action="store_true",
                     help="default run without the learned-proposal comparison")
-    ap.add_argument("--topk", type=int, default=8)
+    ap.add_argument("--topk", type=int, default=0,
+                    help="proposals per block (4, 8, 16); 0 = chosen on calibration frames")
     ap.add_argument("--quick", action="store_true",
                     help="device-timed region only: no e2e pass, CPU baseline or ALU probe (profiling)")
     args = ap.parse_args()

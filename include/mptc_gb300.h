@@ -210,10 +210,16 @@ mptc_status mptc_batch_fetch(mptc_batch *batch, int32_t i, uint64_t *final_host,
 mptc_status mptc_batch_encode(mptc_batch *batch, const int32_t *is_intra, void *stream);
 /* Autotuner: times the candidate launch shapes on the current inputs and the
  * given intra/inter pattern (without advancing the streams) and keeps the
- * fastest: warps per CTA of the inter search (2, 4) and the CTA count of
- * each stream's intra search. Writes the chosen values (synchronises). */
+ * fastest: warps (blocks) per CTA of the exhaustive inter search (2, 4; with a
+ * model attached the current value is kept), the CTA count of each stream's
+ * intra dataflow (all, 8, 4, 2 or 1 per SM) and, with a model attached, the
+ * candidate rows per pipeline stage of the window scoring (4 or 8). Writes the
+ * chosen values (any pointer may be NULL; synchronises). The number of
+ * proposals K is set with the model (mptc_batch_set_model): it changes the
+ * encoder's output, so it is chosen against the exhaustive search's quality,
+ * not by time alone. */
 mptc_status mptc_batch_autotune(mptc_batch *batch, const int32_t *is_intra, int32_t *inter_warps,
-                                int32_t *intra_ctas, void *stream);
+                                int32_t *intra_ctas, int32_t *score_rows, void *stream);
 
 /* ---- Learned candidate proposal (no counterpart in the reference) -------
  * A block MLP f (54 -> 256 -> 256 -> 64 over the 48 pixel bytes, normalised

@@ -124,7 +124,7 @@ def lib() -> ctypes.CDLL:
         L.mptc_batch_upload.argtypes = [vp, i32, vp, vp]
         L.mptc_batch_fetch.argtypes = [vp, i32, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32), vp]
         L.mptc_batch_encode.argtypes = [vp, vp, vp]
-        L.mptc_batch_autotune.argtypes = [vp, vp, ctypes.POINTER(i32), ctypes.POINTER(i32), vp]
+        L.mptc_batch_autotune.argtypes = [vp, vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32), vp]
         fp = ctypes.POINTER(ctypes.c_float)
         L.mptc_model_num_params.restype = ctypes.c_int64
         L.mptc_model_create.argtypes = [ctypes.c_uint64, ctypes.POINTER(vp)]

@@ -81,12 +81,15 @@ class BatchEncoder:
         check(lib().mptc_batch_encode(self._b, arr, s))
         return flags
 
-    def autotune(self, is_intra: list[bool], stream=None) -> tuple[int, int]:
+    def autotune(self, is_intra: list[bool], stream=None) -> dict:
+        """Times the launch shapes on the current inputs and keeps the fastest;
+        returns the chosen inter warps per CTA, intra CTAs per stream (0: all)
+        and scoring rows per stage."""
         arr = (ctypes.c_int32 * self.n)(*[int(bool(f)) for f in is_intra])
-        w, c = ctypes.c_int32(0), ctypes.c_int32(0)
+        w, c, r = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
-        check(lib().mptc_batch_autotune(self._b, arr, ctypes.byref(w), ctypes.byref(c), s))
-        return w.value, c.value
+        check(lib().mptc_batch_autotune(self._b, arr, ctypes.byref(w), ctypes.byref(c), ctypes.byref(r), s))
+        return {"inter_warps_per_cta": w.value, "intra_ctas_per_stream": c.value, "score_rows_per_stage": r.value}
 
     def fetch(self, i: int, stream=None):
         n = self.nblk(i)

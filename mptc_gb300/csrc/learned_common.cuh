@@ -22,6 +22,7 @@ namespace mptc {
 constexpr int kFeatIn = 54, kFeatPad = 64;  // block features, padded K
 constexpr int kH1 = 256, kH2 = 256, kEmb = 64;
 constexpr int kCandIn = 32, kCandH = 128;
+constexpr int kMaxBatch = 32;              // streams (jobs) one learned-proposal launch covers
 constexpr int kMaxK = 16;                  // proposals per block
 constexpr uint16_t kNoProposal = 0xFFFFu;  // empty top-K slot
 

@@ -56,6 +56,17 @@ struct EmbedArgs {
   uint32_t *status;         // device status word (kDevTimeout on an expired wait)
 };
 
+// A launch covers the rows of up to kMaxBatch jobs (the streams of a batch,
+// or one): tiles of 128 rows are numbered across the jobs (job j owns tiles
+// [tile_end[j-1], tile_end[j])) and CTAs take them from one counter, so
+// streams of uneven resolution share the persistent grid.
+struct EmbedBatch {
+  int n;                     // jobs
+  int tile_end[kMaxBatch];   // inclusive prefix of the jobs' tile counts
+  EmbedArgs a[kMaxBatch];
+  uint32_t *next;            // tile counter (zero before the launch)
+};
+
 // The f network (three layers, TMEM 512 columns: acc1 [0,256), acc2
 // [256,512), acc3 [0,64)) and the g network (two layers, TMEM 256 columns:
 // acc1 [0,128), acc2 [128,192)).
@@ -114,7 +125,7 @@ __device__ __forceinline__ void issue_chunk(uint32_t d_tmem, const uint8_t *a_ti
 // issues the MMAs. Chunk kc of a hidden layer goes to operand buffer kc%2, so
 // the epilogue of chunk kc+1 overlaps the MMAs of chunk kc.
 template <class Net, bool kBlocks>
-__global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(EmbedArgs a) {
+__global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_constant__ EmbedBatch batch) {
   extern __shared__ uint8_t dsm[];
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(dsm) + 1023) & ~uintptr_t(1023));
   uint8_t *sW = sm;
@@ -122,6 +133,7 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(EmbedArgs a) {
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm + Net::kWBytes + 2 * kTileBytes);  // weights, mma, buf0, buf1
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
   volatile uint32_t *abort_flag = tslot + 1;
+  volatile int *s_tile = reinterpret_cast<volatile int *>(tslot + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = warp & 3, h = warp >> 2;
   if (tid == 0) {
     for (int i = 0; i < 4; ++i) tc::mbar_init(bar + i, 1);
@@ -136,7 +148,7 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(EmbedArgs a) {
   if (tid == 0) {
     tc::mbar_arrive_expect_tx(bar, Net::kWBytes);
     for (uint32_t o = 0; o < Net::kWBytes; o += 32768)
-      tc::bulk_g2s(sW + o, a.wimg + Net::kW + o, min(32768u, Net::kWBytes - o), bar);
+      tc::bulk_g2s(sW + o, batch.a[0].wimg + Net::kW + o, min(32768u, Net::kWBytes - o), bar);
   }
   if (!tc::mbar_wait(bar, 0, abort_flag)) *abort_flag = 1;
   uint32_t ph_mma = 0, ph_buf[2] = {0, 0};
@@ -146,9 +158,16 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(EmbedArgs a) {
   };
   const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
   const int row = 32 * q + lane;
-  const int ntiles = (a.n + 127) / 128;
-  __syncthreads();
-  for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x) {
+  const int total = batch.tile_end[batch.n - 1];
+  for (;;) {
+    if (tid == 0) *s_tile = (int)atomicAdd(batch.next, 1u);
+    __syncthreads();
+    const int gt = *s_tile;
+    if (gt >= total || *abort_flag) break;
+    int j = 0;
+    while (gt >= batch.tile_end[j]) ++j;
+    const EmbedArgs &a = batch.a[j];
+    const int tile = gt - (j ? batch.tile_end[j - 1] : 0);
     // input features -> sA[0]
     {
       const int r = tid >> 1, half = tid & 1, gi = tile * 128 + r;
@@ -251,7 +270,8 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(EmbedArgs a) {
   __syncthreads();
   tc::tc_fence_after();
   if (warp == 0) tc::tmem_free(tmem, Net::kTmem);
-  if (tid == 0 && *abort_flag) atomicOr(a.status, kDevTimeout);
+  if (tid == 0 && *abort_flag)
+    for (int j = 0; j < batch.n; ++j) atomicOr(batch.a[j].status, kDevTimeout);
 }
 
 

@@ -40,6 +40,17 @@ struct ScoreArgs {
   uint32_t *status;  // device status word
 };
 
+// A launch covers the frames of up to kMaxBatch jobs (the streams of a
+// batch, or one): score tiles are numbered across the jobs and CTAs take them
+// from one counter. Job j's embeddings are reached through its tensor maps.
+struct ScoreBatch {
+  int n;
+  int tile_end[kMaxBatch];
+  ScoreArgs a[kMaxBatch];
+  CUtensorMap tmF[kMaxBatch], tmG[kMaxBatch];
+  uint32_t *next;  // tile counter (zero before the launch)
+};
+
 template <int K>
 __device__ __forceinline__ void topk_insert(float (&s)[K], int (&p)[K], float v, int pos) {
   if (!(v > s[K - 1])) return;
@@ -69,8 +80,7 @@ constexpr size_t score_smem_bytes() {
 }
 
 template <int ROWS, int K>
-__global__ void __launch_bounds__(kScoreThreads, 1)
-    score_topk_tc_kernel(const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmG, ScoreArgs a) {
+__global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const __grid_constant__ ScoreBatch batch) {
   constexpr int N = 32 * ROWS;
   constexpr uint32_t kGBytes = (uint32_t)N * 128u;
   extern __shared__ uint8_t dsm[];
@@ -80,6 +90,7 @@ __global__ void __launch_bounds__(kScoreThreads, 1)
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kTileBytes + 2 * kGBytes);  // F, G0, G1, M0, M1
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 5);
   volatile uint32_t *abort_flag = tslot + 1;
+  volatile int *s_tile = reinterpret_cast<volatile int *>(tslot + 2);
   const int tid = threadIdx.x, warp = tid >> 5;
   if (tid == 0) {
     for (int i = 0; i < 5; ++i) tc::mbar_init(bar + i, 1);
@@ -92,8 +103,6 @@ __global__ void __launch_bounds__(kScoreThreads, 1)
   tc::tc_fence_after();
   const uint32_t tmem = *tslot;
   const uint32_t lane_base = tmem + ((uint32_t)(32 * warp) << 16);
-  const int sa = a.sa, w2 = 2 * sa, U = kScoreTileH + w2 - 1, nst = (U + ROWS - 1) / ROWS;
-  const int tiles_x = (a.bw + kScoreTileW - 1) / kScoreTileW, tiles_y = (a.bh + kScoreTileH - 1) / kScoreTileH;
   const int r = tid >> 4, c = tid & 15;    // this thread's block inside the tile
   const int wr0 = 2 * warp;                // the warp's first tile row; its window rows span wr0 .. wr0 + w2
   const uint32_t idesc = tc::idesc_bf16(128, N);
@@ -102,15 +111,27 @@ __global__ void __launch_bounds__(kScoreThreads, 1)
     if (!tc::mbar_wait(b, ph, abort_flag)) *abort_flag = 1;
     ph ^= 1;
   };
-  for (int tile = blockIdx.x; tile < tiles_x * tiles_y && !*abort_flag; tile += gridDim.x) {
+  const int total = batch.tile_end[batch.n - 1];
+  for (;;) {
+    if (tid == 0) *s_tile = (int)atomicAdd(batch.next, 1u);
+    __syncthreads();
+    const int gt = *s_tile;
+    if (gt >= total || *abort_flag) break;
+    int jb = 0;
+    while (gt >= batch.tile_end[jb]) ++jb;
+    const ScoreArgs &a = batch.a[jb];
+    const CUtensorMap *tmF = &batch.tmF[jb], *tmG = &batch.tmG[jb];
+    const int tile = gt - (jb ? batch.tile_end[jb - 1] : 0);
+    const int sa = a.sa, w2 = 2 * sa, U = kScoreTileH + w2 - 1, nst = (U + ROWS - 1) / ROWS;
+    const int tiles_x = (a.bw + kScoreTileW - 1) / kScoreTileW;
     const int ty0 = (tile / tiles_x) * kScoreTileH, tx0 = (tile % tiles_x) * kScoreTileW;
     const int bx = tx0 + c, by = ty0 + r;
     if (tid == 0) {
       tc::mbar_arrive_expect_tx(bar, kTileBytes);
-      tc::tma_load_3d(sF, &tmF, 0, tx0, ty0, bar);
+      tc::tma_load_3d(sF, tmF, 0, tx0, ty0, bar);
       for (int s = 0; s < 2 && s < nst; ++s) {
         tc::mbar_arrive_expect_tx(bar + 1 + s, kGBytes);
-        tc::tma_load_3d(sG[s], &tmG, 0, tx0 - sa, ty0 - sa + s * ROWS, bar + 1 + s);
+        tc::tma_load_3d(sG[s], tmG, 0, tx0 - sa, ty0 - sa + s * ROWS, bar + 1 + s);
       }
       wait(bar, ph_f);
       wait(bar + 1, ph_g[0]);
@@ -151,7 +172,7 @@ __global__ void __launch_bounds__(kScoreThreads, 1)
         }
         if (s + 2 < nst) {  // stage s's MMA is done: its G buffer takes stage s + 2
           tc::mbar_arrive_expect_tx(bar + 1 + b, kGBytes);
-          tc::tma_load_3d(sG[b], &tmG, 0, tx0 - sa, ty0 - sa + (s + 2) * ROWS, bar + 1 + b);
+          tc::tma_load_3d(sG[b], tmG, 0, tx0 - sa, ty0 - sa + (s + 2) * ROWS, bar + 1 + b);
         }
       }
       // union rows of this stage that meet the warp's window rows
@@ -181,7 +202,8 @@ __global__ void __launch_bounds__(kScoreThreads, 1)
   __syncthreads();
   tc::tc_fence_after();
   if (warp == 0) tc::tmem_free(tmem, 2 * N);
-  if (tid == 0 && *abort_flag) atomicOr(a.status, kDevTimeout);
+  if (tid == 0 && *abort_flag)
+    for (int j = 0; j < batch.n; ++j) atomicOr(batch.a[j].status, kDevTimeout);
 }
 
 // ---- exact test of the proposals -------------------------------------------------
@@ -193,19 +215,34 @@ __global__ void __launch_bounds__(kScoreThreads, 1)
 // minimum) runs over the K proposal positions in closed form. A block whose
 // selection passes the threshold becomes final with the reference's inter
 // motion code; the others are listed for the exhaustive search.
+// The frames of up to kMaxBatch jobs per launch: job j owns the block groups
+// [group_end[j-1], group_end[j]) (a group: the 32/K blocks of one warp pass).
+struct EvalBatch {
+  int n;
+  int group_end[kMaxBatch];
+  SearchParams P[kMaxBatch];
+  const uint16_t *topk[kMaxBatch];
+  uint32_t *fb_count[kMaxBatch];  // zeroed fallback counter
+  uint32_t *fb_list[kMaxBatch];   // room for every block of the frame
+};
+
 template <int K, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) learned_eval_kernel(SearchParams P, const uint16_t *__restrict__ topk,
-                                                                  uint32_t *__restrict__ fb_count,
-                                                                  uint32_t *__restrict__ fb_list) {
+__global__ void __launch_bounds__(WARPS * 32) learned_eval_kernel(const __grid_constant__ EvalBatch batch) {
   constexpr int BPW = 32 / K;
   __shared__ BlockTab s_tab[WARPS][BPW];
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   build_snap_tables(s_snap5, s_snap6);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, slot = lane / K, k = lane % K;
-  const int nblk = P.bw * P.bh, w2 = 2 * P.sa;
-  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
-  for (int base = (blockIdx.x * WARPS + warp) * BPW; base < nblk; base += gridDim.x * WARPS * BPW) {
+  const int total = batch.group_end[batch.n - 1];
+  for (int gg = blockIdx.x * WARPS + warp; gg < total; gg += gridDim.x * WARPS) {
+    int jb = 0;
+    while (gg >= batch.group_end[jb]) ++jb;
+    const SearchParams &P = batch.P[jb];
+    const uint16_t *__restrict__ topk = batch.topk[jb];
+    const int nblk = P.bw * P.bh, w2 = 2 * P.sa;
+    const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
+    const int base = (gg - (jb ? batch.group_end[jb - 1] : 0)) * BPW;
     int sumsq = 0;
 #pragma unroll
     for (int jj = 0; jj < BPW; ++jj) {
@@ -276,7 +313,7 @@ __global__ void __launch_bounds__(WARPS * 32) learned_eval_kernel(SearchParams P
     }
     if (valid && !accept && k == 0) {
       P.done[idx] = 0;
-      fb_list[atomicAdd(fb_count, 1u)] = (uint32_t)idx;
+      batch.fb_list[jb][atomicAdd(batch.fb_count[jb], 1u)] = (uint32_t)idx;
     }
     __syncwarp();
   }
@@ -284,17 +321,30 @@ __global__ void __launch_bounds__(WARPS * 32) learned_eval_kernel(SearchParams P
 
 // The exhaustive inter search (InterBlockSearch, codec/dxt_image.cpp:715-774)
 // of the listed blocks, one warp per block.
+struct ListBatch {
+  int n;
+  SearchParams P[kMaxBatch];
+  const uint32_t *list[kMaxBatch];
+  const uint32_t *count[kMaxBatch];
+};
+
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) inter_list_kernel(SearchParams P, const uint32_t *__restrict__ list,
-                                                                const uint32_t *__restrict__ count) {
+__global__ void __launch_bounds__(WARPS * 32) inter_list_kernel(const __grid_constant__ ListBatch batch) {
   __shared__ BlockTab s_tab[WARPS];
   __shared__ DedupTab s_dd[WARPS];
   __shared__ uint8_t s_snap5[256], s_snap6[256];
   build_snap_tables(s_snap5, s_snap6);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int n = (int)*count;
-  for (int k = blockIdx.x * WARPS + warp; k < n; k += gridDim.x * WARPS) {
+  // the jobs' lists one after the other, every warp of the grid on each
+  int off = 0;
+  for (int jb = 0; jb < batch.n; ++jb) {
+  const SearchParams &P = batch.P[jb];
+  const uint32_t *__restrict__ list = batch.list[jb];
+  const int n = (int)*batch.count[jb];
+  const int start = (blockIdx.x * WARPS + warp - off % (gridDim.x * WARPS) + gridDim.x * WARPS) % (gridDim.x * WARPS);
+  off += n;
+  for (int k = start; k < n; k += gridDim.x * WARPS) {
     const int idx = (int)list[k];
     const int by = idx / P.bw, bx = idx - by * P.bw;
     const int sumsq = stage_block(s_tab[warp], P.rgb, P.width, bx, by, lane);
@@ -303,6 +353,7 @@ __global__ void __launch_bounds__(WARPS * 32) inter_list_kernel(SearchParams P, 
                                              P.stb[idx], P.orig_err[idx], sumsq, lane);
     if (lane == 0) P.done[idx] = word;
     __syncwarp();
+  }
   }
 }
 

@@ -5,17 +5,34 @@
 #include <cuda_runtime.h>
 
 #include "../../include/mptc_gb300.h"
+#include "learned_common.cuh"
 
 namespace mptc_internal {
 
-// Tensor-core embeddings (bf16, n x 64, row-major) with the model's current
-// weights: the f network over the frame's blocks (blocks NULL = blocks 0 ..
-// n-1 in raster order; width a multiple of 4, the frame 4-byte aligned) and
-// the g network over index words (words[i * word_stride]). An expired
-// device-side wait ORs kDevTimeout into *status (NULL: the model's own word).
-mptc_status model_embed_blocks(const mptc_model *m, const uint8_t *rgb, int width, const uint64_t *stb,
-                               const uint32_t *blocks, int n, __nv_bfloat16 *F, uint32_t *status, cudaStream_t s);
-mptc_status model_embed_words(const mptc_model *m, const uint32_t *words, int word_stride, int n, __nv_bfloat16 *G,
-                              uint32_t *status, cudaStream_t s);
+// One embedding job: the f network over `n` blocks of a frame (rgb, width a
+// multiple of 4, 4-byte aligned frame; stb endpoints; blocks NULL = blocks
+// 0 .. n-1 in raster order) or the g network over n index words
+// (words[i * word_stride]); bf16 output n x 64. An expired device-side wait
+// ORs kDevTimeout into *status.
+struct EmbedJob {
+  const uint8_t *rgb = nullptr;
+  int width = 0;
+  const uint64_t *stb = nullptr;
+  const uint32_t *blocks = nullptr;
+  const uint32_t *words = nullptr;
+  int word_stride = 1;
+  int n = 0;
+  __nv_bfloat16 *out = nullptr;
+  uint32_t *status = nullptr;
+};
+
+// Jobs a single embedding launch takes (the streams of a batch).
+constexpr int kMaxEmbedJobs = mptc::kMaxBatch;
+
+// One persistent launch of the f (blocks = true) or g network over up to
+// kMaxEmbedJobs jobs with the model's current weights; `next` is a zeroed
+// device counter the launch's CTAs draw tiles from.
+mptc_status model_embed(const mptc_model *m, bool blocks, const EmbedJob *jobs, int n_jobs, uint32_t *next,
+                        cudaStream_t s);
 
 }  // namespace mptc_internal

@@ -40,7 +40,7 @@ size_t work_bytes(int ntiles) { return (kWorkWords + 4 * (size_t)ntiles) * sizeo
 struct mptc_ctx {
   mptc_config cfg{};
   int width = 0, height = 0, bw = 0, bh = 0, nblk = 0, ntiles = 0;
-  int device = 0, sm_count = 0, intra_grid = 0;
+  int device = 0, sm_count = 0, intra_grid = 0, intra_warp_grid = 0;
   // launch shapes (tunable): warps per CTA of the inter search, CTA cap of the intra search
   int inter_warps = kSearchWarps, intra_cap = 0;
   // learned proposal (optional): K proposals per block, union rows per
@@ -216,13 +216,18 @@ mptc::SearchParams make_params(mptc_ctx *ctx, const uint8_t *rgb, const uint64_t
   return P;
 }
 
-enum KernelId { K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE, K_COUNT };
+enum KernelId {
+  K_DXT1 = 0, K_INTER, K_INTRA, K_PENDING, K_UNIQUE,
+  K_EMBED_G, K_EMBED_F, K_SCORE, K_EVAL, K_FALLBACK, K_COUNT
+};
 // inter_search: the inter search kernels of an inter frame (inter_run_kernel
 // and inter_overflow_kernel at sa <= 8, inter_dedup_kernel above; the
 // learned proposal's kernels when a model is attached)
 const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_search",
                                      "intra_search_kernel",     "intra_sweep_kernel/inter_frame",
-                                     "unique_scan_kernel"};
+                                     "unique_scan_kernel",      "embed_kernel/g",
+                                     "embed_kernel/f",          "score_topk_tc_kernel",
+                                     "learned_eval_kernel",     "inter_list_kernel"};
 
 cudaEvent_t pool_event(mptc_ctx *ctx) {
   if (ctx->ev_used == ctx->ev_pool.size()) {
@@ -389,51 +394,193 @@ cudaError_t score_attr() {
 }
 
 template <int ROWS, int K>
-void launch_score(mptc_ctx *ctx, const CUtensorMap &tg, const mptc::ScoreArgs &sa_, cudaStream_t s) {
-  const int tiles = ((ctx->bw + mptc::kScoreTileW - 1) / mptc::kScoreTileW) *
-                    ((ctx->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
-  const int grid = std::min(tiles, ctx->sm_count * (ROWS == 8 ? 1 : 2));
-  mptc::score_topk_tc_kernel<ROWS, K><<<grid, mptc::kScoreThreads, score_smem<ROWS>(), s>>>(ctx->tm_f, tg, sa_);
+void launch_score(const mptc::ScoreBatch &sb, int sm_count, cudaStream_t s) {
+  const int grid = std::min(sb.tile_end[sb.n - 1], sm_count * (ROWS == 8 ? 1 : 2));
+  mptc::score_topk_tc_kernel<ROWS, K><<<grid, mptc::kScoreThreads, score_smem<ROWS>(), s>>>(sb);
 }
 
 template <int K>
-void launch_eval(mptc_ctx *ctx, const mptc::SearchParams &P, cudaStream_t s) {
-  constexpr int WARPS = 4, BPW = 32 / K;
-  const int grid = std::min((ctx->nblk + WARPS * BPW - 1) / (WARPS * BPW), ctx->sm_count * 16);
-  mptc::learned_eval_kernel<K, WARPS><<<grid, WARPS * 32, 0, s>>>(P, ctx->topk, ctx->work + 6, ctx->pending);
+void launch_eval(const mptc::EvalBatch &eb, int sm_count, cudaStream_t s) {
+  constexpr int WARPS = 4;
+  const int grid = std::min((eb.group_end[eb.n - 1] + WARPS - 1) / WARPS, sm_count * 16);
+  mptc::learned_eval_kernel<K, WARPS><<<grid, WARPS * 32, 0, s>>>(eb);
 }
 
-// The learned inter search of one frame: g over the previous frame's final
-// words, f over this frame's blocks, window scoring with the top-K distinct
-// proposals, their exact test, and the exhaustive search of the blocks none
-// of whose proposals passed (listed in ctx->pending, counted in work[6]; the
-// list is consumed before the pending scan reuses the buffer). Returns the
+// One inter frame of a context with a model attached: its frame and the
+// search parameters of the frame.
+struct LearnedJob {
+  mptc_ctx *ctx;
+  mptc::SearchParams P;
+};
+
+// The learned inter search of up to kMaxBatch frames (one per context; the
+// contexts share one model, K and stage shape), each phase one persistent
+// launch over all of them: g over the previous frames' final words, f over
+// the frames' blocks, the window scoring with the top-K distinct proposals,
+// their exact test, and the exhaustive search of the blocks none of whose
+// proposals passed (listed in ctx->pending, counted in work[6]; the list is
+// consumed before the pending scan reuses the buffer). `counters`: three
+// zeroed words the embedding and scoring launches draw tiles from. Returns the
 // number of kernels launched.
-int launch_learned_inter(mptc_ctx *ctx, const mptc::SearchParams &P, const uint8_t *rgb, const uint64_t *stb,
-                         const uint64_t *prev, cudaStream_t s) {
-  const int n = ctx->nblk;
-  mptc_internal::model_embed_words(ctx->model, reinterpret_cast<const uint32_t *>(prev) + 1, 2, n, ctx->gemb,
-                                   ctx->work + 1, s);
-  mptc_internal::model_embed_blocks(ctx->model, rgb, ctx->width, stb, nullptr, n, ctx->femb, ctx->work + 1, s);
-  mptc::ScoreArgs a{ctx->bw, ctx->bh, ctx->cfg.search_area, ctx->topk, ctx->work + 1};
-  const bool r8 = ctx->score_rows == 8;
-  const CUtensorMap &tg = r8 ? ctx->tm_g8 : ctx->tm_g4;
-  switch (ctx->topk_k) {
-    case 4:
-      r8 ? launch_score<8, 4>(ctx, tg, a, s) : launch_score<4, 4>(ctx, tg, a, s);
-      launch_eval<4>(ctx, P, s);
-      break;
-    case 16:
-      r8 ? launch_score<8, 16>(ctx, tg, a, s) : launch_score<4, 16>(ctx, tg, a, s);
-      launch_eval<16>(ctx, P, s);
-      break;
-    default:
-      r8 ? launch_score<8, 8>(ctx, tg, a, s) : launch_score<4, 8>(ctx, tg, a, s);
-      launch_eval<8>(ctx, P, s);
-      break;
+int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream_t s) {
+  mptc_ctx *c0 = jobs[0].ctx;
+  mptc_internal::EmbedJob ej[mptc::kMaxBatch];
+  for (int j = 0; j < n; ++j) {
+    mptc_ctx *c = jobs[j].ctx;
+    ej[j] = mptc_internal::EmbedJob{};
+    ej[j].words = reinterpret_cast<const uint32_t *>(jobs[j].P.prev) + 1;
+    ej[j].word_stride = 2;
+    ej[j].n = c->nblk;
+    ej[j].out = c->gemb;
+    ej[j].status = c->work + 1;
   }
-  mptc::inter_list_kernel<4><<<ctx->sm_count * 8, 4 * 32, 0, s>>>(P, ctx->pending, ctx->work + 6);
+  {
+    KernelTimer t(c0, K_EMBED_G, s);
+    mptc_internal::model_embed(c0->model, false, ej, n, counters, s);
+  }
+  for (int j = 0; j < n; ++j) {
+    mptc_ctx *c = jobs[j].ctx;
+    ej[j] = mptc_internal::EmbedJob{};
+    ej[j].rgb = jobs[j].P.rgb;
+    ej[j].width = c->width;
+    ej[j].stb = jobs[j].P.stb;
+    ej[j].n = c->nblk;
+    ej[j].out = c->femb;
+    ej[j].status = c->work + 1;
+  }
+  {
+    KernelTimer t(c0, K_EMBED_F, s);
+    mptc_internal::model_embed(c0->model, true, ej, n, counters + 1, s);
+  }
+  mptc::ScoreBatch sb{};
+  sb.n = n;
+  sb.next = counters + 2;
+  mptc::EvalBatch eb{};
+  eb.n = n;
+  mptc::ListBatch lb{};
+  lb.n = n;
+  const bool r8 = c0->score_rows == 8;
+  const int bpw = 32 / c0->topk_k;
+  int tiles = 0, groups = 0;
+  for (int j = 0; j < n; ++j) {
+    mptc_ctx *c = jobs[j].ctx;
+    tiles += ((c->bw + mptc::kScoreTileW - 1) / mptc::kScoreTileW) *
+             ((c->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
+    sb.tile_end[j] = tiles;
+    sb.a[j] = mptc::ScoreArgs{c->bw, c->bh, c->cfg.search_area, c->topk, c->work + 1};
+    sb.tmF[j] = c->tm_f;
+    sb.tmG[j] = r8 ? c->tm_g8 : c->tm_g4;
+    groups += (c->nblk + bpw - 1) / bpw;
+    eb.group_end[j] = groups;
+    eb.P[j] = jobs[j].P;
+    eb.topk[j] = c->topk;
+    eb.fb_count[j] = c->work + 6;
+    eb.fb_list[j] = c->pending;
+    lb.P[j] = jobs[j].P;
+    lb.list[j] = c->pending;
+    lb.count[j] = c->work + 6;
+  }
+  const int sms = c0->sm_count;
+  {
+    KernelTimer t(c0, K_SCORE, s);
+    switch (c0->topk_k) {
+      case 4: r8 ? launch_score<8, 4>(sb, sms, s) : launch_score<4, 4>(sb, sms, s); break;
+      case 16: r8 ? launch_score<8, 16>(sb, sms, s) : launch_score<4, 16>(sb, sms, s); break;
+      default: r8 ? launch_score<8, 8>(sb, sms, s) : launch_score<4, 8>(sb, sms, s); break;
+    }
+  }
+  {
+    KernelTimer t(c0, K_EVAL, s);
+    switch (c0->topk_k) {
+      case 4: launch_eval<4>(eb, sms, s); break;
+      case 16: launch_eval<16>(eb, sms, s); break;
+      default: launch_eval<8>(eb, sms, s); break;
+    }
+  }
+  {
+    KernelTimer t(c0, K_FALLBACK, s);
+    mptc::inter_list_kernel<4><<<sms * 8, 4 * 32, 0, s>>>(lb);
+  }
   return 5;
+}
+
+// CTAs of the warp-per-block intra dataflow: the context's cap counts blocks
+// in flight (CTAs of the CTA-per-block kernel), here warps, rounded up to
+// whole CTAs; uncapped, one CTA per SM (8 blocks in flight per SM, far more
+// than the ~bw/sa blocks of the wavefront).
+int intra_warp_ctas(const mptc_ctx *ctx) {
+  const int want = ctx->intra_cap > 0 ? (ctx->intra_cap + mptc::kIntraWarps - 1) / mptc::kIntraWarps : ctx->sm_count;
+  return std::max(1, std::min(want, ctx->intra_warp_grid));
+}
+
+mptc_status reencode_check(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev,
+                           const int32_t *orig_err_dev, const uint64_t *prev_final_dev, const uint64_t *final_dev,
+                           const uint8_t *motion_dev, const uint32_t *unique_dev, const uint32_t *n_unique_dev) {
+  if (!ctx) return MPTC_EINVAL;
+  if (!rgb_dev || !stb_dev || !orig_err_dev || !final_dev || !motion_dev || !unique_dev || !n_unique_dev)
+    return fail(ctx, MPTC_EINVAL, "mptc_reencode: null pointer");
+  if (!aligned(rgb_dev, 16) || !aligned(stb_dev, 8) || !aligned(final_dev, 8) || !aligned(motion_dev, 2) ||
+      (prev_final_dev && !aligned(prev_final_dev, 8)) || !aligned(orig_err_dev, 4) || !aligned(unique_dev, 4))
+    return fail(ctx, MPTC_EINVAL, "mptc_reencode: misaligned pointer");
+  if (prev_final_dev == final_dev) return fail(ctx, MPTC_EINVAL, "mptc_reencode: prev and final alias");
+  return MPTC_OK;
+}
+
+// First part of a reencode: the per-frame work area; an inter frame's refit
+// weight sums of the previous frame's blocks, an intra frame's zeroed
+// completion words.
+mptc_status reencode_begin(mptc_ctx *ctx, const mptc::SearchParams &P, cudaStream_t s) {
+  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, work_bytes(ctx->ntiles), s));
+  if (P.prev) {
+    mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(P.prev, ctx->nblk, ctx->wdesc);
+    ctx->launches += 2;  // weight descriptors; the pending compaction follows the search
+  } else {
+    MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint64_t), s));
+  }
+  MPTC_CUDA(cudaGetLastError());
+  return MPTC_OK;
+}
+
+// Last part, after the inter search: an inter frame's pending compaction and
+// intra pass (sweeps + exact fallback), an intra frame's dataflow; the unique
+// palette.
+mptc_status reencode_finish(mptc_ctx *ctx, const mptc::SearchParams &P, uint32_t *unique_dev, uint32_t *n_unique_dev,
+                            cudaStream_t s) {
+  const uint64_t *prev_final_dev = P.prev;
+  if (prev_final_dev) {
+    // pending = blocks the inter pass left open, in wavefront order, with
+    // the sweeps' first estimates and change flags
+    const int sw = sweep_count(ctx->cfg.intra_sweeps);
+    mptc::pending_scan_kernel<<<ctx->ntiles, 256, 0, s>>>(
+        ctx->order, ctx->done, P.stb, ctx->nblk, ctx->ntiles, ctx->tile_state, ctx->work + 10, ctx->pending,
+        ctx->work + 5, ctx->sweep, ctx->sweep + 3 * (size_t)ctx->nblk, sw ? sw + 1 : 0, ctx->work + 1);
+  }
+  {
+    KernelTimer t(ctx, prev_final_dev ? K_PENDING : K_INTRA, s);
+    const int ig = ctx->intra_cap > 0 ? std::min(ctx->intra_cap, ctx->intra_grid) : ctx->intra_grid;
+    if (prev_final_dev)
+      ctx->launches += launch_intra_sweeps(P, ctx->pending, ctx->work + 5, ctx->sweep, ctx->nblk, ig,
+                                           sweep_count(ctx->cfg.intra_sweeps), ctx->sweep_part,
+                                           std::min(ctx->nblk, kSweepPartCap), s);
+    else if (ctx->cfg.search_area <= 8)
+      mptc::intra_warp_kernel<mptc::kIntraWarps><<<intra_warp_ctas(ctx), mptc::kIntraWarps * 32, 0, s>>>(
+          P, ctx->order, nullptr, ctx->nblk);
+    else
+      mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
+    if (!prev_final_dev) ++ctx->launches;
+  }
+  MPTC_CUDA(cudaGetLastError());
+  const uint16_t *m16 = P.motion;
+  {
+    KernelTimer t(ctx, K_UNIQUE, s);
+    mptc::unique_scan_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, P.stb, ctx->nblk, ctx->ntiles,
+                                                        ctx->tile_state + ctx->ntiles, ctx->work + 11, unique_dev,
+                                                        n_unique_dev, ctx->work + 2, ctx->work + 1);
+    ++ctx->launches;
+  }
+  MPTC_CUDA(cudaGetLastError());
+  ctx->last_is_intra = prev_final_dev ? 0u : 1u;
+  return MPTC_OK;
 }
 
 }  // namespace
@@ -482,6 +629,11 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
                                                     kIntraThreads, 0) != cudaSuccess)
     return bad(MPTC_ECUDA);
   ctx->intra_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
+  per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_warp_kernel<mptc::kIntraWarps>,
+                                                    mptc::kIntraWarps * 32, 0) != cudaSuccess)
+    return bad(MPTC_ECUDA);
+  ctx->intra_warp_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
   const size_t n = (size_t)ctx->nblk;
   if (dalloc(&ctx->done, n) || dalloc(&ctx->work, kWorkWords + 4 * (size_t)ctx->ntiles) ||
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
@@ -569,62 +721,24 @@ mptc_status mptc_dxt1_encode(mptc_ctx *ctx, const uint8_t *rgb_dev, uint64_t *bl
 mptc_status mptc_reencode(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev, const int32_t *orig_err_dev,
                           const uint64_t *prev_final_dev, uint64_t *final_dev, uint8_t *motion_dev,
                           uint32_t *unique_dev, uint32_t *n_unique_dev, void *stream) {
-  if (!ctx) return MPTC_EINVAL;
-  if (!rgb_dev || !stb_dev || !orig_err_dev || !final_dev || !motion_dev || !unique_dev || !n_unique_dev)
-    return fail(ctx, MPTC_EINVAL, "mptc_reencode: null pointer");
-  if (!aligned(rgb_dev, 16) || !aligned(stb_dev, 8) || !aligned(final_dev, 8) || !aligned(motion_dev, 2) ||
-      (prev_final_dev && !aligned(prev_final_dev, 8)) || !aligned(orig_err_dev, 4) || !aligned(unique_dev, 4))
-    return fail(ctx, MPTC_EINVAL, "mptc_reencode: misaligned pointer");
-  if (prev_final_dev == final_dev) return fail(ctx, MPTC_EINVAL, "mptc_reencode: prev and final alias");
+  mptc_status st = reencode_check(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev,
+                                  unique_dev, n_unique_dev);
+  if (st != MPTC_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  mptc::SearchParams P = make_params(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev);
-  MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, work_bytes(ctx->ntiles), s));
+  const mptc::SearchParams P = make_params(ctx, rgb_dev, stb_dev, orig_err_dev, prev_final_dev, final_dev, motion_dev);
+  st = reencode_begin(ctx, P, s);
+  if (st != MPTC_OK) return st;
   if (prev_final_dev) {
-    mptc::weight_desc_kernel<<<(ctx->nblk + 255) / 256, 256, 0, s>>>(prev_final_dev, ctx->nblk, ctx->wdesc);
-    // weight descriptors, the search (learned: embeddings, scoring, search),
-    // pending compaction, sweep init + sweeps + dataflow fallback
-    ctx->launches += 2;  // weight descriptors, pending compaction
-    KernelTimer t(ctx, K_INTER, s);
     if (ctx->model) {
-      ctx->launches += launch_learned_inter(ctx, P, rgb_dev, stb_dev, prev_final_dev, s);
+      const LearnedJob job{ctx, P};
+      ctx->launches += launch_learned(&job, 1, ctx->work + 12, s);
     } else {
+      KernelTimer t(ctx, K_INTER, s);
       ctx->launches += launch_inter_search(P, ctx->inter_warps, ctx->work, ctx->pending, ctx->sm_count, s);
     }
     MPTC_CUDA(cudaGetLastError());
-  } else {
-    MPTC_CUDA(cudaMemsetAsync(ctx->done, 0, (size_t)ctx->nblk * sizeof(uint64_t), s));
   }
-  if (prev_final_dev) {
-    // pending = blocks the inter pass left open, in wavefront order, with
-    // the sweeps' first estimates and change flags
-    const int sw = sweep_count(ctx->cfg.intra_sweeps);
-    mptc::pending_scan_kernel<<<ctx->ntiles, 256, 0, s>>>(
-        ctx->order, ctx->done, stb_dev, ctx->nblk, ctx->ntiles, ctx->tile_state, ctx->work + 10, ctx->pending,
-        ctx->work + 5, ctx->sweep, ctx->sweep + 3 * (size_t)ctx->nblk, sw ? sw + 1 : 0, ctx->work + 1);
-  }
-  {
-    KernelTimer t(ctx, prev_final_dev ? K_PENDING : K_INTRA, s);
-    const int ig = ctx->intra_cap > 0 ? std::min(ctx->intra_cap, ctx->intra_grid) : ctx->intra_grid;
-    if (prev_final_dev)
-      ctx->launches += launch_intra_sweeps(P, ctx->pending, ctx->work + 5, ctx->sweep, ctx->nblk, ig,
-                                           sweep_count(ctx->cfg.intra_sweeps), ctx->sweep_part,
-                                           std::min(ctx->nblk, kSweepPartCap), s);
-    else
-      mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
-    if (!prev_final_dev) ++ctx->launches;
-  }
-  MPTC_CUDA(cudaGetLastError());
-  const uint16_t *m16 = reinterpret_cast<const uint16_t *>(motion_dev);
-  {
-    KernelTimer t(ctx, K_UNIQUE, s);
-    mptc::unique_scan_kernel<<<ctx->ntiles, 256, 0, s>>>(m16, stb_dev, ctx->nblk, ctx->ntiles,
-                                                        ctx->tile_state + ctx->ntiles, ctx->work + 11, unique_dev,
-                                                        n_unique_dev, ctx->work + 2, ctx->work + 1);
-    ++ctx->launches;
-  }
-  MPTC_CUDA(cudaGetLastError());
-  ctx->last_is_intra = prev_final_dev ? 0u : 1u;
-  return MPTC_OK;
+  return reencode_finish(ctx, P, unique_dev, n_unique_dev, s);
 }
 
 mptc_status mptc_encode_frame(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *prev_final_dev, uint64_t *stb_dev,
@@ -1018,20 +1132,39 @@ mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int n = ctx->nblk;
   MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, work_bytes(ctx->ntiles), s));
-  mptc_status st = mptc_internal::model_embed_words(ctx->model, reinterpret_cast<const uint32_t *>(prev_final_dev) + 1,
-                                                    2, n, ctx->gemb, ctx->work + 1, s);
-  if (st == MPTC_OK)
-    st = mptc_internal::model_embed_blocks(ctx->model, rgb_dev, ctx->width, stb_dev, nullptr, n, ctx->femb,
-                                           ctx->work + 1, s);
-  if (st != MPTC_OK) return fail(ctx, st, "mptc_learned_proposals: embedding launch failed");
-  mptc::ScoreArgs a{ctx->bw, ctx->bh, ctx->cfg.search_area, ctx->topk, ctx->work + 1};
-  const bool r8 = ctx->score_rows == 8;
-  const CUtensorMap &tg = r8 ? ctx->tm_g8 : ctx->tm_g4;
   MPTC_CUDA(cudaMemsetAsync(ctx->topk, 0xFF, (size_t)n * mptc::kMaxK * sizeof(uint16_t), s));
+  // the learned search's embedding and scoring launches for this one frame
+  mptc_internal::EmbedJob ej;
+  ej.words = reinterpret_cast<const uint32_t *>(prev_final_dev) + 1;
+  ej.word_stride = 2;
+  ej.n = n;
+  ej.out = ctx->gemb;
+  ej.status = ctx->work + 1;
+  mptc_status st = mptc_internal::model_embed(ctx->model, false, &ej, 1, ctx->work + 12, s);
+  if (st == MPTC_OK) {
+    ej = mptc_internal::EmbedJob{};
+    ej.rgb = rgb_dev;
+    ej.width = ctx->width;
+    ej.stb = stb_dev;
+    ej.n = n;
+    ej.out = ctx->femb;
+    ej.status = ctx->work + 1;
+    st = mptc_internal::model_embed(ctx->model, true, &ej, 1, ctx->work + 13, s);
+  }
+  if (st != MPTC_OK) return fail(ctx, st, "mptc_learned_proposals: embedding launch failed");
+  mptc::ScoreBatch sb{};
+  sb.n = 1;
+  sb.next = ctx->work + 14;
+  sb.tile_end[0] = ((ctx->bw + mptc::kScoreTileW - 1) / mptc::kScoreTileW) *
+                   ((ctx->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
+  sb.a[0] = mptc::ScoreArgs{ctx->bw, ctx->bh, ctx->cfg.search_area, ctx->topk, ctx->work + 1};
+  const bool r8 = ctx->score_rows == 8;
+  sb.tmF[0] = ctx->tm_f;
+  sb.tmG[0] = r8 ? ctx->tm_g8 : ctx->tm_g4;
   switch (ctx->topk_k) {
-    case 4: r8 ? launch_score<8, 4>(ctx, tg, a, s) : launch_score<4, 4>(ctx, tg, a, s); break;
-    case 16: r8 ? launch_score<8, 16>(ctx, tg, a, s) : launch_score<4, 16>(ctx, tg, a, s); break;
-    default: r8 ? launch_score<8, 8>(ctx, tg, a, s) : launch_score<4, 8>(ctx, tg, a, s); break;
+    case 4: r8 ? launch_score<8, 4>(sb, ctx->sm_count, s) : launch_score<4, 4>(sb, ctx->sm_count, s); break;
+    case 16: r8 ? launch_score<8, 16>(sb, ctx->sm_count, s) : launch_score<4, 16>(sb, ctx->sm_count, s); break;
+    default: r8 ? launch_score<8, 8>(sb, ctx->sm_count, s) : launch_score<4, 8>(sb, ctx->sm_count, s); break;
   }
   MPTC_CUDA(cudaGetLastError());
   MPTC_CUDA(cudaMemcpyAsync(topk_dev, ctx->topk, (size_t)n * mptc::kMaxK * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s));
@@ -1276,6 +1409,10 @@ struct mptc_batch {
   std::vector<char> has_prev;
   int parity = 0;                // final[parity] receives the next frame
   std::map<std::string, cudaGraphExec_t> graphs;
+  // the learned search's launches cover all streams with a model at once
+  std::vector<cudaEvent_t> begun_ev;  // per stream: its first part is queued
+  cudaEvent_t learned_ev = nullptr;
+  uint32_t *counters = nullptr;       // 3 per launch group of kMaxBatch streams
 };
 
 namespace {
@@ -1285,15 +1422,49 @@ void batch_clear_graphs(mptc_batch *b) {
   b->graphs.clear();
 }
 
-// Launches one frame of every stream on the forked streams (capturable).
+// Launches one frame of every stream on the forked streams (capturable):
+// per stream the stb encode and the first part of the reencode (and the
+// exhaustive inter search of streams without a model); then the learned
+// inter search of every inter frame with a model, each phase one launch for
+// all of them (up to kMaxBatch streams per launch); then per stream the
+// intra pass and the palette.
 mptc_status batch_launch(mptc_batch *b, const int32_t *is_intra, int parity, cudaStream_t s) {
   if (cudaEventRecord(b->fork_ev, s) != cudaSuccess) return MPTC_ECUDA;
+  std::vector<mptc::SearchParams> P(b->n);
+  std::vector<LearnedJob> jobs;
   for (int i = 0; i < b->n; ++i) {
+    mptc_ctx *c = b->ctx[i];
     cudaStream_t si = b->streams[i];
     if (cudaStreamWaitEvent(si, b->fork_ev, 0) != cudaSuccess) return MPTC_ECUDA;
     const uint64_t *prev = is_intra[i] ? nullptr : b->fin[parity ^ 1][i];
-    mptc_status st = mptc_encode_frame(b->ctx[i], b->rgb[i], prev, nullptr, b->fin[parity][i], b->motion[i],
-                                       b->unique[i], b->n_unique + i, si);
+    mptc_status st = mptc_dxt1_encode(c, b->rgb[i], c->stb, c->orig_err, si);
+    if (st != MPTC_OK) return st;
+    P[i] = make_params(c, b->rgb[i], c->stb, c->orig_err, prev, b->fin[parity][i], b->motion[i]);
+    st = reencode_begin(c, P[i], si);
+    if (st != MPTC_OK) return st;
+    if (prev && !c->model) {
+      KernelTimer t(c, K_INTER, si);
+      c->launches += launch_inter_search(P[i], c->inter_warps, c->work, c->pending, c->sm_count, si);
+    }
+    if (prev && c->model) jobs.push_back(LearnedJob{c, P[i]});
+    if (cudaEventRecord(b->begun_ev[i], si) != cudaSuccess) return MPTC_ECUDA;
+  }
+  if (!jobs.empty()) {
+    for (int i = 0; i < b->n; ++i)
+      if (cudaStreamWaitEvent(s, b->begun_ev[i], 0) != cudaSuccess) return MPTC_ECUDA;
+    const int groups = ((int)jobs.size() + mptc::kMaxBatch - 1) / mptc::kMaxBatch;
+    if (cudaMemsetAsync(b->counters, 0, 3 * sizeof(uint32_t) * groups, s) != cudaSuccess) return MPTC_ECUDA;
+    for (int g = 0; g < groups; ++g) {
+      const int n = std::min(mptc::kMaxBatch, (int)jobs.size() - g * mptc::kMaxBatch);
+      jobs[g * mptc::kMaxBatch].ctx->launches += launch_learned(jobs.data() + g * mptc::kMaxBatch, n,
+                                                                b->counters + 3 * g, s);
+    }
+    if (cudaGetLastError() != cudaSuccess || cudaEventRecord(b->learned_ev, s) != cudaSuccess) return MPTC_ECUDA;
+  }
+  for (int i = 0; i < b->n; ++i) {
+    cudaStream_t si = b->streams[i];
+    if (!jobs.empty() && cudaStreamWaitEvent(si, b->learned_ev, 0) != cudaSuccess) return MPTC_ECUDA;
+    mptc_status st = reencode_finish(b->ctx[i], P[i], b->unique[i], b->n_unique + i, si);
     if (st != MPTC_OK) return st;
     if (cudaEventRecord(b->done_ev[i], si) != cudaSuccess) return MPTC_ECUDA;
     if (cudaStreamWaitEvent(s, b->done_ev[i], 0) != cudaSuccess) return MPTC_ECUDA;
@@ -1343,8 +1514,12 @@ mptc_status mptc_batch_create(const mptc_config *cfg, int32_t n_streams, const i
     mptc_batch_destroy(b);
     return st;
   };
-  if (cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bad(MPTC_ECUDA);
-  if (dalloc(&b->n_unique, (size_t)n_streams)) return bad(MPTC_ENOMEM);
+  if (cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->learned_ev, cudaEventDisableTiming) != cudaSuccess)
+    return bad(MPTC_ECUDA);
+  if (dalloc(&b->n_unique, (size_t)n_streams) ||
+      dalloc(&b->counters, 3 * (size_t)((n_streams + mptc::kMaxBatch - 1) / mptc::kMaxBatch)))
+    return bad(MPTC_ENOMEM);
   for (int i = 0; i < n_streams; ++i) {
     mptc_ctx *c = nullptr;
     mptc_status st = mptc_ctx_create(cfg, widths[i], heights[i], &c);
@@ -1356,6 +1531,8 @@ mptc_status mptc_batch_create(const mptc_config *cfg, int32_t n_streams, const i
     b->streams.push_back(si);
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return bad(MPTC_ECUDA);
     b->done_ev.push_back(ev);
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return bad(MPTC_ECUDA);
+    b->begun_ev.push_back(ev);
     const size_t nb = (size_t)c->nblk;
     uint8_t *rgb = nullptr, *mot = nullptr;
     uint64_t *f0 = nullptr, *f1 = nullptr;
@@ -1380,7 +1557,10 @@ mptc_status mptc_batch_destroy(mptc_batch *b) {
   for (auto c : b->ctx) mptc_ctx_destroy(c);
   for (auto s : b->streams) cudaStreamDestroy(s);
   for (auto e : b->done_ev) cudaEventDestroy(e);
+  for (auto e : b->begun_ev) cudaEventDestroy(e);
   if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+  if (b->learned_ev) cudaEventDestroy(b->learned_ev);
+  cudaFree(b->counters);
   for (auto p : b->rgb) cudaFree(p);
   for (int k = 0; k < 2; ++k)
     for (auto p : b->fin[k]) cudaFree(p);
@@ -1460,41 +1640,54 @@ mptc_status mptc_batch_set_model(mptc_batch *b, const mptc_model *model, int32_t
 }
 
 mptc_status mptc_batch_autotune(mptc_batch *b, const int32_t *is_intra, int32_t *inter_warps, int32_t *intra_ctas,
-                                void *stream) {
+                                int32_t *score_rows, void *stream) {
   if (!b || !is_intra) return MPTC_EINVAL;
   for (int i = 0; i < b->n; ++i)
     if (!is_intra[i] && !b->has_prev[i]) return MPTC_ESTATE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // trial steps re-encode the current inputs into the buffers of the next
-  // real step (same parity), so the streams do not advance
-  const int warps[2] = {2, 4};
+  // real step (same parity), so the streams do not advance. Knobs: warps
+  // (blocks) per CTA of the exhaustive inter search, the CTA cap of each
+  // stream's intra dataflow, and, with a model attached, the candidate rows
+  // (dictionary slice) per pipeline stage of the window scoring.
+  const bool learned = b->ctx[0]->model != nullptr;
+  std::vector<int> warps = {2, 4}, rows = {8};
+  if (learned) {
+    warps = {b->ctx[0]->inter_warps};  // the exhaustive search only serves the fallbacks
+    rows = {4, 8};
+  }
   const int sms = b->ctx[0]->sm_count;
   const int caps[5] = {0, 8 * sms, 4 * sms, 2 * sms, sms};
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return MPTC_ECUDA;
   float best = 1e30f;
-  int bw = kSearchWarps, bc = 0;
+  int bw = b->ctx[0]->inter_warps, bc = 0, br = b->ctx[0]->score_rows;
   mptc_status st = MPTC_OK;
   for (int w : warps) {
-    for (int c : caps) {
-      for (auto cx : b->ctx) {
-        cx->inter_warps = w;
-        cx->intra_cap = c;
+    for (int r : rows) {
+      for (int c : caps) {
+        for (auto cx : b->ctx) {
+          cx->inter_warps = w;
+          cx->intra_cap = c;
+          cx->score_rows = r;
+        }
+        batch_clear_graphs(b);
+        st = batch_run(b, is_intra, b->parity, s);  // capture + warm-up
+        if (st != MPTC_OK) break;
+        cudaEventRecord(e0, s);
+        for (int k = 0; k < 3 && st == MPTC_OK; ++k) st = batch_run(b, is_intra, b->parity, s);
+        cudaEventRecord(e1, s);
+        if (st != MPTC_OK || cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+          best = ms;
+          bw = w;
+          bc = c;
+          br = r;
+        }
       }
-      batch_clear_graphs(b);
-      st = batch_run(b, is_intra, b->parity, s);  // capture + warm-up
       if (st != MPTC_OK) break;
-      cudaEventRecord(e0, s);
-      for (int r = 0; r < 3 && st == MPTC_OK; ++r) st = batch_run(b, is_intra, b->parity, s);
-      cudaEventRecord(e1, s);
-      if (st != MPTC_OK || cudaEventSynchronize(e1) != cudaSuccess) break;
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms < best) {
-        best = ms;
-        bw = w;
-        bc = c;
-      }
     }
     if (st != MPTC_OK) break;
   }
@@ -1503,10 +1696,12 @@ mptc_status mptc_batch_autotune(mptc_batch *b, const int32_t *is_intra, int32_t 
   for (auto cx : b->ctx) {
     cx->inter_warps = bw;
     cx->intra_cap = bc;
+    cx->score_rows = br;
   }
   batch_clear_graphs(b);
   if (inter_warps) *inter_warps = bw;
   if (intra_ctas) *intra_ctas = bc;
+  if (score_rows) *score_rows = br;
   return st;
 }
 

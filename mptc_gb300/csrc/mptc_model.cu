@@ -237,43 +237,41 @@ int sm_count_now() {
 
 namespace mptc_internal {
 
-mptc_status model_embed_blocks(const mptc_model *m, const uint8_t *rgb, int width, const uint64_t *stb,
-                               const uint32_t *blocks, int n, __nv_bfloat16 *F, uint32_t *status, cudaStream_t s) {
-  if (!m || n <= 0) return MPTC_EINVAL;
+mptc_status model_embed(const mptc_model *m, bool blocks, const EmbedJob *jobs, int n_jobs, uint32_t *next,
+                        cudaStream_t s) {
+  if (!m || !jobs || n_jobs <= 0 || n_jobs > mptc::kMaxBatch || !next) return MPTC_EINVAL;
   if (ensure_embed_attrs() != cudaSuccess) return MPTC_ECUDA;
-  mptc::EmbedArgs a{};
-  a.rgb = rgb;
-  a.width = width;
-  a.bw = width / 4;
-  a.n = n;
-  a.stb = stb;
-  a.blocks = blocks;
-  a.wimg = m->img;
-  a.b1 = m->w + kOff.b[0];
-  a.b2 = m->w + kOff.b[1];
-  a.b3 = m->w + kOff.b[2];
-  a.out = F;
-  a.status = status ? status : m->status;
-  const int tiles = (n + 127) / 128;
-  mptc::embed_kernel<mptc::NetF, true><<<std::min(tiles, sm_count_now()), mptc::kEmbedThreads, kSmemF, s>>>(a);
-  return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
-}
-
-mptc_status model_embed_words(const mptc_model *m, const uint32_t *words, int word_stride, int n, __nv_bfloat16 *G,
-                              uint32_t *status, cudaStream_t s) {
-  if (!m || n <= 0) return MPTC_EINVAL;
-  if (ensure_embed_attrs() != cudaSuccess) return MPTC_ECUDA;
-  mptc::EmbedArgs a{};
-  a.n = n;
-  a.words = words;
-  a.word_stride = word_stride;
-  a.wimg = m->img;
-  a.b1 = m->w + kOff.b[3];
-  a.b2 = m->w + kOff.b[4];
-  a.out = G;
-  a.status = status ? status : m->status;
-  const int tiles = (n + 127) / 128;
-  mptc::embed_kernel<mptc::NetG, false><<<std::min(tiles, 2 * sm_count_now()), mptc::kEmbedThreads, kSmemG, s>>>(a);
+  mptc::EmbedBatch b{};
+  b.n = n_jobs;
+  b.next = next;
+  int tiles = 0;
+  const int l0 = blocks ? 0 : 3;
+  for (int j = 0; j < n_jobs; ++j) {
+    const EmbedJob &J = jobs[j];
+    mptc::EmbedArgs &a = b.a[j];
+    a.rgb = J.rgb;
+    a.width = J.width;
+    a.bw = J.width / 4;
+    a.n = J.n;
+    a.stb = J.stb;
+    a.blocks = J.blocks;
+    a.words = J.words;
+    a.word_stride = J.word_stride;
+    a.wimg = m->img;
+    a.b1 = m->w + kOff.b[l0];
+    a.b2 = m->w + kOff.b[l0 + 1];
+    a.b3 = blocks ? m->w + kOff.b[2] : nullptr;
+    a.out = J.out;
+    a.status = J.status ? J.status : m->status;
+    tiles += (J.n + 127) / 128;
+    b.tile_end[j] = tiles;
+  }
+  if (tiles == 0) return MPTC_OK;
+  const int sms = sm_count_now();
+  if (blocks)
+    mptc::embed_kernel<mptc::NetF, true><<<std::min(tiles, sms), mptc::kEmbedThreads, kSmemF, s>>>(b);
+  else
+    mptc::embed_kernel<mptc::NetG, false><<<std::min(tiles, 2 * sms), mptc::kEmbedThreads, kSmemG, s>>>(b);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
@@ -290,8 +288,8 @@ mptc_status mptc_model_create(uint64_t seed, mptc_model **out) {
   if (!m) return MPTC_ENOMEM;
   const size_t n = kOff.total;
   if (dmalloc(&m->w, n) || dmalloc(&m->wb, n) || dmalloc(&m->g, n) || dmalloc(&m->m, n) || dmalloc(&m->v, n) ||
-      dmalloc(&m->loss, 1) || dmalloc(&m->img, mptc::kImgBytes) || dmalloc(&m->status, 1) ||
-      cudaMemset(m->img, 0, mptc::kImgBytes) != cudaSuccess || cudaMemset(m->status, 0, 4) != cudaSuccess) {
+      dmalloc(&m->loss, 1) || dmalloc(&m->img, mptc::kImgBytes) || dmalloc(&m->status, 4) ||
+      cudaMemset(m->img, 0, mptc::kImgBytes) != cudaSuccess || cudaMemset(m->status, 0, 16) != cudaSuccess) {
     mptc_model_destroy(m);
     return MPTC_ENOMEM;
   }
@@ -453,16 +451,28 @@ mptc_status mptc_model_embed(mptc_model *m, const uint8_t *rgb_dev, int32_t widt
     if (dmalloc(&m->emb_tmp, (size_t)need * mptc::kEmb)) return MPTC_ENOMEM;
     m->emb_cap = need;
   }
-  if (cudaMemsetAsync(m->status, 0, 4, s) != cudaSuccess) return MPTC_ECUDA;
+  if (cudaMemsetAsync(m->status, 0, 16, s) != cudaSuccess) return MPTC_ECUDA;
   mptc_status st = MPTC_OK;
   if (n_blocks > 0) {
-    st = mptc_internal::model_embed_blocks(m, rgb_dev, width, stb_dev, blocks_dev, n_blocks, m->emb_tmp, nullptr, s);
+    mptc_internal::EmbedJob j;
+    j.rgb = rgb_dev;
+    j.width = width;
+    j.stb = stb_dev;
+    j.blocks = blocks_dev;
+    j.n = n_blocks;
+    j.out = m->emb_tmp;
+    st = mptc_internal::model_embed(m, true, &j, 1, m->status + 1, s);
     if (st != MPTC_OK) return st;
     mptc::bf16_to_f32_kernel<<<blocks_for((size_t)n_blocks * mptc::kEmb), 256, 0, s>>>(m->emb_tmp, emb_blocks_dev,
                                                                                       n_blocks * mptc::kEmb);
   }
   if (n_words > 0) {
-    st = mptc_internal::model_embed_words(m, words_dev, word_stride, n_words, m->emb_tmp, nullptr, s);
+    mptc_internal::EmbedJob j;
+    j.words = words_dev;
+    j.word_stride = word_stride;
+    j.n = n_words;
+    j.out = m->emb_tmp;
+    st = mptc_internal::model_embed(m, false, &j, 1, m->status + 2, s);
     if (st != MPTC_OK) return st;
     mptc::bf16_to_f32_kernel<<<blocks_for((size_t)n_words * mptc::kEmb), 256, 0, s>>>(m->emb_tmp, emb_words_dev,
                                                                                      n_words * mptc::kEmb);

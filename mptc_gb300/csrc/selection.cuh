@@ -19,8 +19,9 @@ namespace mptc {
 //   before r0 hold no e <= 0, and row r0 breaks at P0. m = 0.
 // - otherwise the first position of the minimum e (strict improvement), m = it.
 // Each lane keeps the three positions (first e <= 0; the key
-// row << 16 | (0xFFFF - pos) of its e < 0 positions; first minimum); four warp
-// reductions give the selected position, whose candidate data the caller
+// row << 16 | (0xFFFF - pos) of its e < 0 positions; first minimum, ties
+// broken by position, so a lane may visit its positions in any order); four
+// warp reductions give the selected position, whose candidate data the caller
 // recovers.
 struct LaneSel {
   int le0_pos = 0x7fffffff;  // first position with e <= 0
@@ -30,7 +31,7 @@ struct LaneSel {
     if (e == kInvalid) return;
     if (e <= 0 && pos < le0_pos) le0_pos = pos;
     if (e < 0) neg_key = max(neg_key, (row << 16) | (0xFFFF - pos));
-    if (e < min_e) {  // positions arrive in increasing order: keeps the first minimum
+    if (e < min_e || (e == min_e && pos < min_pos)) {  // the first minimum, in any arrival order
       min_e = e;
       min_pos = pos;
     }
@@ -73,7 +74,7 @@ struct ThreadSel : LaneSel {
         neg = SelPick{cand, eps, refit};
       }
     }
-    if (e < min_e) {
+    if (e < min_e || (e == min_e && pos < min_pos)) {
       min_e = e;
       min_pos = pos;
       mn = SelPick{cand, eps, refit};

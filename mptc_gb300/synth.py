@@ -85,6 +85,8 @@ HD720 = StreamSpec(1280, 720, 64, period_min=64, period_max=512, n_squares=4, sq
                    speed_min=1, speed_max=4, cut_every=32)
 FHD1080 = StreamSpec(1920, 1080, 120)
 FHD1080_TRAIN = StreamSpec(1920, 1080, 200, seed=5000)
+# calibration frames of the learned proposal's K: neither trained on nor measured
+FHD1080_CALIB = StreamSpec(1920, 1080, 16, seed=7000)
 UHD2160 = StreamSpec(3840, 2160, 60, period_min=128, period_max=1024, n_squares=16,
                      square_size=256, speed_min=1, speed_max=4, cut_every=20)
 

@@ -145,3 +145,65 @@ def train_proposal(torch, frames_dev, search_area=8, err_threshold=5, intra_inte
     info = dict(frames=T, examples=int(sum(e[1].numel() for e in examples)), label_seconds=round(label_s, 2),
                 train_seconds=round(time.time() - t1, 2), steps=steps, batch=batch, candidates=cands)
     return model, losses, info
+
+
+def decoded_sse(torch, rgb, width, height, blocks) -> int:
+    """Squared error of a frame against its decoded DXT1 blocks (device tensors)."""
+    sse = torch.zeros(1, dtype=torch.int64, device=rgb.device)
+    check(lib().mptc_decoded_sse(dev_ptr(rgb, "rgb", 1, width * height * 3), width, height,
+                                 dev_ptr(blocks, "blocks", 8, (width // 4) * (height // 4)),
+                                 dev_ptr(sse, "sse", 8, 1), ctypes.c_void_p(0)))
+    return int(sse.item())
+
+
+def choose_topk(torch, model, frames_dev, search_area=8, err_threshold=5, intra_interval=16, ks=(4, 8, 16),
+                max_psnr_loss_db=0.05, log=None):
+    """The number of proposals per block, chosen against the exhaustive search:
+    the calibration frames are encoded by the exhaustive search and with each
+    K; the fastest K whose decoded PSNR stays within max_psnr_loss_db of the
+    exhaustive search's is kept (half the 0.1 dB budget, the rest is margin
+    for content the calibration frames do not show), else the most accurate.
+    Returns (K, {K: (psnr loss dB, ms per frame, fallback rate)})."""
+    T, H, W, _ = frames_dev.shape
+    n = (W // 4) * (H // 4)
+    dev = frames_dev.device
+    flags = intra_schedule(T, intra_interval)
+    s = torch.cuda.current_stream()
+
+    def run(K):
+        enc = Encoder(W, H, search_area, err_threshold, intra_interval)
+        if K:
+            enc.set_model(model, K)
+        fin = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(2)]
+        mot = torch.empty(2 * n, dtype=torch.uint8, device=dev)
+        uni = torch.empty(n, dtype=torch.int32, device=dev)
+        nu = torch.zeros(1, dtype=torch.int32, device=dev)
+        sse, fb, inter, ms = 0, 0, 0, 0.0
+        for rep in range(2):  # the second pass is timed
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for t in range(T):
+                prev = None if flags[t] else fin[(t - 1) % 2]
+                enc.encode_frame_device(frames_dev[t], prev, None, fin[t % 2], mot, uni, nu, s)
+                if rep == 1:
+                    sse += decoded_sse(torch, frames_dev[t], W, H, fin[t % 2])
+                    if not flags[t]:
+                        fb += enc.stats(s).n_fallback
+                        inter += n
+            e1.record(s)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / T
+        enc.close()
+        return sse, ms, fb / max(1, inter)
+
+    base_sse, base_ms, _ = run(0)
+    table = {}
+    for K in ks:
+        sse, ms, fb = run(K)
+        loss = 10.0 * float(np.log10(max(sse, 1) / max(base_sse, 1)))
+        table[K] = (round(loss, 4), round(ms, 3), round(fb, 4))
+        if log is not None:
+            log(f"K={K}: PSNR loss {loss:.4f} dB, {ms:.3f} ms/frame (exhaustive {base_ms:.3f}), fallback {fb:.4f}")
+    ok = [K for K in ks if table[K][0] <= max_psnr_loss_db]
+    best = min(ok, key=lambda K: table[K][1]) if ok else min(ks, key=lambda K: table[K][0])
+    return best, table

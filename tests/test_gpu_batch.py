@@ -61,8 +61,8 @@ def test_batch_autotune_keeps_results(torch_cuda):
         for k in range(2):
             b.upload(k, streams[k][f])
         if f == 1:
-            warps, ctas = b.autotune([False, False])
-            assert warps in (2, 4) and ctas >= 0
+            t = b.autotune([False, False])
+            assert t["inter_warps_per_cta"] in (2, 4) and t["intra_ctas_per_stream"] >= 0
         b.encode([flags[f]] * 2)
         for k in range(2):
             fin, mot, uni = b.fetch(k)
@@ -70,6 +70,52 @@ def test_batch_autotune_keeps_results(torch_cuda):
             np.testing.assert_array_equal(mot, ref[k][f][1])
             np.testing.assert_array_equal(uni, ref[k][f][2])
     b.close()
+
+
+def single_learned(frames, sa, thr, flags, model, K):
+    from mptc_gb300.encoder import Encoder
+    h, w = frames.shape[1:3]
+    enc = Encoder(w, h, sa, thr, 16)
+    enc.set_model(model, K)
+    out = []
+    for f, intra in zip(frames, flags):
+        o = enc.encode_frame_host(f, is_intra=intra)
+        out.append((o.final.copy(), o.motion.copy(), o.unique.copy()))
+    enc.close()
+    return out
+
+
+@pytest.mark.parametrize("K", [8, 16])
+def test_learned_batch_matches_single_streams(torch_cuda, K):
+    """With a model attached, the batch runs each phase of the learned search
+    as one launch over every stream (mixed resolutions, staggered intra
+    frames); every stream's outputs equal the same stream encoded alone with
+    the same model, before and after the autotuner changes the scoring's
+    stage shape."""
+    from mptc_gb300.batch import BatchEncoder
+    from mptc_gb300.model import ProposalModel
+    sizes = [(256, 128), (128, 96), (320, 240), (64, 64), (136, 72)]
+    nf = 5
+    streams = [StreamSpec(w, h, nf, seed=80 + k, square_size=32).generate() for k, (w, h) in enumerate(sizes)]
+    flags = [[f == 0 or f == k for f in range(nf)] for k in range(len(sizes))]
+    model = ProposalModel(seed=7)
+    ref = [single_learned(streams[k], 8, 5, flags[k], model, K) for k in range(len(sizes))]
+    b = BatchEncoder(sizes, 8, 5, 16)
+    b.set_model(model, K)
+    for f in range(nf):
+        for k in range(len(sizes)):
+            b.upload(k, streams[k][f])
+        if f == 3:
+            t = b.autotune([flags[k][f] for k in range(len(sizes))])
+            assert t["score_rows_per_stage"] in (4, 8)
+        b.encode([flags[k][f] for k in range(len(sizes))])
+        for k in range(len(sizes)):
+            fin, mot, uni = b.fetch(k)
+            np.testing.assert_array_equal(fin, ref[k][f][0], err_msg=f"stream {k} frame {f}")
+            np.testing.assert_array_equal(mot, ref[k][f][1])
+            np.testing.assert_array_equal(uni, ref[k][f][2])
+    b.close()
+    model.close()
 
 
 def test_batch_rejects_inter_first_frame(torch_cuda):

@@ -74,7 +74,8 @@ def mlp(torch, Ws, x, ids):
     for i, li in enumerate(ids):
         inp = bf(torch, h)
         z = inp @ bf(torch, Ws[li][0]) + Ws[li][1]
-        z.retain_grad()
+        if z.requires_grad:
+            z.retain_grad()
         trace.append((inp, z))
         h = torch.relu(z) if i < len(ids) - 1 else z
     return h, trace
