@@ -208,6 +208,23 @@ mptc_status mptc_batch_fetch(mptc_batch *batch, int32_t i, uint64_t *final_host,
  * flag per stream (a stream's first frame must be intra). Asynchronous on
  * `stream`. */
 mptc_status mptc_batch_encode(mptc_batch *batch, const int32_t *is_intra, void *stream);
+/* A run of n_frames frames of every stream in one call, from device memory:
+ * stream i's frames back to back at frames_dev[i] (its width*height*3 bytes
+ * each), its intra flags at is_intra[i * n_frames .. +n_frames] (a stream's
+ * first frame ever must be intra), its outputs for frame k at
+ * final_dev[i] + k*nblk_i, motion_dev[i] + 2*k*nblk_i, unique_dev[i] + k*nblk_i
+ * and n_unique_dev[i][k]. The streams continue across calls (the run's last
+ * frame becomes each stream's previous frame, for this call or
+ * mptc_batch_encode). The results equal n_frames calls of mptc_batch_encode.
+ * All the run's intra frames are encoded first, each stream's on an intra lane
+ * of its own (they depend on no earlier frame), overlapping the inter frames;
+ * the inter frames follow frame by frame, and with a model attached each phase
+ * of their learned search is one launch over all streams. Returns after
+ * `stream` has completed the run. The multi-stream form of the reference's
+ * per-stream encoder loop (codec/codec.cpp:1383-1509) for whole runs. */
+mptc_status mptc_batch_encode_run(mptc_batch *batch, int32_t n_frames, const uint8_t *const *frames_dev,
+                                  const int32_t *is_intra, uint64_t *const *final_dev, uint8_t *const *motion_dev,
+                                  uint32_t *const *unique_dev, uint32_t *const *n_unique_dev, void *stream);
 /* Autotuner: times the candidate launch shapes on the current inputs and the
  * given intra/inter pattern (without advancing the streams) and keeps the
  * fastest: warps (blocks) per CTA of the exhaustive inter search (2, 4; with a

@@ -31,7 +31,7 @@ EXPORTED = [
     "mptc_ctx_set_model", "mptc_decoded_sse", "mptc_batch_set_model",
     "mptc_endpoint_coefficients", "mptc_decoder_create", "mptc_decoder_destroy", "mptc_decode_frame",
     "mptc_decoder_check", "mptc_decoder_last_error", "mptc_kernel_launches", "mptc_candidate_errors",
-    "mptc_learned_proposals", "mptc_ctx_set_learned_shape",
+    "mptc_learned_proposals", "mptc_ctx_set_learned_shape", "mptc_batch_encode_run",
 ]
 
 NOALLOC_MAX_BLOCKS = 131072  # MPTC_NOALLOC_MAX_BLOCKS
@@ -140,6 +140,7 @@ def lib() -> ctypes.CDLL:
         L.mptc_ctx_set_model.argtypes = [vp, vp, i32]
         L.mptc_decoded_sse.argtypes = [vp, i32, i32, vp, vp, vp]
         L.mptc_learned_proposals.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.mptc_batch_encode_run.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
         L.mptc_ctx_set_learned_shape.argtypes = [vp, i32]
         L.mptc_candidate_errors.argtypes = [vp, i32, i32, vp, vp, vp, i32, i32, vp, vp]
         L.mptc_batch_set_model.argtypes = [vp, vp, i32]

@@ -81,6 +81,34 @@ class BatchEncoder:
         check(lib().mptc_batch_encode(self._b, arr, s))
         return flags
 
+    def encode_run(self, frames, finals, motions, uniques, n_uniques, is_intra, stream=None) -> None:
+        """A run of F frames of every stream (mptc_batch_encode_run): frames[i]
+        a CUDA uint8 tensor (F, H_i, W_i, 3); finals[i] (F, nblk_i) int64,
+        motions[i] (F, 2 nblk_i) uint8, uniques[i] (F, nblk_i) int32 and
+        n_uniques[i] (F,) int32 CUDA tensors receive stream i's outputs;
+        is_intra[i]: F flags."""
+        if len(frames) != self.n:
+            raise ValueError(f"{len(frames)} frame runs for {self.n} streams")
+        F = int(frames[0].shape[0])
+        ptr = lambda xs: (ctypes.c_void_p * self.n)(*xs)  # noqa: E731
+        fr, fi, mo, un, nu, flags = [], [], [], [], [], []
+        for i in range(self.n):
+            w, h = self.sizes[i]
+            n = self.nblk(i)
+            if tuple(frames[i].shape) != (F, h, w, 3):
+                raise ValueError(f"stream {i}: frames {tuple(frames[i].shape)}, expected ({F}, {h}, {w}, 3)")
+            fr.append(dev_ptr(frames[i], "frames", 1, F * h * w * 3))
+            fi.append(dev_ptr(finals[i], "final", 8, F * n))
+            mo.append(dev_ptr(motions[i], "motion", 1, F * 2 * n))
+            un.append(dev_ptr(uniques[i], "unique", 4, F * n))
+            nu.append(dev_ptr(n_uniques[i], "n_unique", 4, F))
+            if len(is_intra[i]) != F:
+                raise ValueError(f"stream {i}: {len(is_intra[i])} intra flags for {F} frames")
+            flags.extend(int(bool(x)) for x in is_intra[i])
+        arr = (ctypes.c_int32 * len(flags))(*flags)
+        s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+        check(lib().mptc_batch_encode_run(self._b, F, ptr(fr), arr, ptr(fi), ptr(mo), ptr(un), ptr(nu), s))
+
     def autotune(self, is_intra: list[bool], stream=None) -> dict:
         """Times the launch shapes on the current inputs and keeps the fastest;
         returns the chosen inter warps per CTA, intra CTAs per stream (0: all)

@@ -19,8 +19,7 @@ namespace mptc {
 // eps = 0xFFFFFFFF, since its high half would be q2 < q1 <= 0xFFFF). A thread
 // that finds its word still being evaluated, or no free bucket within the
 // probe limit, evaluates it itself; results are identical either way.
-constexpr int kEvalBuckets = 512;  // power of two, indexed by a 9-bit hash (CTA per block)
-constexpr int kWarpEvalBuckets = 128;  // the same per warp (warp per block)
+constexpr int kEvalBuckets = 512;  // power of two, indexed by a 9-bit hash
 constexpr int kEvalProbes = 16;
 constexpr uint64_t kEvalPending = ~0ull;
 
@@ -30,7 +29,6 @@ struct EvalCacheN {
   unsigned long long val[NB];
 };
 using EvalCache = EvalCacheN<kEvalBuckets>;
-using WarpEvalCache = EvalCacheN<kWarpEvalBuckets>;
 
 // Resets a cache with the threads first, first + stride, ... of the CTA.
 template <int NB>
@@ -220,143 +218,6 @@ __global__ void __launch_bounds__(THREADS, 4) intra_search_kernel(SearchParams P
     }
     publish_intra(P, ts, red, idx, stb, w2, tid, true);
     cache.update(__syncthreads_count(looked > 0), __syncthreads_count(hits > 0));
-  }
-}
-
-// The same dataflow with one warp per block (search areas up to 8: at most
-// 256 window positions, 8 per lane). A lane evaluates whichever of its
-// positions' blocks are already final, in any order, and polls for the rest
-// (backing off while nothing arrives), so when the last dependency (usually
-// the left neighbour) is published only its word remains to look up or
-// evaluate; the selection is four warp reductions, with no CTA barrier on the
-// dependency chain. Per-warp evaluation caches of 128 buckets. Warps claim
-// blocks in wavefront order from P.work, one at a time, so every block a warp
-// waits on was claimed earlier by a resident warp and the dataflow cannot
-// deadlock; every wait is bounded as in wait_done.
-constexpr int kIntraWarps = 8;  // warps per CTA of intra_warp_kernel
-
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) intra_warp_kernel(SearchParams P, const uint32_t *__restrict__ pending,
-                                                                const uint32_t *__restrict__ n_pending_dev,
-                                                                int n_pending_host,
-                                                                const uint32_t *__restrict__ run_flag = nullptr) {
-  if (run_flag && __ldcg(run_flag) == 0u) return;  // the sweeps converged
-  __shared__ BlockTab s_tab[WARPS];
-  __shared__ WarpEvalCache s_cache[WARPS];
-  __shared__ uint8_t s_snap5[256], s_snap6[256];
-  __shared__ float4 s_wk[4];
-  build_snap_tables(s_snap5, s_snap6);
-  build_weight_table(s_wk);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  BlockTab &tab = s_tab[warp];
-  WarpEvalCache &cache = s_cache[warp];
-  const int n_pend = n_pending_host >= 0 ? n_pending_host : (int)__ldcg(n_pending_dev);
-  const int w2 = 2 * P.sa, npos = w2 * w2;
-  bool use_cache = true;
-  int cache_off = 0;
-  while (true) {
-    int k = 0;
-    if (lane == 0) k = (int)atomicAdd(P.work, 1u);
-    k = __shfl_sync(kFull, k, 0);
-    if (k >= n_pend) break;
-    const int idx = (int)__ldcg(pending + k);
-    const int by = idx / P.bw, bx = idx - by * P.bw;
-    const uint64_t stb = __ldg(P.stb + idx);
-    const uint32_t own = (uint32_t)(stb >> 32);
-    eval_cache_reset(cache, own, lane, 32);
-    const int sumsq = stage_block(tab, P.rgb, P.width, bx, by, lane);  // ends with __syncwarp
-    const int orig = __ldg(P.orig_err + idx);
-    const PixelGroups pg = load_groups(tab);
-    // this lane's positions pos = lane + 32 r (scan order of IntraSearch:
-    // rows j = by .. by-2sa+1, columns i = bx+sa-1 .. bx-sa, without j == by,
-    // i >= bx), bit r of `open` while its block is not final yet
-    uint32_t open = 0;
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const int pos = lane + 32 * r;
-      const int row = pos / w2, col = pos - row * w2;
-      const int j = by - row, i = bx + P.sa - 1 - col;
-      if (pos < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh && !(j == by && i >= bx)) open |= 1u << r;
-    }
-    ThreadSel ts;
-    int looked = 0, hits = 0;
-    uint64_t t0 = 0;
-    uint32_t idle = 0;
-    while (open) {
-      bool progress = false;
-#pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        if (!((open >> r) & 1u)) continue;
-        const int pos = lane + 32 * r;
-        const int row = pos / w2, col = pos - row * w2;
-        const size_t nidx = (size_t)(by - row) * P.bw + (bx + P.sa - 1 - col);
-        const uint64_t w = ld_relaxed(P.done + nidx);
-        if (!w) continue;
-        open &= ~(1u << r);
-        progress = true;
-        const uint32_t cand = (uint32_t)w;
-        uint32_t eps = 0;
-        int refit = 0;
-        const int e = cached_eval(cache, use_cache, tab, pg, s_snap5, s_snap6, s_wk, cand, own, orig, sumsq, eps,
-                                  refit, looked, hits);
-        ts.add(pos, row, e, cand, eps, refit);
-      }
-      if (!open || progress) {
-        idle = 0;
-        continue;
-      }
-      // nothing arrived: back off a little, and give up after ~1 s (or at
-      // once when another wait of the launch gave up)
-      if (idle == 0) t0 = global_ns();
-      ++idle;
-      if (idle > 16) __nanosleep(idle > 256 ? 256 : 32);
-      if ((idle & 63u) == 0u) {
-        if ((ld_acquire(P.status) & kDevTimeout) || global_ns() - t0 > 1000000000ull) {
-          atomicOr(P.status, kDevTimeout);
-          open = 0;
-        }
-      }
-    }
-    // selection (LaneSel closed form) and the result, written by the lane
-    // holding the selected statistic
-    int m;
-    const int sel = warp_select(ts, w2, m);
-    const bool accept = sel >= 0 && m <= P.thr;
-    int pick = 2;
-    if (sel >= 0 && m == 0) {
-      const int p0 = __reduce_min_sync(kFull, ts.le0_pos);
-      pick = sel == p0 ? 0 : 1;
-    }
-    const bool holder = pick == 0   ? ts.le0_pos == sel
-                        : pick == 1 ? ts.neg_key >= 0 && 0xFFFF - (ts.neg_key & 0xFFFF) == sel
-                                    : ts.min_e == m && ts.min_pos == sel;
-    const unsigned hb = __ballot_sync(kFull, accept && holder);
-    const int writer = accept ? __ffs(hb) - 1 : 0;
-    if (lane == writer) {
-      uint16_t code = 0xFFFFu;
-      uint64_t blk = stb;
-      if (accept) {
-        const SelPick &pk = pick == 0 ? ts.le0 : (pick == 1 ? ts.neg : ts.mn);
-        const int row = sel / w2, col = sel - row * w2;
-        code = (uint16_t)((w2 - 1 - col) | ((w2 - 1 - row) << 8));
-        if (pk.refit) blk = (uint64_t)pk.eps | ((uint64_t)pk.cand << 32);
-      }
-      P.final_blk[idx] = blk;
-      P.motion[idx] = code;
-      st_relaxed(P.done + idx, done_word(blk));
-    }
-    // the cache's bypass on content without repeated words, per warp
-    const int nl = __popc(__ballot_sync(kFull, looked > 0)), nh = __popc(__ballot_sync(kFull, hits > 0));
-    if (use_cache) {
-      if (nl >= 8 && 4 * nh < nl) {
-        use_cache = false;
-        cache_off = 8;
-      }
-    } else if (--cache_off <= 0) {
-      use_cache = true;
-    }
-    __syncwarp();
   }
 }
 

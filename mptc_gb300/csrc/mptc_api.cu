@@ -40,7 +40,7 @@ size_t work_bytes(int ntiles) { return (kWorkWords + 4 * (size_t)ntiles) * sizeo
 struct mptc_ctx {
   mptc_config cfg{};
   int width = 0, height = 0, bw = 0, bh = 0, nblk = 0, ntiles = 0;
-  int device = 0, sm_count = 0, intra_grid = 0, intra_warp_grid = 0;
+  int device = 0, sm_count = 0, intra_grid = 0;
   // launch shapes (tunable): warps per CTA of the inter search, CTA cap of the intra search
   int inter_warps = kSearchWarps, intra_cap = 0;
   // learned proposal (optional): K proposals per block, union rows per
@@ -504,15 +504,6 @@ int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream
   return 5;
 }
 
-// CTAs of the warp-per-block intra dataflow: the context's cap counts blocks
-// in flight (CTAs of the CTA-per-block kernel), here warps, rounded up to
-// whole CTAs; uncapped, one CTA per SM (8 blocks in flight per SM, far more
-// than the ~bw/sa blocks of the wavefront).
-int intra_warp_ctas(const mptc_ctx *ctx) {
-  const int want = ctx->intra_cap > 0 ? (ctx->intra_cap + mptc::kIntraWarps - 1) / mptc::kIntraWarps : ctx->sm_count;
-  return std::max(1, std::min(want, ctx->intra_warp_grid));
-}
-
 mptc_status reencode_check(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev,
                            const int32_t *orig_err_dev, const uint64_t *prev_final_dev, const uint64_t *final_dev,
                            const uint8_t *motion_dev, const uint32_t *unique_dev, const uint32_t *n_unique_dev) {
@@ -562,9 +553,6 @@ mptc_status reencode_finish(mptc_ctx *ctx, const mptc::SearchParams &P, uint32_t
       ctx->launches += launch_intra_sweeps(P, ctx->pending, ctx->work + 5, ctx->sweep, ctx->nblk, ig,
                                            sweep_count(ctx->cfg.intra_sweeps), ctx->sweep_part,
                                            std::min(ctx->nblk, kSweepPartCap), s);
-    else if (ctx->cfg.search_area <= 8)
-      mptc::intra_warp_kernel<mptc::kIntraWarps><<<intra_warp_ctas(ctx), mptc::kIntraWarps * 32, 0, s>>>(
-          P, ctx->order, nullptr, ctx->nblk);
     else
       mptc::intra_search_kernel<kIntraThreads><<<ig, kIntraThreads, 0, s>>>(P, ctx->order, nullptr, ctx->nblk);
     if (!prev_final_dev) ++ctx->launches;
@@ -629,11 +617,7 @@ mptc_status mptc_ctx_create(const mptc_config *cfg, int32_t width, int32_t heigh
                                                     kIntraThreads, 0) != cudaSuccess)
     return bad(MPTC_ECUDA);
   ctx->intra_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
-  per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mptc::intra_warp_kernel<mptc::kIntraWarps>,
-                                                    mptc::kIntraWarps * 32, 0) != cudaSuccess)
-    return bad(MPTC_ECUDA);
-  ctx->intra_warp_grid = ctx->sm_count * (per_sm > 0 ? per_sm : 1);
+
   const size_t n = (size_t)ctx->nblk;
   if (dalloc(&ctx->done, n) || dalloc(&ctx->work, kWorkWords + 4 * (size_t)ctx->ntiles) ||
       dalloc(&ctx->stb, n) || dalloc(&ctx->orig_err, n) || dalloc(&ctx->rgb_dev, n * 48) ||
@@ -1413,6 +1397,11 @@ struct mptc_batch {
   std::vector<cudaEvent_t> begun_ev;  // per stream: its first part is queued
   cudaEvent_t learned_ev = nullptr;
   uint32_t *counters = nullptr;       // 3 per launch group of kMaxBatch streams
+  // runs (mptc_batch_encode_run): an event per stream and frame slot marking
+  // an intra frame of the stream's lane, the run's start, its status word
+  std::vector<std::vector<cudaEvent_t>> lane_ev;
+  cudaEvent_t run_start = nullptr;
+  uint32_t *run_status = nullptr;
 };
 
 namespace {
@@ -1499,6 +1488,132 @@ mptc_status batch_run(mptc_batch *b, const int32_t *is_intra, int parity, cudaSt
   return cudaGraphLaunch(it->second, s) == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
+// A run of frames of every stream. Every intra frame depends on no earlier
+// frame, so all of them are queued first, each stream's on its own intra lane
+// (the lane context and high-priority stream of the stream calls), where they
+// overlap whatever the other streams do; then the inter frames go step by
+// step: per stream the stb encode and the first part of the reencode on the
+// stream's CUDA stream (an inter frame after an intra frame first waits for
+// that frame's lane event), then, with a model, each phase of the learned
+// search as one launch over every stream's inter frame of the step, then per
+// stream the intra pass and the palette. Without a model the streams' inter
+// frames run side by side, each on its own stream.
+mptc_status batch_run_frames(mptc_batch *b, int32_t n_frames, const uint8_t *const *frames, const int32_t *is_intra,
+                             uint64_t *const *fin, uint8_t *const *mot, uint32_t *const *uni,
+                             uint32_t *const *n_uni, cudaStream_t s) {
+  const int S = b->n;
+  for (int i = 0; i < S; ++i) {
+    mptc_ctx *c = b->ctx[i];
+    if (!frames[i] || !fin[i] || !mot[i] || !uni[i] || !n_uni[i]) return MPTC_EINVAL;
+    if (!aligned(frames[i], 16) || !aligned(fin[i], 8) || !aligned(mot[i], 2) || !aligned(uni[i], 4) ||
+        !aligned(n_uni[i], 4))
+      return MPTC_EINVAL;
+    if (!is_intra[(size_t)i * n_frames] && !b->has_prev[i]) return MPTC_ESTATE;
+    mptc_status st = lane_init(c);
+    if (st != MPTC_OK) return st;
+    c->lane_b->timing = c->timing;
+    c->lane_b->model = nullptr;  // intra frames: no inter search
+    while ((int)b->lane_ev[i].size() < n_frames) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return MPTC_ECUDA;
+      b->lane_ev[i].push_back(e);
+    }
+  }
+  if (!b->run_start && cudaEventCreateWithFlags(&b->run_start, cudaEventDisableTiming) != cudaSuccess)
+    return MPTC_ECUDA;
+  if (!b->run_status && cudaMalloc(&b->run_status, sizeof(uint32_t)) != cudaSuccess) return MPTC_ENOMEM;
+  if (cudaMemsetAsync(b->run_status, 0, sizeof(uint32_t), s) != cudaSuccess ||
+      cudaEventRecord(b->run_start, s) != cudaSuccess)
+    return MPTC_ECUDA;
+  for (int i = 0; i < S; ++i) {
+    mptc_ctx *c = b->ctx[i];
+    if (cudaStreamWaitEvent(b->streams[i], b->run_start, 0) != cudaSuccess ||
+        cudaStreamWaitEvent(c->lane_s, b->run_start, 0) != cudaSuccess)
+      return MPTC_ECUDA;
+  }
+  // every intra frame, on its stream's lane
+  for (int i = 0; i < S; ++i) {
+    mptc_ctx *c = b->ctx[i];
+    const size_t n = (size_t)c->nblk;
+    for (int k = 0; k < n_frames; ++k) {
+      if (!is_intra[(size_t)i * n_frames + k]) continue;
+      mptc_status st = mptc_encode_frame(c->lane_b, frames[i] + k * n * 48, nullptr, nullptr, fin[i] + k * n,
+                                         mot[i] + 2 * k * n, uni[i] + k * n, n_uni[i] + k, c->lane_s);
+      if (st != MPTC_OK) return st;
+      status_or_kernel<<<1, 32, 0, c->lane_s>>>(c->lane_b->work, b->run_status);
+      if (cudaEventRecord(b->lane_ev[i][k], c->lane_s) != cudaSuccess) return MPTC_ECUDA;
+    }
+  }
+  // the inter frames, step by step
+  std::vector<mptc::SearchParams> P(S);
+  std::vector<char> active(S);
+  for (int k = 0; k < n_frames; ++k) {
+    std::vector<LearnedJob> jobs;
+    for (int i = 0; i < S; ++i) {
+      active[i] = !is_intra[(size_t)i * n_frames + k];
+      if (!active[i]) continue;
+      mptc_ctx *c = b->ctx[i];
+      cudaStream_t si = b->streams[i];
+      const size_t n = (size_t)c->nblk;
+      const uint64_t *prev = k > 0 ? fin[i] + (k - 1) * n : b->fin[b->parity ^ 1][i];
+      if (k > 0 && is_intra[(size_t)i * n_frames + k - 1] &&
+          cudaStreamWaitEvent(si, b->lane_ev[i][k - 1], 0) != cudaSuccess)
+        return MPTC_ECUDA;
+      const uint8_t *in = frames[i] + k * n * 48;
+      mptc_status st = mptc_dxt1_encode(c, in, c->stb, c->orig_err, si);
+      if (st != MPTC_OK) return st;
+      P[i] = make_params(c, in, c->stb, c->orig_err, prev, fin[i] + k * n, mot[i] + 2 * k * n);
+      st = reencode_begin(c, P[i], si);
+      if (st != MPTC_OK) return st;
+      if (c->model) {
+        jobs.push_back(LearnedJob{c, P[i]});
+        if (cudaEventRecord(b->begun_ev[i], si) != cudaSuccess) return MPTC_ECUDA;
+      } else {
+        KernelTimer t(c, K_INTER, si);
+        c->launches += launch_inter_search(P[i], c->inter_warps, c->work, c->pending, c->sm_count, si);
+      }
+    }
+    if (!jobs.empty()) {
+      for (int i = 0; i < S; ++i)
+        if (active[i] && b->ctx[i]->model && cudaStreamWaitEvent(s, b->begun_ev[i], 0) != cudaSuccess)
+          return MPTC_ECUDA;
+      const int groups = ((int)jobs.size() + mptc::kMaxBatch - 1) / mptc::kMaxBatch;
+      if (cudaMemsetAsync(b->counters, 0, 3 * sizeof(uint32_t) * groups, s) != cudaSuccess) return MPTC_ECUDA;
+      for (int g = 0; g < groups; ++g) {
+        const int m = std::min(mptc::kMaxBatch, (int)jobs.size() - g * mptc::kMaxBatch);
+        jobs[g * mptc::kMaxBatch].ctx->launches +=
+            launch_learned(jobs.data() + g * mptc::kMaxBatch, m, b->counters + 3 * g, s);
+      }
+      if (cudaGetLastError() != cudaSuccess || cudaEventRecord(b->learned_ev, s) != cudaSuccess) return MPTC_ECUDA;
+    }
+    for (int i = 0; i < S; ++i) {
+      if (!active[i]) continue;
+      mptc_ctx *c = b->ctx[i];
+      cudaStream_t si = b->streams[i];
+      const size_t n = (size_t)c->nblk;
+      if (c->model && !jobs.empty() && cudaStreamWaitEvent(si, b->learned_ev, 0) != cudaSuccess) return MPTC_ECUDA;
+      mptc_status st = reencode_finish(c, P[i], uni[i] + k * n, n_uni[i] + k, si);
+      if (st != MPTC_OK) return st;
+      status_or_kernel<<<1, 32, 0, si>>>(c->work, b->run_status);
+    }
+  }
+  // `stream` completes after every stream and lane; each stream's last frame
+  // becomes its previous frame for the next call
+  for (int i = 0; i < S; ++i) {
+    mptc_ctx *c = b->ctx[i];
+    if (cudaEventRecord(b->done_ev[i], b->streams[i]) != cudaSuccess ||
+        cudaStreamWaitEvent(s, b->done_ev[i], 0) != cudaSuccess ||
+        cudaEventRecord(c->lane_done, c->lane_s) != cudaSuccess ||
+        cudaStreamWaitEvent(s, c->lane_done, 0) != cudaSuccess)
+      return MPTC_ECUDA;
+    const size_t n = (size_t)c->nblk;
+    if (cudaMemcpyAsync(b->fin[b->parity][i], fin[i] + (size_t)(n_frames - 1) * n, n * 8, cudaMemcpyDeviceToDevice,
+                        s) != cudaSuccess)
+      return MPTC_ECUDA;
+  }
+  return MPTC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1533,6 +1648,7 @@ mptc_status mptc_batch_create(const mptc_config *cfg, int32_t n_streams, const i
     b->done_ev.push_back(ev);
     if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return bad(MPTC_ECUDA);
     b->begun_ev.push_back(ev);
+    b->lane_ev.emplace_back();
     const size_t nb = (size_t)c->nblk;
     uint8_t *rgb = nullptr, *mot = nullptr;
     uint64_t *f0 = nullptr, *f1 = nullptr;
@@ -1560,7 +1676,11 @@ mptc_status mptc_batch_destroy(mptc_batch *b) {
   for (auto e : b->begun_ev) cudaEventDestroy(e);
   if (b->fork_ev) cudaEventDestroy(b->fork_ev);
   if (b->learned_ev) cudaEventDestroy(b->learned_ev);
+  if (b->run_start) cudaEventDestroy(b->run_start);
+  for (auto &v : b->lane_ev)
+    for (auto e : v) cudaEventDestroy(e);
   cudaFree(b->counters);
+  cudaFree(b->run_status);
   for (auto p : b->rgb) cudaFree(p);
   for (int k = 0; k < 2; ++k)
     for (auto p : b->fin[k]) cudaFree(p);
@@ -1627,6 +1747,33 @@ mptc_status mptc_batch_encode(mptc_batch *b, const int32_t *is_intra, void *stre
   for (int i = 0; i < b->n; ++i) b->has_prev[i] = 1;
   b->parity ^= 1;
   return MPTC_OK;
+}
+
+mptc_status mptc_batch_encode_run(mptc_batch *b, int32_t n_frames, const uint8_t *const *frames_dev,
+                                  const int32_t *is_intra, uint64_t *const *final_dev, uint8_t *const *motion_dev,
+                                  uint32_t *const *unique_dev, uint32_t *const *n_unique_dev, void *stream) {
+  if (!b || n_frames < 0 || (n_frames > 0 && (!frames_dev || !is_intra || !final_dev || !motion_dev || !unique_dev ||
+                                              !n_unique_dev)))
+    return MPTC_EINVAL;
+  if (n_frames == 0) return MPTC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  mptc_status st = batch_run_frames(b, n_frames, frames_dev, is_intra, final_dev, motion_dev, unique_dev,
+                                    n_unique_dev, s);
+  if (st != MPTC_OK) {
+    cudaStreamSynchronize(s);
+    for (int i = 0; i < b->n; ++i) {
+      cudaStreamSynchronize(b->streams[i]);
+      if (b->ctx[i]->lane_s) cudaStreamSynchronize(b->ctx[i]->lane_s);
+    }
+    return st;
+  }
+  for (int i = 0; i < b->n; ++i) b->has_prev[i] = 1;
+  b->parity ^= 1;
+  uint32_t h = 0;
+  if (cudaMemcpyAsync(&h, b->run_status, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return MPTC_ECUDA;
+  return (h & mptc::kDevTimeout) ? MPTC_ETIMEOUT : MPTC_OK;
 }
 
 mptc_status mptc_batch_set_model(mptc_batch *b, const mptc_model *model, int32_t k) {
