@@ -471,70 +471,32 @@ def run_gpu(args, rank: int, world: int, dist) -> None:
 
 
 def run_batch(args, rank: int, world: int, dist) -> None:
-    """S concurrent 1080p streams: stream k plays the 120-frame stream from
-    frame offset 15k, with its intra frames at phase 16k/S (streams started at
-    different times). A step encodes every stream's whole 120 frames."""
+    """S concurrent 1080p streams through the batched encoder's run call (see
+    time_batch), plain exhaustive search."""
     import torch
 
-    from mptc_gb300.batch import BatchEncoder
     from mptc_gb300.synth import FHD1080, StreamSpec
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     S, nf = args.batch, args.frames
-    frames_np = StreamSpec(**{**FHD1080.__dict__, "seed": FHD1080.seed + rank}).generate(0, nf)
-    frames_dev = torch.from_numpy(frames_np).to(dev)
-    b = BatchEncoder([(W, H)] * S, SA, THR, II)
-    offsets = [(15 * k) % nf for k in range(S)]
-    phases = [(II * k) // S for k in range(S)]
-    stream = torch.cuda.current_stream()
-
-    def flags(f):
-        return [f == 0 or (f - phases[k]) % II == 0 for k in range(S)]
-
-    def step():
-        for f in range(nf):
-            for k in range(S):
-                b.upload(k, frames_dev[(f + offsets[k]) % nf], stream)
-            b.encode(flags(f), stream)
-
-    # warm-up: the first frames, then tune the launch shapes on a typical mixed step
-    for f in range(2):
-        for k in range(S):
-            b.upload(k, frames_dev[(f + offsets[k]) % nf], stream)
-        b.encode(flags(f), stream)
-    tuned = b.autotune(flags(2), stream)
-    log(f"[rank {rank}] autotune: {tuned}")
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+    frames_dev = torch.from_numpy(StreamSpec(**{**FHD1080.__dict__, "seed": FHD1080.seed + rank}).generate(0, nf)).to(dev)
     if dist is not None:
         dist.barrier()
     clk = ClockSampler(local)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if dist is not None:
-        dist.barrier()
+    value, tuned = time_batch(torch, frames_dev, S, None, 0, args.steps, args.warmup)
     clocks = clk.stop()
-    elapsed_ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
-    b.fetch(0)  # raises on a device-side timeout
-    value = whole_job_rate(S * nf * args.steps, world, elapsed_ms * 1e-3)
+    value = whole_job_rate(S * nf * args.steps, world, max_over_ranks(S * nf * args.steps / value, dist, dev))
     if rank == 0:
         cfg = workload_config()
         cfg.update({"workload": f"batched 1080p MPTC encode: {S} concurrent streams x {nf} frames",
-                    "streams_per_gpu": S, "intra_phase": "stream k: 16k/S",
-                    "autotune": tuned})
+                    "streams_per_gpu": S, "intra_phase": "stream k: 16k/S", "autotune": tuned})
         print(json.dumps(dict(metric=METRIC, value=round(value, 3), unit="frames/s", n_gpus=world,
                               steps=args.steps, warmup=args.warmup,
-                              ms_per_step=round(elapsed_ms / args.steps, 3), higher_is_better=True,
+                              ms_per_step=round(1000.0 * S * nf * world / value, 3), higher_is_better=True,
                               scaling="weak", vs_baseline=None, dtype="fp32+int32", data="synthetic",
                               config=cfg, clocks=clocks)), flush=True)
-    b.close()
 
 
 def adaptive_code_bits(symbols: np.ndarray, alphabet: int) -> float:
@@ -655,11 +617,15 @@ def time_stream_call(torch, enc, frames_dev, sched, steps, warmup):
 
 
 def time_batch(torch, frames_dev, S, model, topk, steps, warmup):
-    """S concurrent streams of the 1080p stream (stream k from frame offset 15k,
-    its intra frames at phase 16k/S) through the batched encoder; frames/s of
-    all streams together."""
+    """S concurrent 1080p streams (stream k plays the 120-frame stream from
+    frame offset 15k, its intra frames at phase 16k/S) through the batched
+    encoder: the launch shapes are tuned on a mixed frame step, then each step
+    is one mptc_batch_encode_run over every stream's 120 frames (outputs in
+    HBM). Returns (frames/s of all streams together, the tuned shapes)."""
     from mptc_gb300.batch import BatchEncoder
     nf = frames_dev.shape[0]
+    n = (W // 4) * (H // 4)
+    dev = frames_dev.device
     b = BatchEncoder([(W, H)] * S, SA, THR, II)
     if model is not None:
         b.set_model(model, topk)
@@ -669,17 +635,20 @@ def time_batch(torch, frames_dev, S, model, topk, steps, warmup):
 
     def flags(f):
         return [f == 0 or (f - phases[k]) % II == 0 for k in range(S)]
-
-    def step():
-        for f in range(nf):
-            for k in range(S):
-                b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
-            b.encode(flags(f), s)
     for f in range(2):
         for k in range(S):
             b.upload(k, frames_dev[(f + offsets[k]) % nf], s)
         b.encode(flags(f), s)
     tuned = b.autotune(flags(2), s)
+    runs = [torch.roll(frames_dev, -offsets[k], dims=0).contiguous() for k in range(S)]
+    fins = [torch.empty((nf, n), dtype=torch.int64, device=dev) for _ in range(S)]
+    mots = [torch.empty((nf, 2 * n), dtype=torch.uint8, device=dev) for _ in range(S)]
+    unis = [torch.empty((nf, n), dtype=torch.int32, device=dev) for _ in range(S)]
+    nus = [torch.empty(nf, dtype=torch.int32, device=dev) for _ in range(S)]
+    run_flags = [[flags(f)[k] for f in range(nf)] for k in range(S)]
+
+    def step():
+        b.encode_run(runs, fins, mots, unis, nus, run_flags, s)
     for _ in range(warmup):
         step()
     torch.cuda.synchronize()
@@ -689,8 +658,8 @@ def time_batch(torch, frames_dev, S, model, topk, steps, warmup):
         step()
     e1.record(s)
     torch.cuda.synchronize()
-    b.fetch(0)
     b.close()
+    del runs, fins, mots, unis, nus
     return S * nf * steps / (e0.elapsed_time(e1) * 1e-3), tuned
 
 

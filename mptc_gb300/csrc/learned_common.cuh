@@ -30,35 +30,18 @@ constexpr uint16_t kNoProposal = 0xFFFFu;  // empty top-K slot
 // 48 pixel channels (p - lo_c) / (hi_c - lo_c) over the block's own channel
 // range (0 for a flat channel), the stb endpoints ep1, ep2 as r/31, g/63,
 // b/31, zero padding to 64.
-__device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ rgb, int width, int bx, int by,
-                                                   uint64_t stb, int half, uint32_t (&out)[16]) {
-  uint32_t w[12];
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const uint32_t *p = reinterpret_cast<const uint32_t *>(rgb + ((size_t)(4 * by + r) * width + 4 * bx) * 3);
-    w[3 * r] = __ldg(p);
-    w[3 * r + 1] = __ldg(p + 1);
-    w[3 * r + 2] = __ldg(p + 2);
-  }
-  auto byte = [&](int i) -> uint32_t { return (w[i >> 2] >> (8 * (i & 3))) & 0xFFu; };
-  uint32_t lo[3] = {255u, 255u, 255u}, hi[3] = {0u, 0u, 0u};
-#pragma unroll
-  for (int i = 0; i < 48; ++i) {
-    const uint32_t v = byte(i);
-    lo[i % 3] = min(lo[i % 3], v);
-    hi[i % 3] = max(hi[i % 3], v);
-  }
-  float inv[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) inv[c] = hi[c] > lo[c] ? 1.0f / (float)(hi[c] - lo[c]) : 0.0f;
-  const uint32_t e1 = (uint32_t)(stb & 0xFFFF), e2 = (uint32_t)((stb >> 16) & 0xFFFF);
+template <int HALF>
+__device__ __forceinline__ void block_feature_cols(const uint32_t (&w)[12], const uint32_t (&lo)[3],
+                                                   const float (&inv)[3], uint32_t e1, uint32_t e2,
+                                                   uint32_t (&out)[16]) {
   float f[32];
 #pragma unroll
   for (int j = 0; j < 32; ++j) {
-    const int i = 32 * half + j;
+    const int i = 32 * HALF + j;  // a compile-time column
     float v = 0.f;
     if (i < 48) {
-      v = (float)(byte(i) - lo[i % 3]) * inv[i % 3];
+      const uint32_t byte = (w[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+      v = (float)(byte - lo[i % 3]) * inv[i % 3];
     } else if (i < 54) {
       const uint32_t ep = i < 51 ? e1 : e2;
       const int ch = (i - 48) % 3;
@@ -72,6 +55,33 @@ __device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ r
     const __nv_bfloat162 b = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
     out[j] = *reinterpret_cast<const uint32_t *>(&b);
   }
+}
+
+__device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ rgb, int width, int bx, int by,
+                                                   uint64_t stb, int half, uint32_t (&out)[16]) {
+  uint32_t w[12];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t *p = reinterpret_cast<const uint32_t *>(rgb + ((size_t)(4 * by + r) * width + 4 * bx) * 3);
+    w[3 * r] = __ldg(p);
+    w[3 * r + 1] = __ldg(p + 1);
+    w[3 * r + 2] = __ldg(p + 2);
+  }
+  uint32_t lo[3] = {255u, 255u, 255u}, hi[3] = {0u, 0u, 0u};
+#pragma unroll
+  for (int i = 0; i < 48; ++i) {
+    const uint32_t v = (w[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+    lo[i % 3] = min(lo[i % 3], v);
+    hi[i % 3] = max(hi[i % 3], v);
+  }
+  float inv[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) inv[c] = hi[c] > lo[c] ? 1.0f / (float)(hi[c] - lo[c]) : 0.0f;
+  const uint32_t e1 = (uint32_t)(stb & 0xFFFF), e2 = (uint32_t)((stb >> 16) & 0xFFFF);
+  if (half)
+    block_feature_cols<1>(w, lo, inv, e1, e2, out);
+  else
+    block_feature_cols<0>(w, lo, inv, e1, e2, out);
 }
 
 // Word features, half `half`: the 32 bits of an index word as 0/1 (half 0),

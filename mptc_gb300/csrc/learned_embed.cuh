@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
   extern __shared__ uint8_t dsm[];
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(dsm) + 1023) & ~uintptr_t(1023));
   uint8_t *sW = sm;
-  uint8_t *sA[2] = {sm + Net::kWBytes, sm + Net::kWBytes + kTileBytes};
+  uint8_t *const sA0 = sm + Net::kWBytes, *const sA1 = sm + Net::kWBytes + kTileBytes;
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm + Net::kWBytes + 2 * kTileBytes);  // weights, mma, buf0, buf1
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 4);
   volatile uint32_t *abort_flag = tslot + 1;
@@ -151,10 +151,10 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
       tc::bulk_g2s(sW + o, batch.a[0].wimg + Net::kW + o, min(32768u, Net::kWBytes - o), bar);
   }
   if (!tc::mbar_wait(bar, 0, abort_flag)) *abort_flag = 1;
-  uint32_t ph_mma = 0, ph_buf[2] = {0, 0};
+  uint32_t ph_mma = 0, ph_buf = 0;  // ph_buf bit b: parity of operand buffer b's barrier
   auto wait_buf = [&](int b) {
-    if (!tc::mbar_wait(bar + 2 + b, ph_buf[b], abort_flag)) *abort_flag = 1;
-    ph_buf[b] ^= 1;
+    if (!tc::mbar_wait(bar + 2 + b, (ph_buf >> b) & 1u, abort_flag)) *abort_flag = 1;
+    ph_buf ^= 1u << b;
   };
   const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
   const int row = 32 * q + lane;
@@ -186,14 +186,14 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j)
-        *reinterpret_cast<uint4 *>(sA[0] + tc::sw128_offset(r, 4 * half + j)) =
+        *reinterpret_cast<uint4 *>(sA0 + tc::sw128_offset(r, 4 * half + j)) =
             make_uint4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
     }
     tc::fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc::tc_fence_after();
-      issue_chunk(tmem, sA[0], sW + Net::kW1, tc::idesc_bf16(128, Net::N1), false);
+      issue_chunk(tmem, sA0, sW + Net::kW1, tc::idesc_bf16(128, Net::N1), false);
       tc::mma_commit(bar + 1);
     }
     if (!tc::mbar_wait(bar + 1, ph_mma, abort_flag)) *abort_flag = 1;
@@ -205,13 +205,14 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
     for (int kc = 0; kc < KC2; ++kc) {
       const int b = kc & 1;
       if (kc >= 2) wait_buf(b);
-      epilogue_to_tile(lane_base + 64 * kc + 32 * h, a.b1 + 64 * kc + 32 * h, sA[b], row, h);
+      uint8_t *const buf = b ? sA1 : sA0;
+      epilogue_to_tile(lane_base + 64 * kc + 32 * h, a.b1 + 64 * kc + 32 * h, buf, row, h);
       tc::fence_async_smem();
       tc::tc_fence_before();
       __syncthreads();
       if (tid == 0) {
         tc::tc_fence_after();
-        issue_chunk(tmem + Net::N1, sA[b], sW + Net::kW2 + (uint32_t)kc * Net::N2 * 128u, tc::idesc_bf16(128, Net::N2),
+        issue_chunk(tmem + Net::N1, buf, sW + Net::kW2 + (uint32_t)kc * Net::N2 * 128u, tc::idesc_bf16(128, Net::N2),
                     kc > 0);
         tc::mma_commit(bar + 2 + b);
       }
@@ -228,13 +229,14 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
       for (int kc = 0; kc < KC3; ++kc) {
         const int b = kc & 1;
         if (kc >= 2) wait_buf(b);
-        epilogue_to_tile(lane_base + Net::N1 + 64 * kc + 32 * h, a.b2 + 64 * kc + 32 * h, sA[b], row, h);
+        uint8_t *const buf = b ? sA1 : sA0;
+        epilogue_to_tile(lane_base + Net::N1 + 64 * kc + 32 * h, a.b2 + 64 * kc + 32 * h, buf, row, h);
         tc::fence_async_smem();
         tc::tc_fence_before();
         __syncthreads();
         if (tid == 0) {
           tc::tc_fence_after();
-          issue_chunk(tmem, sA[b], sW + Net::kW3 + (uint32_t)kc * Net::N3 * 128u, tc::idesc_bf16(128, Net::N3),
+          issue_chunk(tmem, buf, sW + Net::kW3 + (uint32_t)kc * Net::N3 * 128u, tc::idesc_bf16(128, Net::N3),
                       kc > 0);
           tc::mma_commit(bar + 2 + b);
         }

@@ -72,6 +72,21 @@ __device__ __forceinline__ void topk_insert(float (&s)[K], int (&p)[K], float v,
   }
 }
 
+// v[j] for a runtime j without indexing the register array (which would put
+// it in local memory): a five-level tree of selects.
+__device__ __forceinline__ float pick32(const float (&v)[32], int j) {
+  float a[16], b[8], c[4], d[2];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a[i] = (j & 16) ? v[i + 16] : v[i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) b[i] = (j & 8) ? a[i + 8] : a[i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) c[i] = (j & 4) ? b[i + 4] : b[i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) d[i] = (j & 2) ? c[i + 2] : c[i];
+  return (j & 1) ? d[1] : d[0];
+}
+
 using tc::kTileBytes;
 
 template <int ROWS>
@@ -106,10 +121,11 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
   const int r = tid >> 4, c = tid & 15;    // this thread's block inside the tile
   const int wr0 = 2 * warp;                // the warp's first tile row; its window rows span wr0 .. wr0 + w2
   const uint32_t idesc = tc::idesc_bf16(128, N);
-  uint32_t ph_f = 0, ph_g[2] = {0, 0}, ph_m[2] = {0, 0};
-  auto wait = [&](uint64_t *b, uint32_t &ph) {
-    if (!tc::mbar_wait(b, ph, abort_flag)) *abort_flag = 1;
-    ph ^= 1;
+  // phase parities: bit 0 F, bits 1-2 the G buffers, bits 3-4 the accumulators
+  uint32_t phase = 0;
+  auto wait = [&](uint64_t *b, int bit) {
+    if (!tc::mbar_wait(b, (phase >> bit) & 1u, abort_flag)) *abort_flag = 1;
+    phase ^= 1u << bit;
   };
   const int total = batch.tile_end[batch.n - 1];
   for (;;) {
@@ -133,8 +149,8 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
         tc::mbar_arrive_expect_tx(bar + 1 + s, kGBytes);
         tc::tma_load_3d(sG[s], tmG, 0, tx0 - sa, ty0 - sa + s * ROWS, bar + 1 + s);
       }
-      wait(bar, ph_f);
-      wait(bar + 1, ph_g[0]);
+      wait(bar, 0);
+      wait(bar + 1, 1);
       tc::tc_fence_after();
       const uint32_t fa = tc::smem_addr(sF), ga = tc::smem_addr(sG[0]);
 #pragma unroll
@@ -153,15 +169,16 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
     // window columns j of the union (relative to the block: j - c in [0, w2))
     // that lie inside the frame: tx0 - sa + j in [0, bw)
     const int jlo = max(c, sa - tx0), jhi = min(c + w2, a.bw - tx0 + sa);
+    const uint32_t cols = jhi > jlo ? (0xFFFFFFFFu >> (32 - (jhi - jlo))) << jlo : 0u;
 #pragma unroll 1
     for (int s = 0; s < nst; ++s) {
       const int b = s & 1;
-      wait(bar + 3 + b, ph_m[b]);
+      wait(bar + 3 + b, 3 + b);
       tc::tc_fence_after();
       if (tid == 0) {
         if (s + 1 < nst) {
           const int b1 = (s + 1) & 1;
-          wait(bar + 1 + b1, ph_g[b1]);
+          wait(bar + 1 + b1, 1 + b1);
           tc::tc_fence_after();
           const uint32_t fa = tc::smem_addr(sF), ga = tc::smem_addr(sG[b1]);
 #pragma unroll
@@ -184,9 +201,18 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
         const int gy = ty0 - sa + ur;
         if (in_frame && ur >= r && ur < r + w2 && gy >= 0 && gy < a.bh) {
           const int prow = (ur - r) * w2 - c;
+          // the window's columns scoring above the current K-th best, then
+          // the insertions (few once the list is full) in scan order
+          const float thr = ts[K - 1];
+          uint32_t m = 0;
 #pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (j >= jlo && j < jhi) topk_insert<K>(ts, tp, v[j], prow + j);
+          for (int j = 0; j < 32; ++j) m |= (v[j] > thr ? 1u : 0u) << j;
+          m &= cols;
+          while (m) {
+            const int j = __ffs(m) - 1;
+            m &= m - 1;
+            topk_insert<K>(ts, tp, pick32(v, j), prow + j);
+          }
         }
       }
       tc::tc_fence_before();

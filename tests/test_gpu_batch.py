@@ -125,3 +125,44 @@ def test_batch_rejects_inter_first_frame(torch_cuda):
     with pytest.raises(MptcError):
         b.encode([False])
     b.close()
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_batch_run_matches_single_streams(torch_cuda, learned):
+    """mptc_batch_encode_run (a run of frames of every stream: intra frames
+    first on per-stream lanes, inter frames step by step) gives every stream's
+    outputs of the same stream encoded alone, with and without a model, over
+    two runs in a row (the streams continue across runs)."""
+    torch = torch_cuda
+    from mptc_gb300.batch import BatchEncoder
+    from mptc_gb300.model import ProposalModel
+    sizes = [(256, 128), (128, 96), (64, 64)]
+    nf, runs = 6, 2
+    streams = [StreamSpec(w, h, nf * runs, seed=90 + k, square_size=32).generate() for k, (w, h) in enumerate(sizes)]
+    flags = [[f == 0 or f % 4 == k for f in range(nf * runs)] for k in range(len(sizes))]
+    model = ProposalModel(seed=9) if learned else None
+    ref = [single_learned(streams[k], 8, 5, flags[k], model, 8) if learned else single(streams[k], 8, 5, 16, flags[k])
+           for k in range(len(sizes))]
+    b = BatchEncoder(sizes, 8, 5, 16)
+    if learned:
+        b.set_model(model, 8)
+    dev = torch.device("cuda")
+    for r in range(runs):
+        lo, hi = r * nf, (r + 1) * nf
+        frames = [torch.from_numpy(streams[k][lo:hi].copy()).to(dev) for k in range(len(sizes))]
+        fins = [torch.empty((nf, b.nblk(k)), dtype=torch.int64, device=dev) for k in range(len(sizes))]
+        mots = [torch.empty((nf, 2 * b.nblk(k)), dtype=torch.uint8, device=dev) for k in range(len(sizes))]
+        unis = [torch.empty((nf, b.nblk(k)), dtype=torch.int32, device=dev) for k in range(len(sizes))]
+        nus = [torch.empty(nf, dtype=torch.int32, device=dev) for k in range(len(sizes))]
+        b.encode_run(frames, fins, mots, unis, nus, [flags[k][lo:hi] for k in range(len(sizes))])
+        torch.cuda.synchronize()
+        for k in range(len(sizes)):
+            for f in range(nf):
+                np.testing.assert_array_equal(fins[k][f].cpu().numpy().view(np.uint64), ref[k][lo + f][0],
+                                              err_msg=f"run {r} stream {k} frame {f}")
+                np.testing.assert_array_equal(mots[k][f].cpu().numpy(), ref[k][lo + f][1])
+                n = int(nus[k][f].item())
+                np.testing.assert_array_equal(unis[k][f, :n].cpu().numpy().view(np.uint32), ref[k][lo + f][2])
+    b.close()
+    if model is not None:
+        model.close()
