@@ -760,13 +760,16 @@ def run_learned(args, rank: int, world: int, dist) -> None:
         model = ProposalModel(seed=1)
         enc = Encoder(W, H, SA, THR, II)
         enc.set_model(model, args.topk or 8)
+        from mptc_gb300._lib import check, lib
+        check(lib().mptc_ctx_set_learned_shape(enc.handle, args.score_rows), enc.handle)
         fps = time_stream_call(torch, enc, frames_dev, sched, max(1, args.steps), max(1, args.warmup))
         enc.set_kernel_timing(True)
         time_stream_call(torch, enc, frames_dev, sched, 1, 0)
         enc.set_kernel_timing(False)
         kt = enc.kernel_times()
         if rank == 0:
-            print(json.dumps(dict(quick=True, learned=True, frames=nf, value=round(fps, 2), kernels={
+            print(json.dumps(dict(quick=True, learned=True, frames=nf, score_rows=args.score_rows, topk=args.topk or 8,
+                                  value=round(fps, 2), kernels={
                 k: {"launches": v[0], "total_ms": round(v[1], 3)} for k, v in kt.items()})), flush=True)
         enc.close()
         model.close()
@@ -802,6 +805,8 @@ def main() -> None:
     ap.add_argument("--learned", action="store_true",
                     help="learned proposal: train on 200 separate seeded frames, then time plain vs learned")
     ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--score-rows", type=int, default=8, choices=(4, 8),
+                    help="--learned --quick: candidate rows per stage of the window scoring")
     ap.add_argument("--no-learned", action="store_true",
                     help="default run without the learned-proposal comparison")
     ap.add_argument("--topk", type=int, default=0,

@@ -57,9 +57,10 @@ __device__ __forceinline__ void block_feature_cols(const uint32_t (&w)[12], cons
   }
 }
 
-__device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ rgb, int width, int bx, int by,
-                                                   uint64_t stb, int half, uint32_t (&out)[16]) {
-  uint32_t w[12];
+// The block's 48 pixel bytes as 12 words (rows of 12 bytes; frame rows are a
+// multiple of 4 bytes apart).
+__device__ __forceinline__ void load_block_words(const uint8_t *__restrict__ rgb, int width, int bx, int by,
+                                                 uint32_t (&w)[12]) {
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const uint32_t *p = reinterpret_cast<const uint32_t *>(rgb + ((size_t)(4 * by + r) * width + 4 * bx) * 3);
@@ -67,6 +68,11 @@ __device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ r
     w[3 * r + 1] = __ldg(p + 1);
     w[3 * r + 2] = __ldg(p + 2);
   }
+}
+
+// Feature half `half` from the block's pixel words and stb block.
+__device__ __forceinline__ void block_feature_words(const uint32_t (&w)[12], uint64_t stb, int half,
+                                                    uint32_t (&out)[16]) {
   uint32_t lo[3] = {255u, 255u, 255u}, hi[3] = {0u, 0u, 0u};
 #pragma unroll
   for (int i = 0; i < 48; ++i) {
@@ -82,6 +88,13 @@ __device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ r
     block_feature_cols<1>(w, lo, inv, e1, e2, out);
   else
     block_feature_cols<0>(w, lo, inv, e1, e2, out);
+}
+
+__device__ __forceinline__ void block_feature_half(const uint8_t *__restrict__ rgb, int width, int bx, int by,
+                                                   uint64_t stb, int half, uint32_t (&out)[16]) {
+  uint32_t w[12];
+  load_block_words(rgb, width, bx, by, w);
+  block_feature_words(w, stb, half, out);
 }
 
 // Word features, half `half`: the 32 bits of an index word as 0/1 (half 0),

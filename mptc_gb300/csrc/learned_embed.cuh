@@ -159,27 +159,56 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
   const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
   const int row = 32 * q + lane;
   const int total = batch.tile_end[batch.n - 1];
+  // The next tile is drawn while the current one is in its hidden layers and
+  // its input words are loaded then, so the feature build never waits on
+  // global memory.
+  struct Pending {
+    uint32_t w[12];
+    uint64_t stb;
+    uint32_t word;
+    bool valid;
+  } pf;
+  auto locate = [&](int gt, int &jb, int &tile) {
+    jb = 0;
+    while (gt >= batch.tile_end[jb]) ++jb;
+    tile = gt - (jb ? batch.tile_end[jb - 1] : 0);
+  };
+  auto prefetch = [&](int gt) {
+    pf.valid = false;
+    if (gt >= total) return;
+    int jb, tile;
+    locate(gt, jb, tile);
+    const EmbedArgs &a = batch.a[jb];
+    const int gi = tile * 128 + (tid >> 1);
+    if (gi >= a.n) return;
+    pf.valid = true;
+    if constexpr (kBlocks) {
+      const int bi = a.blocks ? (int)__ldg(a.blocks + gi) : gi;
+      const int by = bi / a.bw, bx = bi - by * a.bw;
+      load_block_words(a.rgb, a.width, bx, by, pf.w);
+      pf.stb = __ldg(a.stb + bi);
+    } else {
+      pf.word = __ldg(a.words + (size_t)gi * a.word_stride);
+    }
+  };
+  if (tid == 0) *s_tile = (int)atomicAdd(batch.next, 1u);
+  __syncthreads();
+  int gt = *s_tile;
+  prefetch(gt);
   for (;;) {
-    if (tid == 0) *s_tile = (int)atomicAdd(batch.next, 1u);
-    __syncthreads();
-    const int gt = *s_tile;
     if (gt >= total || *abort_flag) break;
-    int j = 0;
-    while (gt >= batch.tile_end[j]) ++j;
-    const EmbedArgs &a = batch.a[j];
-    const int tile = gt - (j ? batch.tile_end[j - 1] : 0);
-    // input features -> sA[0]
+    int jb, tile;
+    locate(gt, jb, tile);
+    const EmbedArgs &a = batch.a[jb];
+    // input features -> sA0
     {
-      const int r = tid >> 1, half = tid & 1, gi = tile * 128 + r;
+      const int r = tid >> 1, half = tid & 1;
       uint32_t f[16];
-      if (gi < a.n) {
-        if constexpr (kBlocks) {
-          const int bi = a.blocks ? (int)__ldg(a.blocks + gi) : gi;
-          const int by = bi / a.bw, bx = bi - by * a.bw;
-          block_feature_half(a.rgb, a.width, bx, by, __ldg(a.stb + bi), half, f);
-        } else {
-          word_feature_half(__ldg(a.words + (size_t)gi * a.word_stride), half, f);
-        }
+      if (pf.valid) {
+        if constexpr (kBlocks)
+          block_feature_words(pf.w, pf.stb, half, f);
+        else
+          word_feature_half(pf.word, half, f);
       } else {
 #pragma unroll
         for (int j = 0; j < 16; ++j) f[j] = 0u;
@@ -195,7 +224,9 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
       tc::tc_fence_after();
       issue_chunk(tmem, sA0, sW + Net::kW1, tc::idesc_bf16(128, Net::N1), false);
       tc::mma_commit(bar + 1);
+      *s_tile = (int)atomicAdd(batch.next, 1u);  // the next tile, read after the next barrier
     }
+    int gt_next = total;
     if (!tc::mbar_wait(bar + 1, ph_mma, abort_flag)) *abort_flag = 1;
     ph_mma ^= 1;
     tc::tc_fence_after();
@@ -215,6 +246,10 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
         issue_chunk(tmem + Net::N1, buf, sW + Net::kW2 + (uint32_t)kc * Net::N2 * 128u, tc::idesc_bf16(128, Net::N2),
                     kc > 0);
         tc::mma_commit(bar + 2 + b);
+      }
+      if (kc == 0) {
+        gt_next = *s_tile;
+        prefetch(gt_next);
       }
     }
     wait_buf(0);
@@ -267,6 +302,7 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
     }
     tc::tc_fence_before();
     __syncthreads();
+    gt = gt_next;
   }
   tc::tc_fence_before();
   __syncthreads();
