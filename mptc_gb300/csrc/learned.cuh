@@ -32,10 +32,14 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
 #pragma unroll
       for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < K; k0 += kGBK) {
+  // split K (blockIdx.z): slice z writes its partial product to C + z * M * ldc
+  const int ksplit = gridDim.z > 1 ? (K + gridDim.z - 1) / gridDim.z : K;
+  const int kbeg = blockIdx.z * ((ksplit + kGBK - 1) / kGBK * kGBK);
+  const int kend = min(K, kbeg + (ksplit + kGBK - 1) / kGBK * kGBK);
+  for (int k0 = kbeg; k0 < kend; k0 += kGBK) {
     // tiles with k contiguous in memory move as 16-byte vectors when aligned
-    const bool avec = !TA && (lda % 8 == 0) && (k0 + kGBK <= K) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
-    const bool bvec = TB && (ldb % 8 == 0) && (k0 + kGBK <= K) && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
+    const bool avec = !TA && (lda % 8 == 0) && (k0 + kGBK <= kend) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+    const bool bvec = TB && (ldb % 8 == 0) && (k0 + kGBK <= kend) && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
     if (avec) {
       for (int e = tid; e < kGBM * kGBK / 8; e += 128) {
         const int r = e / (kGBK / 8), c = 8 * (e % (kGBK / 8)), m = m0 + r;
@@ -47,7 +51,7 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
       for (int e = tid; e < kGBM * kGBK; e += 128) {
         const int r = e / kGBK, c = e % kGBK, m = m0 + r, k = k0 + c;
         __nv_bfloat16 v = zero;
-        if (m < M && k < K) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+        if (m < M && k < kend) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
         As[r][c] = v;
       }
     }
@@ -62,7 +66,7 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
       for (int e = tid; e < kGBN * kGBK; e += 128) {
         const int r = e / kGBK, c = e % kGBK, n = n0 + r, k = k0 + c;
         __nv_bfloat16 v = zero;
-        if (n < N && k < K) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
+        if (n < N && k < kend) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
         Bs[r][c] = v;
       }
     }
@@ -101,6 +105,10 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__r
         const int n = n0 + wn + 8 * j + 2 * t + (q & 1);
         if (m >= M || n >= N) continue;
         float v = acc[i][j][q];
+        if (gridDim.z > 1) {  // a K slice: its partial sum into slice z of C (no bias, ReLU or bf16 copy)
+          C[(size_t)blockIdx.z * M * ldc + (size_t)m * ldc + n] = v;
+          continue;
+        }
         if (accumulate && C) v += C[(size_t)m * ldc + n];
         if (bias) v += bias[n];
         if (relu) v = v > 0.f ? v : 0.f;
@@ -157,13 +165,24 @@ __global__ void to_bf16_kernel(const float *__restrict__ x, __nv_bfloat16 *__res
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = __float2bfloat16(x[i]);
 }
 
-// Column sums of d [rows x cols] into db (bias gradient).
-__global__ void colsum_kernel(const float *__restrict__ d, int rows, int cols, float *__restrict__ db) {
+// Partial column sums of d [rows x cols]: slice blockIdx.y sums rows y,
+// y + gridDim.y, ... into part[y * cols + c].
+__global__ void colsum_kernel(const float *__restrict__ d, int rows, int cols, float *__restrict__ part) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= cols) return;
   float s = 0.f;
-  for (int r = 0; r < rows; ++r) s += d[(size_t)r * cols + c];
-  db[c] = s;
+  for (int r = blockIdx.y; r < rows; r += gridDim.y) s += d[(size_t)r * cols + c];
+  part[(size_t)blockIdx.y * cols + c] = s;
+}
+
+// out[i] = sum over slices k = 0 .. slices-1 of part[k * n + i], in slice
+// order (the same bits on every run).
+__global__ void slice_sum_kernel(const float *__restrict__ part, int slices, int n, float *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < slices; ++k) s += part[(size_t)k * n + i];
+    out[i] = s;
+  }
 }
 
 constexpr int kMaxCE = 64;  // candidates per block in one training example

@@ -78,6 +78,7 @@ struct mptc_model {
   __nv_bfloat16 *emb_tmp = nullptr;
   int emb_cap = 0;
   uint32_t *status = nullptr;
+  float *part = nullptr;  // partial sums of the split gradient reductions
 };
 
 namespace {
@@ -124,10 +125,26 @@ void gemm_fwd(const bf16 *x, const bf16 *W, const float *b, float *y, bf16 *yb, 
   mptc::gemm_bf16_kernel<false, false><<<grid, 128, 0, s>>>(x, K, W, N, y, yb, N, b, M, N, K, relu ? 1 : 0, 0);
 }
 
-// dW[K x N] = x^T[K x M] dy[M x N]
-void gemm_dw(const bf16 *x, const bf16 *dy, float *dW, int M, int K, int N, cudaStream_t s) {
-  dim3 grid((N + mptc::kGBN - 1) / mptc::kGBN, (K + mptc::kGBM - 1) / mptc::kGBM);
-  mptc::gemm_bf16_kernel<true, false><<<grid, 128, 0, s>>>(x, K, dy, N, dW, nullptr, N, nullptr, K, N, M, 0, 0);
+// Partial sums of the split reductions below (slices x outputs floats).
+constexpr size_t kPartFloats = 1 << 20;
+
+// dW[K x N] = x^T[K x M] dy[M x N]: few outputs and a long reduction over the
+// M examples, so the reduction is split into slices of about 2048 rows whose
+// partial products are summed in slice order afterwards (deterministic).
+void gemm_dw(const bf16 *x, const bf16 *dy, float *dW, int M, int K, int N, float *part, cudaStream_t s) {
+  const int splits = (int)std::min<size_t>(std::min(64, std::max(1, M / 2048)), kPartFloats / ((size_t)K * N));
+  dim3 grid((N + mptc::kGBN - 1) / mptc::kGBN, (K + mptc::kGBM - 1) / mptc::kGBM, std::max(1, splits));
+  mptc::gemm_bf16_kernel<true, false><<<grid, 128, 0, s>>>(x, K, dy, N, splits > 1 ? part : dW, nullptr, N, nullptr,
+                                                          K, N, M, 0, 0);
+  if (splits > 1) mptc::slice_sum_kernel<<<blocks_for((size_t)K * N), 256, 0, s>>>(part, splits, K * N, dW);
+}
+
+// Bias gradient db[cols] = column sums of d[rows x cols].
+void colsum(const float *d, int rows, int cols, float *db, float *part, cudaStream_t s) {
+  const int slices = (int)std::min<size_t>(std::min(512, std::max(1, rows / 64)), kPartFloats / cols);
+  dim3 grid((cols + 127) / 128, slices);
+  mptc::colsum_kernel<<<grid, 128, 0, s>>>(d, rows, cols, part);
+  mptc::slice_sum_kernel<<<blocks_for((size_t)cols), 256, 0, s>>>(part, slices, cols, db);
 }
 
 // dx[M x K] = dy[M x N] W^T  (W stored K x N, i.e. "N x K" transposed access)
@@ -167,27 +184,27 @@ mptc_status forward_backward(mptc_model *m, const uint8_t *rgb, int width, int b
   }
   // block MLP
   to_bf16_kernel<<<blocks_for((size_t)B * kEmb), 256, 0, s>>>(m->df, m->dfb, B * kEmb);
-  gemm_dw(m->h2b, m->dfb, G[2], B, kH2, kEmb, s);
-  colsum_kernel<<<1, kEmb, 0, s>>>(m->df, B, kEmb, Gb[2]);
+  gemm_dw(m->h2b, m->dfb, G[2], B, kH2, kEmb, m->part, s);
+  colsum(m->df, B, kEmb, Gb[2], m->part, s);
   gemm_dx(m->dfb, W[2], m->dh2, B, kH2, kEmb, s);
   relu_backward_kernel<<<blocks_for((size_t)B * kH2), 256, 0, s>>>(m->dh2, m->h2, B * kH2);
   to_bf16_kernel<<<blocks_for((size_t)B * kH2), 256, 0, s>>>(m->dh2, m->dh2b, B * kH2);
-  gemm_dw(m->h1b, m->dh2b, G[1], B, kH1, kH2, s);
-  colsum_kernel<<<1, kH2, 0, s>>>(m->dh2, B, kH2, Gb[1]);
+  gemm_dw(m->h1b, m->dh2b, G[1], B, kH1, kH2, m->part, s);
+  colsum(m->dh2, B, kH2, Gb[1], m->part, s);
   gemm_dx(m->dh2b, W[1], m->dh1, B, kH1, kH2, s);
   relu_backward_kernel<<<blocks_for((size_t)B * kH1), 256, 0, s>>>(m->dh1, m->h1, B * kH1);
   to_bf16_kernel<<<blocks_for((size_t)B * kH1), 256, 0, s>>>(m->dh1, m->dh1b, B * kH1);
-  gemm_dw(m->x, m->dh1b, G[0], B, kFeatPad, kH1, s);
-  colsum_kernel<<<1, kH1, 0, s>>>(m->dh1, B, kH1, Gb[0]);
+  gemm_dw(m->x, m->dh1b, G[0], B, kFeatPad, kH1, m->part, s);
+  colsum(m->dh1, B, kH1, Gb[0], m->part, s);
   // candidate MLP
   to_bf16_kernel<<<blocks_for((size_t)BC * kEmb), 256, 0, s>>>(m->dgg, m->dggb, BC * kEmb);
-  gemm_dw(m->g1b, m->dggb, G[4], BC, kCandH, kEmb, s);
-  colsum_kernel<<<1, kEmb, 0, s>>>(m->dgg, BC, kEmb, Gb[4]);
+  gemm_dw(m->g1b, m->dggb, G[4], BC, kCandH, kEmb, m->part, s);
+  colsum(m->dgg, BC, kEmb, Gb[4], m->part, s);
   gemm_dx(m->dggb, W[4], m->dg1, BC, kCandH, kEmb, s);
   relu_backward_kernel<<<blocks_for((size_t)BC * kCandH), 256, 0, s>>>(m->dg1, m->g1, BC * kCandH);
   to_bf16_kernel<<<blocks_for((size_t)BC * kCandH), 256, 0, s>>>(m->dg1, m->dg1b, BC * kCandH);
-  gemm_dw(m->xc, m->dg1b, G[3], BC, kCandIn, kCandH, s);
-  colsum_kernel<<<1, kCandH, 0, s>>>(m->dg1, BC, kCandH, Gb[3]);
+  gemm_dw(m->xc, m->dg1b, G[3], BC, kCandIn, kCandH, m->part, s);
+  colsum(m->dg1, BC, kCandH, Gb[3], m->part, s);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
 }
 
@@ -288,7 +305,7 @@ mptc_status mptc_model_create(uint64_t seed, mptc_model **out) {
   if (!m) return MPTC_ENOMEM;
   const size_t n = kOff.total;
   if (dmalloc(&m->w, n) || dmalloc(&m->wb, n) || dmalloc(&m->g, n) || dmalloc(&m->m, n) || dmalloc(&m->v, n) ||
-      dmalloc(&m->loss, 1) || dmalloc(&m->img, mptc::kImgBytes) || dmalloc(&m->status, 4) ||
+      dmalloc(&m->loss, 1) || dmalloc(&m->img, mptc::kImgBytes) || dmalloc(&m->status, 4) || dmalloc(&m->part, kPartFloats) ||
       cudaMemset(m->img, 0, mptc::kImgBytes) != cudaSuccess || cudaMemset(m->status, 0, 16) != cudaSuccess) {
     mptc_model_destroy(m);
     return MPTC_ENOMEM;
@@ -330,6 +347,7 @@ mptc_status mptc_model_destroy(mptc_model *m) {
   cudaFree(m->img);
   cudaFree(m->emb_tmp);
   cudaFree(m->status);
+  cudaFree(m->part);
   delete m;
   return MPTC_OK;
 }
