@@ -58,17 +58,37 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// One try_wait that lets the hardware suspend the thread until the phase
+// completes or `hint_ns` nanoseconds have passed (no instructions issue while
+// it is suspended).
+__device__ __forceinline__ bool mbar_test_suspend(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Waits until the phase with the given parity has completed; false after
-// `limit_ns` nanoseconds (or at once when *abort is set by another wait of the
-// same CTA that already gave up).
+// about `limit_ns` nanoseconds (or soon after *abort is set by another wait of
+// the same CTA that already gave up). The thread sleeps in the try_wait
+// between checks; the clock and the abort flag are read every 16 tries.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, const volatile uint32_t *abort,
                                           uint64_t limit_ns = 1000000000ull) {
   if (mbar_test(bar, parity)) return true;
-  const uint64_t t0 = global_ns();
-  for (;;) {
-    if (mbar_test(bar, parity)) return true;
-    if (*abort) return false;
-    if (global_ns() - t0 > limit_ns) return false;
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_test_suspend(bar, parity, 100000u)) return true;
+    if ((it & 15u) == 15u) {
+      if (*abort) return false;
+      const uint64_t t = global_ns();
+      if (t0 == 0) t0 = t;
+      else if (t - t0 > limit_ns) return false;
+    }
   }
 }
 
