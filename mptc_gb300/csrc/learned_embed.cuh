@@ -94,12 +94,21 @@ constexpr size_t embed_smem_bytes() {
 // swizzled operand tile.
 __device__ __forceinline__ void epilogue_to_tile(uint32_t taddr, const float *__restrict__ bias, uint8_t *tile,
                                                  int row, int h) {
-  float v[32];
+  float v[32], bb[32];
+  const float4 *b4 = reinterpret_cast<const float4 *>(bias);  // 32 biases, 16-byte aligned
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float4 t = __ldg(b4 + j);
+    bb[4 * j] = t.x;
+    bb[4 * j + 1] = t.y;
+    bb[4 * j + 2] = t.z;
+    bb[4 * j + 3] = t.w;
+  }
   tc::tmem_ld32(taddr, v);
   uint32_t pk[16];
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
-    const float x0 = fmaxf(v[2 * j] + __ldg(bias + 2 * j), 0.f), x1 = fmaxf(v[2 * j + 1] + __ldg(bias + 2 * j + 1), 0.f);
+    const float x0 = fmaxf(v[2 * j] + bb[2 * j], 0.f), x1 = fmaxf(v[2 * j + 1] + bb[2 * j + 1], 0.f);
     const __nv_bfloat162 b = __floats2bfloat162_rn(x0, x1);
     pk[j] = *reinterpret_cast<const uint32_t *>(&b);
   }
@@ -127,7 +136,7 @@ __device__ __forceinline__ void issue_chunk(uint32_t d_tmem, const uint8_t *a_ti
 template <class Net, bool kBlocks>
 __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_constant__ EmbedBatch batch) {
   extern __shared__ uint8_t dsm[];
-  uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(dsm) + 1023) & ~uintptr_t(1023));
+  uint8_t *sm = tc::align_1024(dsm);
   uint8_t *sW = sm;
   uint8_t *const sA0 = sm + Net::kWBytes, *const sA1 = sm + Net::kWBytes + kTileBytes;
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm + Net::kWBytes + 2 * kTileBytes);  // weights, mma, buf0, buf1
@@ -284,15 +293,23 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
     }
     // embedding: 64 columns, half h of them per warp, + bias, bf16 to the output row
     {
-      float v[32];
+      float v[32], bb[32];
+      const float4 *b4 = reinterpret_cast<const float4 *>(out_bias + 32 * h);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float4 t = __ldg(b4 + j);
+        bb[4 * j] = t.x;
+        bb[4 * j + 1] = t.y;
+        bb[4 * j + 2] = t.z;
+        bb[4 * j + 3] = t.w;
+      }
       tc::tmem_ld32(lane_base + out_col + 32 * h, v);
       const int gi = tile * 128 + row;
       if (gi < a.n) {
         uint32_t pk[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] + __ldg(out_bias + 32 * h + 2 * j),
-                                                          v[2 * j + 1] + __ldg(out_bias + 32 * h + 2 * j + 1));
+          const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] + bb[2 * j], v[2 * j + 1] + bb[2 * j + 1]);
           pk[j] = *reinterpret_cast<const uint32_t *>(&b2);
         }
         uint4 *dst = reinterpret_cast<uint4 *>(a.out + (size_t)gi * kEmb + 32 * h);

@@ -50,7 +50,7 @@ struct mptc_ctx {
   int topk_k = 0, score_rows = 8;
   __nv_bfloat16 *femb = nullptr, *gemb = nullptr;
   uint16_t *topk = nullptr;
-  CUtensorMap tm_f{}, tm_g4{}, tm_g8{};
+  CUtensorMap tm_f{};  // F rows in boxes of one block column, 16 rows
   // device scratch
   uint64_t *done = nullptr;        // per block completion words
   // [0] dataflow counter, [1] status, [2..4] stats, [5] pending count,
@@ -380,23 +380,23 @@ bool embedding_map(CUtensorMap *m, void *base, int bw, int bh, int box_w, int bo
          CUDA_SUCCESS;
 }
 
-// The scoring kernels' shared memory: ROWS = 8 stages use 512 TMEM columns and
-// ask for 120 KB (one CTA per SM); ROWS = 4 use 256 and ask for 80 KB (two).
-template <int ROWS>
+// The scoring kernels' shared memory (palette, slices, first offsets and
+// the blocks' lists): one CTA per SM.
+template <int ROWS, int K>
 constexpr int score_smem() {
-  return (int)std::max<size_t>(mptc::score_smem_bytes<ROWS>(), ROWS == 8 ? 122880 : 81920);
+  return (int)mptc::score_smem_bytes<ROWS, K>();
 }
 
 template <int ROWS, int K>
 cudaError_t score_attr() {
   return cudaFuncSetAttribute(mptc::score_topk_tc_kernel<ROWS, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              score_smem<ROWS>());
+                              score_smem<ROWS, K>());
 }
 
 template <int ROWS, int K>
 void launch_score(const mptc::ScoreBatch &sb, int sm_count, cudaStream_t s) {
-  const int grid = std::min(sb.tile_end[sb.n - 1], sm_count * (ROWS == 8 ? 1 : 2));
-  mptc::score_topk_tc_kernel<ROWS, K><<<grid, mptc::kScoreThreads, score_smem<ROWS>(), s>>>(sb);
+  const int grid = std::min(sb.tile_end[sb.n - 1], sm_count);
+  mptc::score_topk_tc_kernel<ROWS, K><<<grid, mptc::kScoreThreads, score_smem<ROWS, K>(), s>>>(sb);
 }
 
 template <int K>
@@ -459,7 +459,7 @@ int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream
   eb.n = n;
   mptc::ListBatch lb{};
   lb.n = n;
-  const bool r8 = c0->score_rows == 8;
+  const bool r8 = c0->score_rows == 8;  // 128- or 64-entry palette slices
   const int bpw = 32 / c0->topk_k;
   int tiles = 0, groups = 0;
   for (int j = 0; j < n; ++j) {
@@ -467,9 +467,9 @@ int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream
     tiles += ((c->bw + mptc::kScoreTileW - 1) / mptc::kScoreTileW) *
              ((c->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
     sb.tile_end[j] = tiles;
-    sb.a[j] = mptc::ScoreArgs{c->bw, c->bh, c->cfg.search_area, c->topk, c->work + 1};
+    sb.a[j] = mptc::ScoreArgs{c->bw, c->bh, c->cfg.search_area, reinterpret_cast<const uint32_t *>(jobs[j].P.prev) + 1,
+                              2, c->gemb, c->topk, c->work + 1};
     sb.tmF[j] = c->tm_f;
-    sb.tmG[j] = r8 ? c->tm_g8 : c->tm_g4;
     groups += (c->nblk + bpw - 1) / bpw;
     eb.group_end[j] = groups;
     eb.P[j] = jobs[j].P;
@@ -1090,9 +1090,7 @@ mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k
   if (!ctx->femb) {
     if (dalloc(&ctx->femb, n * mptc::kEmb) || dalloc(&ctx->gemb, n * mptc::kEmb) || dalloc(&ctx->topk, n * mptc::kMaxK))
       return fail(ctx, MPTC_ENOMEM, "learned proposal buffers");
-    if (!embedding_map(&ctx->tm_f, ctx->femb, ctx->bw, ctx->bh, mptc::kScoreTileW, mptc::kScoreTileH) ||
-        !embedding_map(&ctx->tm_g4, ctx->gemb, ctx->bw, ctx->bh, 32, 4) ||
-        !embedding_map(&ctx->tm_g8, ctx->gemb, ctx->bw, ctx->bh, 32, 8))
+    if (!embedding_map(&ctx->tm_f, ctx->femb, ctx->bw, ctx->bh, 1, mptc::kScoreTileH))
       return fail(ctx, MPTC_ECUDA, "learned proposal: tensor map encoding failed");
     MPTC_CUDA((score_attr<8, 4>()));
     MPTC_CUDA((score_attr<8, 8>()));
@@ -1141,10 +1139,10 @@ mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const 
   sb.next = ctx->work + 14;
   sb.tile_end[0] = ((ctx->bw + mptc::kScoreTileW - 1) / mptc::kScoreTileW) *
                    ((ctx->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
-  sb.a[0] = mptc::ScoreArgs{ctx->bw, ctx->bh, ctx->cfg.search_area, ctx->topk, ctx->work + 1};
+  sb.a[0] = mptc::ScoreArgs{ctx->bw, ctx->bh, ctx->cfg.search_area, reinterpret_cast<const uint32_t *>(prev_final_dev) + 1,
+                            2, ctx->gemb, ctx->topk, ctx->work + 1};
   const bool r8 = ctx->score_rows == 8;
   sb.tmF[0] = ctx->tm_f;
-  sb.tmG[0] = r8 ? ctx->tm_g8 : ctx->tm_g4;
   switch (ctx->topk_k) {
     case 4: r8 ? launch_score<8, 4>(sb, ctx->sm_count, s) : launch_score<4, 4>(sb, ctx->sm_count, s); break;
     case 16: r8 ? launch_score<8, 16>(sb, ctx->sm_count, s) : launch_score<4, 16>(sb, ctx->sm_count, s); break;

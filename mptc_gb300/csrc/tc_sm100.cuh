@@ -196,6 +196,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// The first 1024-byte aligned byte of dynamic shared memory at or after p.
+// The offset is added to p itself (no round trip through an integer), so
+// the compiler still sees a shared-memory pointer and emits shared-memory
+// loads, stores and atomics rather than generic ones.
+__device__ __forceinline__ uint8_t *align_1024(uint8_t *p) {
+  const uint32_t a = smem_addr(p);
+  return p + (((a + 1023u) & ~1023u) - a);
+}
+
 // One operand tile of 128 rows x 64 bf16 (128 bytes per row).
 constexpr uint32_t kTileBytes = 128 * 128;
 

@@ -132,18 +132,25 @@ def test_embeddings_match_cpu_reference(torch_cuda):
     m.close()
 
 
-def test_proposals_are_the_top_scored_distinct_words(torch_cuda):
+@pytest.mark.parametrize("content", ["stream", "noise"])
+def test_proposals_are_the_top_scored_distinct_words(torch_cuda, content):
     """mptc_learned_proposals against scores recomputed on the CPU from the
     same embeddings: in-frame window positions, K distinct words, each at its
     first position in scan order, and no word left out that scores clearly
-    above the lowest one kept (the approximate top-K of an FP32 dot product)."""
+    above the lowest one kept (the approximate top-K of an FP32 dot product).
+    The stream frames' final blocks repeat dictionary words (a tile's word
+    palette fits one slice); the noise frames' words are nearly all distinct,
+    so a tile's palette spans several slices of 128 and of 64 entries."""
     torch = torch_cuda
     from mptc_gb300._lib import check, lib
     from mptc_gb300.encoder import Encoder
     from mptc_gb300.model import ProposalModel
     from mptc_gb300.training import window_words
     w, h, sa, K = 256, 192, 8, 8
-    frames = StreamSpec(w, h, 2, seed=21, n_squares=2, square_size=48).generate()
+    if content == "stream":
+        frames = StreamSpec(w, h, 2, seed=21, n_squares=2, square_size=48).generate()
+    else:
+        frames = np.random.default_rng(22).integers(0, 256, size=(2, h, w, 3), dtype=np.uint8)
     bw, bh = w // 4, h // 4
     n = bw * bh
     enc = Encoder(w, h, sa, 5, 16)
