@@ -683,6 +683,8 @@ def learned_comparison(args, torch, dev, frames_dev, plain_fps, log):
     # K: given, or the fastest that stays within half the PSNR budget on
     # separate calibration frames, judged by the exhaustive search
     calib = torch.from_numpy(FHD1080_CALIB.generate()).to(dev)
+    if getattr(args, "save_model", ""):
+        model.save(args.save_model)
     K, k_table = choose_topk(torch, model, calib, SA, THR, II, ks=(args.topk,) if args.topk > 0 else (4, 8, 16),
                              log=log)
     del calib
@@ -758,6 +760,8 @@ def run_learned(args, rank: int, world: int, dist) -> None:
         # learned stream call only (no training, quality or batch runs)
         from mptc_gb300.model import ProposalModel
         model = ProposalModel(seed=1)
+        if args.model:
+            model.load(args.model)
         enc = Encoder(W, H, SA, THR, II)
         enc.set_model(model, args.topk or 8)
         from mptc_gb300._lib import check, lib
@@ -811,6 +815,10 @@ def main() -> None:
                     help="default run without the learned-proposal comparison")
     ap.add_argument("--topk", type=int, default=0,
                     help="proposals per block (4, 8, 16); 0 = chosen on calibration frames")
+    ap.add_argument("--save-model", default="",
+                    help="--learned: write the trained model's weights to this file")
+    ap.add_argument("--model", default="",
+                    help="--learned --quick: weights to load (a file --save-model wrote) instead of an untrained model")
     ap.add_argument("--quick", action="store_true",
                     help="device-timed region only: no e2e pass, CPU baseline or ALU probe (profiling)")
     args = ap.parse_args()
