@@ -810,7 +810,7 @@ def main() -> None:
                     help="learned proposal: train on 200 separate seeded frames, then time plain vs learned")
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--score-rows", type=int, default=8, choices=(4, 8),
-                    help="--learned --quick: candidate rows per stage of the window scoring")
+                    help="--learned --quick: dictionary slice per stage of the window scoring (x16 words)")
     ap.add_argument("--no-learned", action="store_true",
                     help="default run without the learned-proposal comparison")
     ap.add_argument("--topk", type=int, default=0,

@@ -230,7 +230,8 @@ mptc_status mptc_batch_encode_run(mptc_batch *batch, int32_t n_frames, const uin
  * fastest: warps (blocks) per CTA of the exhaustive inter search (2, 4; with a
  * model attached the current value is kept), the CTA count of each stream's
  * intra dataflow (all, 8, 4, 2 or 1 per SM) and, with a model attached, the
- * candidate rows per pipeline stage of the window scoring (4 or 8). Writes the
+ * dictionary slice per pipeline stage of the window scoring (4 or 8: 64 or
+ * 128 words, mptc_ctx_set_learned_shape). Writes the
  * chosen values (any pointer may be NULL; synchronises). The number of
  * proposals K is set with the model (mptc_batch_set_model): it changes the
  * encoder's output, so it is chosen against the exhaustive search's quality,
@@ -243,8 +244,9 @@ mptc_status mptc_batch_autotune(mptc_batch *batch, const int32_t *is_intra, int3
  * per channel to the block's range, and the stb endpoints) and a candidate MLP
  * g (32 -> 128 -> 64 over an index word's bits) score window candidates by
  * f(block) . g(candidate). With a model attached, the inter search scores
- * every window position on the tcgen05 tensor cores, tests only the K
- * best-scored distinct index words exactly, applies the reference's selection
+ * each block against the distinct index words of its window on the tcgen05
+ * tensor cores (per tile of 16 x 8 blocks, against the words of the tile's
+ * window union), tests only the K best-scored words exactly, applies the reference's selection
  * rule to those K positions and accepts under the error threshold; a block
  * none of whose K proposals passes goes to the exhaustive search. Every
  * accepted block meets the reference's acceptance rule and the stream stays a
@@ -292,9 +294,10 @@ mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k
  * topk_dev: blocks x 16 u16. Synchronises `stream`. */
 mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev,
                                    const uint64_t *prev_final_dev, uint16_t *topk_dev, void *stream);
-/* Candidate window rows staged per pipeline stage of the scoring kernel (4 or
- * 8; the default 8): 8 rows make 256-candidate MMAs, one CTA per SM; 4 rows
- * 128-candidate MMAs, two CTAs per SM. Results do not depend on it. */
+/* The dictionary slice of a pipeline stage of the scoring kernel, as 4 or 8
+ * (the default): each stage scores a tile's 128 blocks against 16 x that many
+ * distinct words of the tile's window union (64 or 128 words per tcgen05 MMA);
+ * a union with more words takes more stages. Results do not depend on it. */
 mptc_status mptc_ctx_set_learned_shape(mptc_ctx *ctx, int32_t rows_per_stage);
 /* Attaches (or detaches) a model to every stream of a batch. */
 mptc_status mptc_batch_set_model(mptc_batch *batch, const mptc_model *model, int32_t k);

@@ -112,7 +112,8 @@ class BatchEncoder:
     def autotune(self, is_intra: list[bool], stream=None) -> dict:
         """Times the launch shapes on the current inputs and keeps the fastest;
         returns the chosen inter warps per CTA, intra CTAs per stream (0: all)
-        and scoring rows per stage."""
+        and the scoring's dictionary slice per stage (4 or 8: 64 or 128 words
+        per MMA)."""
         arr = (ctypes.c_int32 * self.n)(*[int(bool(f)) for f in is_intra])
         w, c, r = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
         s = ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
