@@ -484,6 +484,58 @@ __global__ void __launch_bounds__(256) weight_desc_kernel(const uint64_t *__rest
 // own thread, then the closed-form selection over the CTA (cta_select). The
 // many distinct words of such windows are evaluated side by side instead of
 // in a warp's successive rounds.
+// One listed block searched by a CTA (THREADS >= 256, sa <= 8): thread t
+// evaluates window position t, then the CTA-wide closed-form selection.
+// Starts with a barrier (the previous block's readers of s_tab are done).
+template <int THREADS>
+__device__ __forceinline__ void cta_block_search(const SearchParams &P, int idx, BlockTab &s_tab,
+                                                 const uint8_t *s_snap5, const uint8_t *s_snap6,
+                                                 CtaReduce<THREADS> &red, int *s_sumsq) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w2 = 2 * P.sa, npos = w2 * w2;
+  const int row = tid / w2, col = tid - row * w2;  // the thread's window position tid
+  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
+  const int by = idx / P.bw, bx = idx - by * P.bw;
+  const uint64_t stb = __ldg(P.stb + idx);
+  const uint32_t own = (uint32_t)(stb >> 32);
+  __syncthreads();
+  if (tid < 32) {
+    const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
+    if (tid == 0) *s_sumsq = sq;
+  }
+  __syncthreads();
+  const int orig = __ldg(P.orig_err + idx), sumsq = *s_sumsq;
+  const PixelGroups pg = load_groups(s_tab);
+  LaneSel ls;
+  uint32_t cand = own, eps = 0;
+  const int j = by - P.sa + row, i = bx - P.sa + col;
+  if (tid < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
+    const size_t nidx = (size_t)j * P.bw + i;
+    cand = __ldg(prev_hi + 2 * nidx);
+    int e = 0;  // the block's own word: the stb block, no refit
+    if (cand != own) {
+      const float4 d = __ldg(P.wdesc + nidx);
+      const WeightSums ws{d.x, d.y, d.z, d.w};
+      int refit = 0;
+      e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
+    }
+    ls.add(tid, row, e);
+  }
+  int m, pick;
+  const int sel = cta_select<THREADS>(ls, red, w2, m, pick);
+  const bool accept = sel >= 0 && m <= P.thr;  // CTA-uniform
+  if (accept ? tid == sel : tid == 0) {
+    uint64_t word = 0;
+    if (accept) {
+      const uint64_t blk = cand == own ? stb : ((uint64_t)eps | ((uint64_t)cand << 32));
+      P.final_blk[idx] = blk;
+      P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
+      word = done_word(blk);
+    }
+    P.done[idx] = word;
+  }
+}
+
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) inter_overflow_kernel(SearchParams P, const uint32_t *__restrict__ list,
                                                                  const uint32_t *__restrict__ count) {
@@ -496,52 +548,8 @@ __global__ void __launch_bounds__(THREADS) inter_overflow_kernel(SearchParams P,
   __shared__ int s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
   CtaReduce<THREADS> red{s_red, 0};
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int w2 = 2 * P.sa, npos = w2 * w2;
-  const int row = tid / w2, col = tid - row * w2;  // the thread's window position tid
-  const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
-  for (int k = blockIdx.x; k < n; k += gridDim.x) {
-    const int idx = (int)__ldcg(list + k);
-    const int by = idx / P.bw, bx = idx - by * P.bw;
-    const uint64_t stb = __ldg(P.stb + idx);
-    const uint32_t own = (uint32_t)(stb >> 32);
-    __syncthreads();  // the previous block's readers of s_tab are done
-    if (tid < 32) {
-      const int sq = stage_block(s_tab, P.rgb, P.width, bx, by, lane);
-      if (tid == 0) s_sumsq = sq;
-    }
-    __syncthreads();
-    const int orig = __ldg(P.orig_err + idx), sumsq = s_sumsq;
-    const PixelGroups pg = load_groups(s_tab);
-    LaneSel ls;
-    uint32_t cand = own, eps = 0;
-    const int j = by - P.sa + row, i = bx - P.sa + col;
-    if (tid < npos && i >= 0 && j >= 0 && i < P.bw && j < P.bh) {
-      const size_t nidx = (size_t)j * P.bw + i;
-      cand = __ldg(prev_hi + 2 * nidx);
-      int e = 0;  // the block's own word: the stb block, no refit
-      if (cand != own) {
-        const float4 d = __ldg(P.wdesc + nidx);
-        const WeightSums ws{d.x, d.y, d.z, d.w};
-        int refit = 0;
-        e = eval_candidate(s_tab, pg, s_snap5, s_snap6, cand, ws, own, orig, sumsq, eps, refit);
-      }
-      ls.add(tid, row, e);
-    }
-    int m, pick;
-    const int sel = cta_select<THREADS>(ls, red, w2, m, pick);
-    const bool accept = sel >= 0 && m <= P.thr;  // CTA-uniform
-    if (accept ? tid == sel : tid == 0) {
-      uint64_t word = 0;
-      if (accept) {
-        const uint64_t blk = cand == own ? stb : ((uint64_t)eps | ((uint64_t)cand << 32));
-        P.final_blk[idx] = blk;
-        P.motion[idx] = (uint16_t)((col | 0x80) | ((row | 0x80) << 8));
-        word = done_word(blk);
-      }
-      P.done[idx] = word;
-    }
-  }
+  for (int k = blockIdx.x; k < n; k += gridDim.x)
+    cta_block_search<THREADS>(P, (int)__ldcg(list + k), s_tab, s_snap5, s_snap6, red, &s_sumsq);
 }
 
 }  // namespace mptc

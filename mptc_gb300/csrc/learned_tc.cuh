@@ -598,7 +598,11 @@ __global__ void __launch_bounds__(WARPS * 32) learned_eval_kernel(const __grid_c
 }
 
 // The exhaustive inter search (InterBlockSearch, codec/dxt_image.cpp:715-774)
-// of the listed blocks, one warp per block.
+// of the listed blocks (sa <= 8), one CTA per block, one window position per
+// thread: the short lists of blocks none of whose proposals passed, searched
+// side by side so that the kernel ends with its slowest block's 256
+// evaluations in parallel rather than a warp's successive rounds. The jobs'
+// lists are taken as one concatenated list.
 struct ListBatch {
   int n;
   SearchParams P[kMaxBatch];
@@ -606,32 +610,28 @@ struct ListBatch {
   const uint32_t *count[kMaxBatch];
 };
 
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) inter_list_kernel(const __grid_constant__ ListBatch batch) {
-  __shared__ BlockTab s_tab[WARPS];
-  __shared__ DedupTab s_dd[WARPS];
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) inter_list_kernel(const __grid_constant__ ListBatch batch) {
+  static_assert(THREADS >= 256, "one thread per position of a 16x16 window");
+  int total = 0;
+  for (int j = 0; j < batch.n; ++j) total += (int)__ldcg(batch.count[j]);
+  if ((int)blockIdx.x >= total) return;  // the whole CTA, before its barriers
+  __shared__ BlockTab s_tab;
   __shared__ uint8_t s_snap5[256], s_snap6[256];
+  __shared__ int s_red[2 * (THREADS / 32)];
+  __shared__ int s_sumsq;
   build_snap_tables(s_snap5, s_snap6);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // the jobs' lists one after the other, every warp of the grid on each
-  int off = 0;
-  for (int jb = 0; jb < batch.n; ++jb) {
-  const SearchParams &P = batch.P[jb];
-  const uint32_t *__restrict__ list = batch.list[jb];
-  const int n = (int)*batch.count[jb];
-  const int start = (blockIdx.x * WARPS + warp - off % (gridDim.x * WARPS) + gridDim.x * WARPS) % (gridDim.x * WARPS);
-  off += n;
-  for (int k = start; k < n; k += gridDim.x * WARPS) {
-    const int idx = (int)list[k];
-    const int by = idx / P.bw, bx = idx - by * P.bw;
-    const int sumsq = stage_block(s_tab[warp], P.rgb, P.width, bx, by, lane);
-    const PixelGroups pg = load_groups(s_tab[warp]);
-    const uint64_t word = inter_block_search(P, s_tab[warp], s_dd[warp], pg, s_snap5, s_snap6, idx, bx, by,
-                                             P.stb[idx], P.orig_err[idx], sumsq, lane);
-    if (lane == 0) P.done[idx] = word;
-    __syncwarp();
-  }
+  CtaReduce<THREADS> red{s_red, 0};
+  for (int k = blockIdx.x; k < total; k += gridDim.x) {
+    int jb = 0, off = 0;
+    for (;;) {
+      const int c = (int)__ldcg(batch.count[jb]);
+      if (k - off < c) break;
+      off += c;
+      ++jb;
+    }
+    cta_block_search<THREADS>(batch.P[jb], (int)__ldcg(batch.list[jb] + (k - off)), s_tab, s_snap5, s_snap6, red,
+                              &s_sumsq);
   }
 }
 

@@ -499,7 +499,7 @@ int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream
   }
   {
     KernelTimer t(c0, K_FALLBACK, s);
-    mptc::inter_list_kernel<4><<<sms * 8, 4 * 32, 0, s>>>(lb);
+    mptc::inter_list_kernel<256><<<sms * 4, 256, 0, s>>>(lb);  // CTAs past the lists' end return at once
   }
   return 5;
 }
