@@ -112,6 +112,54 @@ __device__ __forceinline__ int stage_block(BlockTab &t, const uint8_t *__restric
   return __reduce_add_sync(kFull, sq);
 }
 
+// Stages two blocks with one warp, lanes 0-15 the pixels of block (ax, ay)
+// into ta, lanes 16-31 those of (bx2, by2) into tb (a block with has_* false
+// is not read); the same tables as stage_block. Returns each lane's half's sum
+// of squared pixel values.
+__device__ __forceinline__ int stage_block_pair(BlockTab &ta, BlockTab &tb, const uint8_t *__restrict__ rgb,
+                                                int width, int ax, int ay, bool has_a, int bx2, int by2, bool has_b,
+                                                int lane) {
+  const int half = lane >> 4, p = lane & 15;
+  BlockTab &t = half ? tb : ta;
+  const bool has = half ? has_b : has_a;
+  const int bx = half ? bx2 : ax, by = half ? by2 : ay;
+  int sq = 0;
+  uint32_t pk = 0;
+  if (has) {
+    const int r = p >> 2, c = p & 3;
+    const uint8_t *px = rgb + ((size_t)(4 * by + r) * width + 4 * bx + c) * 3;
+    const uint32_t R = px[0], G = px[1], B = px[2];
+    const float third = __fdiv_rn(1.0f, 3.0f);
+    const float fr = __uint2float_rn(R), fg = __uint2float_rn(G), fb = __uint2float_rn(B);
+    const float qr = __fmul_rn(fr, third), qg = __fmul_rn(fg, third), qb = __fmul_rn(fb, third);
+    const float4 P = make_float4(fr, fg, fb, 0.0f), Z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 Q = make_float4(qr, qg, qb, 0.0f);
+    const float4 Q2 = make_float4(__fadd_rn(qr, qr), __fadd_rn(qg, qg), __fadd_rn(qb, qb), 0.0f);
+    const float4 va[4] = {P, Z, Q2, Q}, vb[4] = {Z, P, Q, Q2};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      t.ab[p][0][k] = make_float2(va[k].x, va[k].y);
+      t.ab[p][1][k] = make_float2(va[k].z, vb[k].x);
+      t.ab[p][2][k] = make_float2(vb[k].y, vb[k].z);
+    }
+    pk = R | (G << 8) | (B << 16);
+    sq = (int)(R * R + G * G + B * B);
+  }
+  // channel bytes of each group of four pixels of this half's block
+  const int c = p >> 2, g = p & 3, base = lane & 16;
+  const uint32_t p0 = __shfl_sync(kFull, pk, base + 4 * g + 0), p1 = __shfl_sync(kFull, pk, base + 4 * g + 1);
+  const uint32_t p2 = __shfl_sync(kFull, pk, base + 4 * g + 2), p3 = __shfl_sync(kFull, pk, base + 4 * g + 3);
+  if (has && p < 12) {
+    const uint32_t sh = 8 * c;
+    t.pg[c][g] = ((p0 >> sh) & 0xFF) | (((p1 >> sh) & 0xFF) << 8) | (((p2 >> sh) & 0xFF) << 16) |
+                 (((p3 >> sh) & 0xFF) << 24);
+  }
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) sq += __shfl_xor_sync(kFull, sq, o);
+  __syncwarp();
+  return sq;
+}
+
 // Weight sums of the refit for index word `cand`, accumulated in the
 // reference's order (codec/dxt_image.cpp:307-312) from the per-index constants
 // wk[index] = (a*a, b*b, a*b).

@@ -522,13 +522,22 @@ __global__ void __launch_bounds__(WARPS * 32) learned_eval_kernel(const __grid_c
     const uint32_t *prev_hi = reinterpret_cast<const uint32_t *>(P.prev) + 1;
     const int base = (gg - (jb ? batch.group_end[jb - 1] : 0)) * BPW;
     int sumsq = 0;
+    if constexpr (BPW == 1) {
+      if (base < nblk) {
+        const int by = base / P.bw, bx = base - by * P.bw;
+        sumsq = stage_block(s_tab[warp][0], P.rgb, P.width, bx, by, lane);
+      }
+    } else {
+      // two blocks per staging pass, half a warp each
 #pragma unroll
-    for (int jj = 0; jj < BPW; ++jj) {
-      const int idx = base + jj;
-      if (idx < nblk) {
-        const int by = idx / P.bw, bx = idx - by * P.bw;
-        const int sq = stage_block(s_tab[warp][jj], P.rgb, P.width, bx, by, lane);
-        if (jj == slot) sumsq = sq;
+      for (int jj = 0; jj < BPW; jj += 2) {
+        const int ia = base + jj, ib = ia + 1;
+        const int ay = ia / P.bw, ax = ia - ay * P.bw, by2 = ib / P.bw, bx2 = ib - by2 * P.bw;
+        const int sq = stage_block_pair(s_tab[warp][jj], s_tab[warp][jj + 1], P.rgb, P.width, ax, ay, ia < nblk,
+                                        bx2, by2, ib < nblk, lane);
+        const int sqa = __shfl_sync(kFull, sq, 0), sqb = __shfl_sync(kFull, sq, 16);
+        if (slot == jj) sumsq = sqa;
+        if (slot == jj + 1) sumsq = sqb;
       }
     }
     const int idx = base + slot;
