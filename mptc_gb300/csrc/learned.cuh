@@ -3,118 +3,165 @@
 // fused bias/ReLU, feature builders, sampled softmax cross-entropy, AdamW.
 #pragma once
 #include "learned_common.cuh"
+#include "tc_sm100.cuh"
 
 namespace mptc {
 
-// C[M x N] = op(A)[M x K] * op(B)[K x N] (+ C) (+ bias) (ReLU), BF16 in, FP32
-// accumulate. TA: A is stored K x M (row-major, lda); else M x K. TB: B is
-// stored N x K; else K x N. Outputs: C (fp32) and/or Cb (bf16), row-major ldc.
-// Tiles of 64 x 64 x 32; 4 warps, each 32 x 32 (2 x 4 mma tiles).
-constexpr int kGBM = 64, kGBN = 64, kGBK = 32;
+// C[M x N] = op(A)[M x K] * op(B)[K x N] (+ C) (+ bias) (ReLU) on the
+// fifth-generation tensor cores, BF16 in, FP32 accumulate in TMEM. TA: A is
+// stored K x M (row-major, lda), else M x K; TB: B is stored N x K, else
+// K x N. Outputs: C (fp32) and/or Cb (bf16), row-major ldc. Split K
+// (gridDim.z > 1): slice z writes its partial product to C + z * M * ldc, no
+// bias, ReLU or bf16 copy; the caller sums the slices in order. Tiles of
+// 128 x 128 (one TMEM lane per row), K in steps of 64: each operand tile is
+// staged in shared memory in the 128-byte-swizzled K-major layout (rows of
+// 64 K values); an operand whose K run is contiguous in memory (A not
+// transposed, B transposed) moves as 16-byte vectors, the other is read 8
+// rows (or columns) at a time along its contiguous dimension and goes into
+// the tile's rows through a register transpose (stage_transposed). Thread 0
+// issues 4 tcgen05.mma (K = 16 each) per step; the epilogue reads the
+// accumulator with tcgen05.ld, warp w rows 32w .. .
+constexpr int kTcBM = 128, kTcBN = 128, kTcBK = 64;
+
+// Eight consecutive bf16 at p, of which the first `valid` exist (zeros after):
+// one 16-byte load when all eight exist and p is 16-byte aligned.
+__device__ __forceinline__ uint4 load8_bf16(const __nv_bfloat16 *p, int valid) {
+  if (valid >= 8 && (reinterpret_cast<uintptr_t>(p) & 15) == 0) return *reinterpret_cast<const uint4 *>(p);
+  uint16_t h[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) h[j] = j < valid ? reinterpret_cast<const uint16_t *>(p)[j] : (uint16_t)0;
+  return make_uint4(h[0] | ((uint32_t)h[1] << 16), h[2] | ((uint32_t)h[3] << 16), h[4] | ((uint32_t)h[5] << 16),
+                    h[6] | ((uint32_t)h[7] << 16));
+}
+
+// Stages an operand whose rows (tile rows r = 0..127, index row0 + r < nrows)
+// are contiguous along the other dimension: src[k][row0 + r] for k in
+// [k0, kend), stride ld. Thread t takes the 8 x 8 block of K values
+// k0 + 8 (t % 8) .. and rows 8 (t / 8) ..: eight 16-byte loads (one per K
+// value), a register transpose (each output word one byte permutation of two
+// input words) and eight 16-byte stores (one per tile row).
+__device__ __forceinline__ void stage_transposed(uint8_t *tile, const __nv_bfloat16 *__restrict__ src, int ld,
+                                                 int row0, int nrows, int k0, int kend, int tid) {
+  const int kb = tid & 7, rb = tid >> 3;  // 8 K blocks x 16 row blocks
+  const int r = 8 * rb, row = row0 + r;
+  uint32_t w[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int k = k0 + 8 * kb + i;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (k < kend && row < nrows) v = load8_bf16(src + (size_t)k * ld + row, nrows - row);
+    w[i][0] = v.x;
+    w[i][1] = v.y;
+    w[i][2] = v.z;
+    w[i][3] = v.w;
+  }
+  // out[j][q] = (w[2q] element j, w[2q+1] element j): row r + j, K values 8 kb + 2q, + 1
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint32_t sel = (j & 1) ? 0x7632u : 0x5410u;
+    const uint4 o = make_uint4(__byte_perm(w[0][j >> 1], w[1][j >> 1], sel), __byte_perm(w[2][j >> 1], w[3][j >> 1], sel),
+                               __byte_perm(w[4][j >> 1], w[5][j >> 1], sel), __byte_perm(w[6][j >> 1], w[7][j >> 1], sel));
+    *reinterpret_cast<uint4 *>(tile + tc::sw128_offset((uint32_t)(r + j), (uint32_t)kb)) = o;
+  }
+}
 
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(const __nv_bfloat16 *__restrict__ A, int lda,
-                                                        const __nv_bfloat16 *__restrict__ B, int ldb,
-                                                        float *__restrict__ C, __nv_bfloat16 *__restrict__ Cb,
-                                                        int ldc, const float *__restrict__ bias, int M, int N, int K,
-                                                        int relu, int accumulate) {
-  __shared__ __align__(16) __nv_bfloat16 As[kGBM][kGBK + 8];
-  __shared__ __align__(16) __nv_bfloat16 Bs[kGBN][kGBK + 8];  // stored [n][k]
+__global__ void __launch_bounds__(128) gemm_tc_kernel(const __nv_bfloat16 *__restrict__ A, int lda,
+                                                      const __nv_bfloat16 *__restrict__ B, int ldb,
+                                                      float *__restrict__ C, __nv_bfloat16 *__restrict__ Cb, int ldc,
+                                                      const float *__restrict__ bias, int M, int N, int K, int relu,
+                                                      int accumulate) {
+  __shared__ __align__(1024) uint8_t sA[kTcBM * 128];
+  __shared__ __align__(1024) uint8_t sB[kTcBN * 128];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  __shared__ volatile uint32_t abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int g = lane >> 2, t = lane & 3;
-  const int m0 = blockIdx.y * kGBM, n0 = blockIdx.x * kGBN;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  // split K (blockIdx.z): slice z writes its partial product to C + z * M * ldc
-  const int ksplit = gridDim.z > 1 ? (K + gridDim.z - 1) / gridDim.z : K;
-  const int kbeg = blockIdx.z * ((ksplit + kGBK - 1) / kGBK * kGBK);
-  const int kend = min(K, kbeg + (ksplit + kGBK - 1) / kGBK * kGBK);
-  for (int k0 = kbeg; k0 < kend; k0 += kGBK) {
-    // tiles with k contiguous in memory move as 16-byte vectors when aligned
-    const bool avec = !TA && (lda % 8 == 0) && (k0 + kGBK <= kend) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
-    const bool bvec = TB && (ldb % 8 == 0) && (k0 + kGBK <= kend) && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
-    if (avec) {
-      for (int e = tid; e < kGBM * kGBK / 8; e += 128) {
-        const int r = e / (kGBK / 8), c = 8 * (e % (kGBK / 8)), m = m0 + r;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (m < M) v = *reinterpret_cast<const uint4 *>(A + (size_t)m * lda + k0 + c);
-        *reinterpret_cast<uint4 *>(&As[r][c]) = v;
-      }
-    } else {
-      for (int e = tid; e < kGBM * kGBK; e += 128) {
-        const int r = e / kGBK, c = e % kGBK, m = m0 + r, k = k0 + c;
-        __nv_bfloat16 v = zero;
-        if (m < M && k < kend) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
-        As[r][c] = v;
-      }
-    }
-    if (bvec) {
-      for (int e = tid; e < kGBN * kGBK / 8; e += 128) {
-        const int r = e / (kGBK / 8), c = 8 * (e % (kGBK / 8)), n = n0 + r;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (n < N) v = *reinterpret_cast<const uint4 *>(B + (size_t)n * ldb + k0 + c);
-        *reinterpret_cast<uint4 *>(&Bs[r][c]) = v;
-      }
-    } else {
-      for (int e = tid; e < kGBN * kGBK; e += 128) {
-        const int r = e / kGBK, c = e % kGBK, n = n0 + r, k = k0 + c;
-        __nv_bfloat16 v = zero;
-        if (n < N && k < kend) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
-        Bs[r][c] = v;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < kGBK; ks += 16) {
-      uint32_t af[2][4], bf[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r = wm + 16 * i + g, c = ks + 2 * t;
-        af[i][0] = pack_bf16x2(As[r][c], As[r][c + 1]);
-        af[i][1] = pack_bf16x2(As[r + 8][c], As[r + 8][c + 1]);
-        af[i][2] = pack_bf16x2(As[r][c + 8], As[r][c + 9]);
-        af[i][3] = pack_bf16x2(As[r + 8][c + 8], As[r + 8][c + 9]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int n = wn + 8 * j + g, c = ks + 2 * t;
-        bf[j][0] = pack_bf16x2(Bs[n][c], Bs[n][c + 1]);
-        bf[j][1] = pack_bf16x2(Bs[n][c + 8], Bs[n][c + 9]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16_16816(acc[i][j], af[i], bf[j]);
-    }
-    __syncthreads();
+  const int m0 = blockIdx.y * kTcBM, n0 = blockIdx.x * kTcBN;
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    abort_flag = 0;
+    tc::mbar_fence_init();
   }
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int m = m0 + wm + 16 * i + g + (q >= 2 ? 8 : 0);
-        const int n = n0 + wn + 8 * j + 2 * t + (q & 1);
-        if (m >= M || n >= N) continue;
-        float v = acc[i][j][q];
-        if (gridDim.z > 1) {  // a K slice: its partial sum into slice z of C (no bias, ReLU or bf16 copy)
-          C[(size_t)blockIdx.z * M * ldc + (size_t)m * ldc + n] = v;
-          continue;
-        }
-        if (accumulate && C) v += C[(size_t)m * ldc + n];
-        if (bias) v += bias[n];
-        if (relu) v = v > 0.f ? v : 0.f;
-        if (C) C[(size_t)m * ldc + n] = v;
-        if (Cb) Cb[(size_t)m * ldc + n] = __float2bfloat16(v);
+  if (warp == 0) tc::tmem_alloc(&tslot, kTcBN);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tslot;
+  const uint32_t idesc = tc::idesc_bf16(kTcBM, kTcBN);
+  // split K (blockIdx.z): this slice's K range, in whole steps
+  const int ksplit = gridDim.z > 1 ? (K + gridDim.z - 1) / gridDim.z : K;
+  const int kstep = (ksplit + kTcBK - 1) / kTcBK * kTcBK;
+  const int kbeg = blockIdx.z * kstep, kend = min(K, kbeg + kstep);
+  const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
+  uint32_t phase = 0;
+  int steps = 0;
+  for (int k0 = kbeg; k0 < kend; k0 += kTcBK, ++steps) {
+    // A tile: row r = m0 + r, K values k0 .. k0 + 63
+    if (!TA) {
+      for (int e = tid; e < kTcBM * 8; e += 128) {
+        const int r = e >> 3, c = e & 7, m = m0 + r, k = k0 + 8 * c;
+        uint4 v = zero4;
+        if (m < M && k < kend) v = load8_bf16(A + (size_t)m * lda + k, kend - k);
+        *reinterpret_cast<uint4 *>(sA + tc::sw128_offset((uint32_t)r, (uint32_t)c)) = v;
       }
+    } else {  // A stored K x M
+      stage_transposed(sA, A, lda, m0, M, k0, kend, tid);
+    }
+    // B tile: row r = n0 + r, K values k0 .. k0 + 63
+    if (TB) {  // B stored N x K
+      for (int e = tid; e < kTcBN * 8; e += 128) {
+        const int r = e >> 3, c = e & 7, n = n0 + r, k = k0 + 8 * c;
+        uint4 v = zero4;
+        if (n < N && k < kend) v = load8_bf16(B + (size_t)n * ldb + k, kend - k);
+        *reinterpret_cast<uint4 *>(sB + tc::sw128_offset((uint32_t)r, (uint32_t)c)) = v;
+      }
+    } else {  // B stored K x N
+      stage_transposed(sB, B, ldb, n0, N, k0, kend, tid);
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::tc_fence_after();
+      const uint32_t a = tc::smem_addr(sA), b = tc::smem_addr(sB);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        tc::mma_bf16(tmem, tc::desc_sw128(a + 32 * k), tc::desc_sw128(b + 32 * k), idesc, (steps > 0 || k > 0) ? 1u : 0u);
+      tc::mma_commit(&bar);
+    }
+    // the MMAs have read the tiles before they are overwritten
+    if (!tc::mbar_wait(&bar, phase, &abort_flag)) abort_flag = 1;
+    phase ^= 1;
+    tc::tc_fence_after();
+  }
+  // epilogue: this thread's row, 32 columns at a time
+  const int m = m0 + 32 * warp + lane;
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
+  for (int c0 = 0; c0 < kTcBN; c0 += 32) {
+    float v[32];
+    tc::tmem_ld32(lane_base + (uint32_t)c0, v);
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int n = n0 + c0 + j;
+      if (n >= N) continue;
+      float x = steps > 0 ? v[j] : 0.f;
+      if (gridDim.z > 1) {  // a K slice: its partial sum into slice z of C (no bias, ReLU or bf16 copy)
+        C[(size_t)blockIdx.z * M * ldc + (size_t)m * ldc + n] = x;
+        continue;
+      }
+      if (accumulate && C) x += C[(size_t)m * ldc + n];
+      if (bias) x += bias[n];
+      if (relu) x = x > 0.f ? x : 0.f;
+      if (C) C[(size_t)m * ldc + n] = x;
+      if (Cb) Cb[(size_t)m * ldc + n] = __float2bfloat16(x);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  if (warp == 0) tc::tmem_free(tmem, kTcBN);
 }
 
 // Block features (block_feature_half) of blocks[r] (NULL: block r), n rows of

@@ -6,12 +6,12 @@
 // reference's acceptance rule (err_diff <= threshold) and the stream stays a
 // valid MPTC stream.
 //
-// Inference (embeddings and window scoring, learned_tc.cuh) runs on the
-// tcgen05 tensor cores; the training step's matrix products (learned.cuh) use
-// mma.sync m16n8k16. Both take BF16 operands and accumulate in FP32.
+// Inference (embeddings and window scoring, learned_tc.cuh) and the training
+// step's matrix products (gemm_tc_kernel, learned.cuh) both run on the tcgen05
+// tensor cores with BF16 operands and FP32 accumulators in tensor memory.
 //
-// This header holds the sizes, the input features (the same for training and
-// inference) and the mma.sync helpers of the training kernels.
+// This header holds the sizes and the input features (the same for training
+// and inference).
 #pragma once
 #include <cuda_bf16.h>
 
@@ -106,18 +106,6 @@ __device__ __forceinline__ void word_feature_half(uint32_t word, int half, uint3
     // bf16 1.0 = 0x3F80
     out[j] = half ? 0u : (b0 ? 0x3F80u : 0u) | (b1 ? 0x3F800000u : 0u);
   }
-}
-
-__device__ __forceinline__ uint32_t pack_bf16x2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
-
-__device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], const uint32_t b[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
 }  // namespace mptc

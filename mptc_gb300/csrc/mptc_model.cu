@@ -121,8 +121,8 @@ int blocks_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 4096); 
 // y[M x N] = x[M x K] W + b (opt. ReLU), outputs fp32 and bf16.
 void gemm_fwd(const bf16 *x, const bf16 *W, const float *b, float *y, bf16 *yb, int M, int K, int N, bool relu,
               cudaStream_t s) {
-  dim3 grid((N + mptc::kGBN - 1) / mptc::kGBN, (M + mptc::kGBM - 1) / mptc::kGBM);
-  mptc::gemm_bf16_kernel<false, false><<<grid, 128, 0, s>>>(x, K, W, N, y, yb, N, b, M, N, K, relu ? 1 : 0, 0);
+  dim3 grid((N + mptc::kTcBN - 1) / mptc::kTcBN, (M + mptc::kTcBM - 1) / mptc::kTcBM);
+  mptc::gemm_tc_kernel<false, false><<<grid, 128, 0, s>>>(x, K, W, N, y, yb, N, b, M, N, K, relu ? 1 : 0, 0);
 }
 
 // Partial sums of the split reductions below (slices x outputs floats).
@@ -133,9 +133,9 @@ constexpr size_t kPartFloats = 1 << 20;
 // partial products are summed in slice order afterwards (deterministic).
 void gemm_dw(const bf16 *x, const bf16 *dy, float *dW, int M, int K, int N, float *part, cudaStream_t s) {
   const int splits = (int)std::min<size_t>(std::min(64, std::max(1, M / 2048)), kPartFloats / ((size_t)K * N));
-  dim3 grid((N + mptc::kGBN - 1) / mptc::kGBN, (K + mptc::kGBM - 1) / mptc::kGBM, std::max(1, splits));
-  mptc::gemm_bf16_kernel<true, false><<<grid, 128, 0, s>>>(x, K, dy, N, splits > 1 ? part : dW, nullptr, N, nullptr,
-                                                          K, N, M, 0, 0);
+  dim3 grid((N + mptc::kTcBN - 1) / mptc::kTcBN, (K + mptc::kTcBM - 1) / mptc::kTcBM, std::max(1, splits));
+  mptc::gemm_tc_kernel<true, false><<<grid, 128, 0, s>>>(x, K, dy, N, splits > 1 ? part : dW, nullptr, N, nullptr, K, N,
+                                                        M, 0, 0);
   if (splits > 1) mptc::slice_sum_kernel<<<blocks_for((size_t)K * N), 256, 0, s>>>(part, splits, K * N, dW);
 }
 
@@ -149,8 +149,8 @@ void colsum(const float *d, int rows, int cols, float *db, float *part, cudaStre
 
 // dx[M x K] = dy[M x N] W^T  (W stored K x N, i.e. "N x K" transposed access)
 void gemm_dx(const bf16 *dy, const bf16 *W, float *dx, int M, int K, int N, cudaStream_t s) {
-  dim3 grid((K + mptc::kGBN - 1) / mptc::kGBN, (M + mptc::kGBM - 1) / mptc::kGBM);
-  mptc::gemm_bf16_kernel<false, true><<<grid, 128, 0, s>>>(dy, N, W, N, dx, nullptr, K, nullptr, M, K, N, 0, 0);
+  dim3 grid((K + mptc::kTcBN - 1) / mptc::kTcBN, (M + mptc::kTcBM - 1) / mptc::kTcBM);
+  mptc::gemm_tc_kernel<false, true><<<grid, 128, 0, s>>>(dy, N, W, N, dx, nullptr, K, nullptr, M, K, N, 0, 0);
 }
 
 // Forward through both MLPs for a training batch; then, if `grads`, the loss
