@@ -263,7 +263,10 @@ mptc_status mptc_model_get_params(mptc_model *model, float *host);
 mptc_status mptc_model_set_params(mptc_model *model, const float *host);
 /* One AdamW step on a batch of B blocks of one frame (block indices
  * blocks_dev) with C candidate index words each (cands_dev, B x C, the
- * accepted candidate first): sampled softmax cross-entropy. */
+ * accepted candidate first): sampled softmax cross-entropy. With loss_host
+ * the call waits for the step and returns MPTC_ETIMEOUT if a bounded
+ * device-side wait of this or an earlier unread step expired; with
+ * loss_host NULL it returns once the step is queued. */
 mptc_status mptc_model_train_step(mptc_model *model, const uint8_t *rgb_dev, int32_t width, const uint64_t *stb_dev,
                                   const uint32_t *blocks_dev, const uint32_t *cands_dev, int32_t B, int32_t C,
                                   float lr, float weight_decay, float *loss_host, void *stream);

@@ -68,89 +68,127 @@ struct mptc_model {
   // training workspace (grown on demand)
   int cap_b = 0, cap_bc = 0;
   bf16 *x = nullptr, *h1b = nullptr, *h2b = nullptr, *xc = nullptr, *g1b = nullptr;
-  float *h1 = nullptr, *h2 = nullptr, *f = nullptr, *g1 = nullptr, *gg = nullptr;
-  float *df = nullptr, *dgg = nullptr, *dh1 = nullptr, *dh2 = nullptr, *dg1 = nullptr;
+  float *f = nullptr, *gg = nullptr;
   bf16 *dfb = nullptr, *dggb = nullptr, *dh1b = nullptr, *dh2b = nullptr, *dg1b = nullptr;
+  float *part = nullptr;  // partial sums of the split gradient reductions (part_floats)
+  size_t part_floats = 0;
   float *loss = nullptr;
   // packed bf16 weight image of the inference kernels (refreshed after every
   // parameter change) and a bf16 staging buffer for mptc_model_embed
   uint8_t *img = nullptr;
   __nv_bfloat16 *emb_tmp = nullptr;
   int emb_cap = 0;
+  // status words: 0 - 3 of mptc_model_embed; 4 the training kernels' timeout
+  // flag (sticky until a step reads it back)
   uint32_t *status = nullptr;
-  float *part = nullptr;  // partial sums of the split gradient reductions
 };
 
 namespace {
 
 void free_ws(mptc_model *m) {
-  void *ps[] = {m->x, m->h1b, m->h2b, m->xc, m->g1b, m->h1, m->h2, m->f, m->g1, m->gg,
-                m->df, m->dgg, m->dh1, m->dh2, m->dg1, m->dfb, m->dggb, m->dh1b, m->dh2b, m->dg1b};
+  void *ps[] = {m->x, m->h1b, m->h2b, m->xc, m->g1b, m->f, m->gg, m->dfb, m->dggb, m->dh1b, m->dh2b, m->dg1b, m->part};
   for (void *p : ps) cudaFree(p);
   m->x = m->h1b = m->h2b = m->xc = m->g1b = nullptr;
-  m->h1 = m->h2 = m->f = m->g1 = m->gg = m->df = m->dgg = m->dh1 = m->dh2 = m->dg1 = nullptr;
+  m->f = m->gg = nullptr;
   m->dfb = m->dggb = m->dh1b = m->dh2b = m->dg1b = nullptr;
+  m->part = nullptr;
   m->cap_b = m->cap_bc = 0;
+  m->part_floats = 0;
+}
+
+// Partial sums of the split dW reductions below (slices x outputs floats).
+constexpr size_t kSplitFloats = 1 << 22;
+// Column partial sums of the bias gradients: softmax_ce (2 x 64 per 8
+// blocks) and the dx epilogues (one row of K_layer per 128 examples).
+size_t part_floats_for(int B, int BC) {
+  using namespace mptc;
+  const size_t ce = 2 * (size_t)((B + 7) / 8) * kEmb;
+  const size_t dxb = (size_t)((B + kTcBM - 1) / kTcBM) * kH2;
+  const size_t dxc = (size_t)((BC + kTcBM - 1) / kTcBM) * kCandH;
+  return std::max(std::max(kSplitFloats, ce), std::max(dxb, dxc));
 }
 
 mptc_status ensure_ws(mptc_model *m, int B, int BC) {
   if (B <= m->cap_b && BC <= m->cap_bc) return MPTC_OK;
   free_ws(m);
   using namespace mptc;
+  const size_t pf = part_floats_for(B, BC);
   bool bad = dmalloc(&m->x, (size_t)B * kFeatPad) || dmalloc(&m->h1b, (size_t)B * kH1) ||
              dmalloc(&m->h2b, (size_t)B * kH2) || dmalloc(&m->xc, (size_t)BC * kCandIn) ||
-             dmalloc(&m->g1b, (size_t)BC * kCandH) || dmalloc(&m->h1, (size_t)B * kH1) ||
-             dmalloc(&m->h2, (size_t)B * kH2) || dmalloc(&m->f, (size_t)B * kEmb) ||
-             dmalloc(&m->g1, (size_t)BC * kCandH) || dmalloc(&m->gg, (size_t)BC * kEmb) ||
-             dmalloc(&m->df, (size_t)B * kEmb) || dmalloc(&m->dgg, (size_t)BC * kEmb) ||
-             dmalloc(&m->dh1, (size_t)B * kH1) || dmalloc(&m->dh2, (size_t)B * kH2) ||
-             dmalloc(&m->dg1, (size_t)BC * kCandH) || dmalloc(&m->dfb, (size_t)B * kEmb) ||
+             dmalloc(&m->g1b, (size_t)BC * kCandH) || dmalloc(&m->f, (size_t)B * kEmb) ||
+             dmalloc(&m->gg, (size_t)BC * kEmb) || dmalloc(&m->dfb, (size_t)B * kEmb) ||
              dmalloc(&m->dggb, (size_t)BC * kEmb) || dmalloc(&m->dh1b, (size_t)B * kH1) ||
-             dmalloc(&m->dh2b, (size_t)B * kH2) || dmalloc(&m->dg1b, (size_t)BC * kCandH);
+             dmalloc(&m->dh2b, (size_t)B * kH2) || dmalloc(&m->dg1b, (size_t)BC * kCandH) || dmalloc(&m->part, pf);
   if (bad) {
     free_ws(m);
     return MPTC_ENOMEM;
   }
   m->cap_b = B;
   m->cap_bc = BC;
+  m->part_floats = pf;
   return MPTC_OK;
 }
 
 int blocks_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 4096); }
 
-// y[M x N] = x[M x K] W + b (opt. ReLU), outputs fp32 and bf16.
-void gemm_fwd(const bf16 *x, const bf16 *W, const float *b, float *y, bf16 *yb, int M, int K, int N, bool relu,
-              cudaStream_t s) {
-  dim3 grid((N + mptc::kTcBN - 1) / mptc::kTcBN, (M + mptc::kTcBM - 1) / mptc::kTcBM);
-  mptc::gemm_tc_kernel<false, false><<<grid, 128, 0, s>>>(x, K, W, N, y, yb, N, b, M, N, K, relu ? 1 : 0, 0);
+// The split training products run as up to 3 CTAs per SM of a 152-SM part
+// (the most two pipeline stages of shared memory allow), fixed so that the
+// split and with it the summation order do not depend on the device.
+constexpr int kTrainCtas = 456;
+
+cudaError_t ensure_gemm_attrs() {
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    err = cudaFuncSetAttribute(mptc::gemm_tc_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               mptc::kTcSmem);
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(mptc::gemm_tc_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 mptc::kTcSmem);
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(mptc::gemm_tc_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 mptc::kTcSmem);
+  });
+  return err;
 }
 
-// Partial sums of the split reductions below (slices x outputs floats).
-constexpr size_t kPartFloats = 1 << 20;
+// y[M x N] = x[M x K] W + b (opt. ReLU) into y (fp32) and/or yb (bf16).
+void gemm_fwd(const bf16 *x, const bf16 *W, const float *b, float *y, bf16 *yb, int M, int K, int N, bool relu,
+              uint32_t *status, cudaStream_t s) {
+  dim3 grid((N + mptc::kTcBN - 1) / mptc::kTcBN, (M + mptc::kTcBM - 1) / mptc::kTcBM);
+  const mptc::GemmEpi e{y, yb, N, b, relu ? 1 : 0, nullptr, nullptr};
+  mptc::gemm_tc_kernel<false, false><<<grid, 128, mptc::kTcSmem, s>>>(x, K, W, N, e, M, N, K, status);
+}
+
+// out[n] = sum of the `slices` rows of part [slices x n], in order.
+void slice_sum(const float *part, int slices, int n, float *out, cudaStream_t s) {
+  mptc::slice_sum_kernel<<<(n + 31) / 32, 256, 0, s>>>(part, slices, n, out);
+}
 
 // dW[K x N] = x^T[K x M] dy[M x N]: few outputs and a long reduction over the
-// M examples, so the reduction is split into slices of about 2048 rows whose
-// partial products are summed in slice order afterwards (deterministic).
-void gemm_dw(const bf16 *x, const bf16 *dy, float *dW, int M, int K, int N, float *part, cudaStream_t s) {
-  const int splits = (int)std::min<size_t>(std::min(64, std::max(1, M / 2048)), kPartFloats / ((size_t)K * N));
-  dim3 grid((N + mptc::kTcBN - 1) / mptc::kTcBN, (K + mptc::kTcBM - 1) / mptc::kTcBM, std::max(1, splits));
-  mptc::gemm_tc_kernel<true, false><<<grid, 128, 0, s>>>(x, K, dy, N, splits > 1 ? part : dW, nullptr, N, nullptr, K, N,
-                                                        M, 0, 0);
-  if (splits > 1) mptc::slice_sum_kernel<<<blocks_for((size_t)K * N), 256, 0, s>>>(part, splits, K * N, dW);
+// M examples, so the reduction is split into slices of at least 256 rows
+// (up to kTrainCtas CTAs in all) whose partial products are summed in slice
+// order afterwards (deterministic).
+void gemm_dw(const bf16 *x, const bf16 *dy, float *dW, int M, int K, int N, float *part, uint32_t *status,
+             cudaStream_t s) {
+  const int tiles = ((N + mptc::kTcBN - 1) / mptc::kTcBN) * ((K + mptc::kTcBM - 1) / mptc::kTcBM);
+  int splits = std::min(M / 256, std::max(1, kTrainCtas / tiles));
+  splits = (int)std::max<size_t>(1, std::min<size_t>((size_t)splits, kSplitFloats / ((size_t)K * N)));
+  dim3 grid((N + mptc::kTcBN - 1) / mptc::kTcBN, (K + mptc::kTcBM - 1) / mptc::kTcBM, splits);
+  const mptc::GemmEpi e{splits > 1 ? part : dW, nullptr, N, nullptr, 0, nullptr, nullptr};
+  mptc::gemm_tc_kernel<true, false><<<grid, 128, mptc::kTcSmem, s>>>(x, K, dy, N, e, K, N, M, status);
+  if (splits > 1) slice_sum(part, splits, K * N, dW, s);
 }
 
-// Bias gradient db[cols] = column sums of d[rows x cols].
-void colsum(const float *d, int rows, int cols, float *db, float *part, cudaStream_t s) {
-  const int slices = (int)std::min<size_t>(std::min(512, std::max(1, rows / 64)), kPartFloats / cols);
-  dim3 grid((cols + 127) / 128, slices);
-  mptc::colsum_kernel<<<grid, 128, 0, s>>>(d, rows, cols, part);
-  mptc::slice_sum_kernel<<<blocks_for((size_t)cols), 256, 0, s>>>(part, slices, cols, db);
-}
-
-// dx[M x K] = dy[M x N] W^T  (W stored K x N, i.e. "N x K" transposed access)
-void gemm_dx(const bf16 *dy, const bf16 *W, float *dx, int M, int K, int N, cudaStream_t s) {
+// dx[M x K] = (dy[M x N] W^T) masked by the ReLU of the layer's input (h > 0)
+// into dxb (bf16), and db[K] = the column sums of that dx (the bias gradient
+// of the layer below).
+void gemm_dx(const bf16 *dy, const bf16 *W, const bf16 *h, bf16 *dxb, float *db, int M, int K, int N, float *part,
+             uint32_t *status, cudaStream_t s) {
   dim3 grid((K + mptc::kTcBN - 1) / mptc::kTcBN, (M + mptc::kTcBM - 1) / mptc::kTcBM);
-  mptc::gemm_tc_kernel<false, true><<<grid, 128, 0, s>>>(dy, N, W, N, dx, nullptr, K, nullptr, M, K, N, 0, 0);
+  const mptc::GemmEpi e{nullptr, dxb, K, nullptr, 0, h, part};
+  mptc::gemm_tc_kernel<false, true><<<grid, 128, mptc::kTcSmem, s>>>(dy, N, W, N, e, M, K, N, status);
+  slice_sum(part, (int)grid.y, K, db, s);
 }
 
 // Forward through both MLPs for a training batch; then, if `grads`, the loss
@@ -167,45 +205,54 @@ mptc_status forward_backward(mptc_model *m, const uint8_t *rgb, int width, int b
     W[l] = m->wb + kOff.w[l];
     b[l] = m->w + kOff.b[l];
   }
+  if (ensure_gemm_attrs() != cudaSuccess) return MPTC_ECUDA;
+  uint32_t *status = m->status + 4;
   block_features_kernel<<<blocks_for((size_t)B * kFeatPad), 256, 0, s>>>(rgb, width, bw, stb, blocks, B, m->x);
-  gemm_fwd(m->x, W[0], b[0], m->h1, m->h1b, B, kFeatPad, kH1, true, s);
-  gemm_fwd(m->h1b, W[1], b[1], m->h2, m->h2b, B, kH1, kH2, true, s);
-  gemm_fwd(m->h2b, W[2], b[2], m->f, nullptr, B, kH2, kEmb, false, s);
+  gemm_fwd(m->x, W[0], b[0], nullptr, m->h1b, B, kFeatPad, kH1, true, status, s);
+  gemm_fwd(m->h1b, W[1], b[1], nullptr, m->h2b, B, kH1, kH2, true, status, s);
+  gemm_fwd(m->h2b, W[2], b[2], m->f, nullptr, B, kH2, kEmb, false, status, s);
   cand_features_kernel<<<blocks_for((size_t)BC * kCandIn), 256, 0, s>>>(cands, 1, BC, m->xc);
-  gemm_fwd(m->xc, W[3], b[3], m->g1, m->g1b, BC, kCandIn, kCandH, true, s);
-  gemm_fwd(m->g1b, W[4], b[4], m->gg, nullptr, BC, kCandH, kEmb, false, s);
+  gemm_fwd(m->xc, W[3], b[3], nullptr, m->g1b, BC, kCandIn, kCandH, true, status, s);
+  gemm_fwd(m->g1b, W[4], b[4], m->gg, nullptr, BC, kCandH, kEmb, false, status, s);
   cudaMemsetAsync(m->loss, 0, sizeof(float), s);
-  softmax_ce_kernel<<<(B * 32 + 255) / 256, 256, 0, s>>>(m->f, m->gg, B, C, m->df, m->dgg, m->loss);
+  const int nce = (B + 7) / 8;
+  float *partF = m->part, *partG = m->part + (size_t)nce * kEmb;
+  softmax_ce_kernel<<<nce, 256, 0, s>>>(m->f, m->gg, B, C, m->dfb, m->dggb, partF, partG, m->loss);
   if (!grads) return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
   float *G[5], *Gb[5];
   for (int l = 0; l < 5; ++l) {
     G[l] = m->g + kOff.w[l];
     Gb[l] = m->g + kOff.b[l];
   }
+  // output biases from the loss kernel's column sums
+  slice_sum(partF, nce, kEmb, Gb[2], s);
+  slice_sum(partG, nce, kEmb, Gb[4], s);
   // block MLP
-  to_bf16_kernel<<<blocks_for((size_t)B * kEmb), 256, 0, s>>>(m->df, m->dfb, B * kEmb);
-  gemm_dw(m->h2b, m->dfb, G[2], B, kH2, kEmb, m->part, s);
-  colsum(m->df, B, kEmb, Gb[2], m->part, s);
-  gemm_dx(m->dfb, W[2], m->dh2, B, kH2, kEmb, s);
-  relu_backward_kernel<<<blocks_for((size_t)B * kH2), 256, 0, s>>>(m->dh2, m->h2, B * kH2);
-  to_bf16_kernel<<<blocks_for((size_t)B * kH2), 256, 0, s>>>(m->dh2, m->dh2b, B * kH2);
-  gemm_dw(m->h1b, m->dh2b, G[1], B, kH1, kH2, m->part, s);
-  colsum(m->dh2, B, kH2, Gb[1], m->part, s);
-  gemm_dx(m->dh2b, W[1], m->dh1, B, kH1, kH2, s);
-  relu_backward_kernel<<<blocks_for((size_t)B * kH1), 256, 0, s>>>(m->dh1, m->h1, B * kH1);
-  to_bf16_kernel<<<blocks_for((size_t)B * kH1), 256, 0, s>>>(m->dh1, m->dh1b, B * kH1);
-  gemm_dw(m->x, m->dh1b, G[0], B, kFeatPad, kH1, m->part, s);
-  colsum(m->dh1, B, kH1, Gb[0], m->part, s);
+  gemm_dw(m->h2b, m->dfb, G[2], B, kH2, kEmb, m->part, status, s);
+  gemm_dx(m->dfb, W[2], m->h2b, m->dh2b, Gb[1], B, kH2, kEmb, m->part, status, s);
+  gemm_dw(m->h1b, m->dh2b, G[1], B, kH1, kH2, m->part, status, s);
+  gemm_dx(m->dh2b, W[1], m->h1b, m->dh1b, Gb[0], B, kH1, kH2, m->part, status, s);
+  gemm_dw(m->x, m->dh1b, G[0], B, kFeatPad, kH1, m->part, status, s);
   // candidate MLP
-  to_bf16_kernel<<<blocks_for((size_t)BC * kEmb), 256, 0, s>>>(m->dgg, m->dggb, BC * kEmb);
-  gemm_dw(m->g1b, m->dggb, G[4], BC, kCandH, kEmb, m->part, s);
-  colsum(m->dgg, BC, kEmb, Gb[4], m->part, s);
-  gemm_dx(m->dggb, W[4], m->dg1, BC, kCandH, kEmb, s);
-  relu_backward_kernel<<<blocks_for((size_t)BC * kCandH), 256, 0, s>>>(m->dg1, m->g1, BC * kCandH);
-  to_bf16_kernel<<<blocks_for((size_t)BC * kCandH), 256, 0, s>>>(m->dg1, m->dg1b, BC * kCandH);
-  gemm_dw(m->xc, m->dg1b, G[3], BC, kCandIn, kCandH, m->part, s);
-  colsum(m->dg1, BC, kCandH, Gb[3], m->part, s);
+  gemm_dw(m->g1b, m->dggb, G[4], BC, kCandH, kEmb, m->part, status, s);
+  gemm_dx(m->dggb, W[4], m->g1b, m->dg1b, Gb[3], BC, kCandH, kEmb, m->part, status, s);
+  gemm_dw(m->xc, m->dg1b, G[3], BC, kCandIn, kCandH, m->part, status, s);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;
+}
+
+// Reads back (and clears) the training kernels' timeout flag after the work
+// queued on s, together with the loss when loss_host is given.
+mptc_status finish_training(mptc_model *m, float *loss_host, cudaStream_t s) {
+  uint32_t flag = 0;
+  if ((loss_host && cudaMemcpyAsync(loss_host, m->loss, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+      cudaMemcpyAsync(&flag, m->status + 4, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return MPTC_ECUDA;
+  if (flag) {
+    cudaMemsetAsync(m->status + 4, 0, 4, s);
+    return MPTC_ETIMEOUT;
+  }
+  return MPTC_OK;
 }
 
 // Refreshes the packed bf16 weight image from the fp32 master weights.
@@ -305,8 +352,8 @@ mptc_status mptc_model_create(uint64_t seed, mptc_model **out) {
   if (!m) return MPTC_ENOMEM;
   const size_t n = kOff.total;
   if (dmalloc(&m->w, n) || dmalloc(&m->wb, n) || dmalloc(&m->g, n) || dmalloc(&m->m, n) || dmalloc(&m->v, n) ||
-      dmalloc(&m->loss, 1) || dmalloc(&m->img, mptc::kImgBytes) || dmalloc(&m->status, 4) || dmalloc(&m->part, kPartFloats) ||
-      cudaMemset(m->img, 0, mptc::kImgBytes) != cudaSuccess || cudaMemset(m->status, 0, 16) != cudaSuccess) {
+      dmalloc(&m->loss, 1) || dmalloc(&m->img, mptc::kImgBytes) || dmalloc(&m->status, 8) ||
+      cudaMemset(m->img, 0, mptc::kImgBytes) != cudaSuccess || cudaMemset(m->status, 0, 32) != cudaSuccess) {
     mptc_model_destroy(m);
     return MPTC_ENOMEM;
   }
@@ -347,7 +394,6 @@ mptc_status mptc_model_destroy(mptc_model *m) {
   cudaFree(m->img);
   cudaFree(m->emb_tmp);
   cudaFree(m->status);
-  cudaFree(m->part);
   delete m;
   return MPTC_OK;
 }
@@ -377,10 +423,9 @@ mptc_status mptc_model_grads(mptc_model *m, const uint8_t *rgb_dev, int32_t widt
   mptc_status st = forward_backward(m, rgb_dev, width, width / 4, stb_dev, blocks_dev, cands_dev, B, C,
                                     grads_host != nullptr, s);
   if (st != MPTC_OK) return st;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return MPTC_ECUDA;
+  st = finish_training(m, loss_host, s);
+  if (st != MPTC_OK) return st;
   if (grads_host && cudaMemcpy(grads_host, m->g, kOff.total * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return MPTC_ECUDA;
-  if (loss_host && cudaMemcpy(loss_host, m->loss, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
     return MPTC_ECUDA;
   return MPTC_OK;
 }
@@ -402,12 +447,9 @@ mptc_status mptc_model_train_step(mptc_model *m, const uint8_t *rgb_dev, int32_t
                                                    weight_decay, c1, c2);
   repack(m, s);
   if (cudaGetLastError() != cudaSuccess) return MPTC_ECUDA;
-  if (loss_host) {
-    if (cudaMemcpyAsync(loss_host, m->loss, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return MPTC_ECUDA;
-  }
-  return MPTC_OK;
+  // without loss_host the step stays asynchronous; a timeout flag it raised
+  // is reported by the next step that reads back
+  return loss_host ? finish_training(m, loss_host, s) : MPTC_OK;
 }
 
 mptc_status mptc_model_save(mptc_model *m, const char *path) {

@@ -207,3 +207,34 @@ def choose_topk(torch, model, frames_dev, search_area=8, err_threshold=5, intra_
     ok = [K for K in ks if table[K][0] <= max_psnr_loss_db]
     best = min(ok, key=lambda K: table[K][1]) if ok else min(ks, key=lambda K: table[K][0])
     return best, table
+
+
+def main(argv=None) -> None:
+    """Trains the proposal on the seeded 1080p training frames and prints the
+    labelling and training times (ms per AdamW step) as one JSON line;
+    --out writes the weights (ProposalModel.load reads them back)."""
+    import argparse
+    import json
+
+    import torch
+
+    from .synth import FHD1080_TRAIN
+    ap = argparse.ArgumentParser(prog="python -m mptc_gb300.training")
+    ap.add_argument("--frames", type=int, default=FHD1080_TRAIN.frames, help="training frames (a prefix of the 200)")
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--cands", type=int, default=32)
+    ap.add_argument("--out", default="")
+    args = ap.parse_args(argv)
+    frames = torch.from_numpy(FHD1080_TRAIN.generate(0, args.frames)).cuda()
+    model, losses, info = train_proposal(torch, frames, steps=args.steps, batch=args.batch, cands=args.cands)
+    info.update(ms_per_step=round(1e3 * info["train_seconds"] / max(1, args.steps), 3),
+                first_loss=round(losses[0], 4), last_loss=round(losses[-1], 4))
+    if args.out:
+        model.save(args.out)
+    model.close()
+    print(json.dumps(info), flush=True)
+
+
+if __name__ == "__main__":
+    main()
