@@ -240,7 +240,7 @@ mptc_status mptc_batch_autotune(mptc_batch *batch, const int32_t *is_intra, int3
                                 int32_t *intra_ctas, int32_t *score_rows, void *stream);
 
 /* ---- Learned candidate proposal (no counterpart in the reference) -------
- * A block MLP f (54 -> 256 -> 256 -> 64 over the 48 pixel bytes, normalised
+ * A block MLP f (54 -> 128 -> 128 -> 64 over the 48 pixel bytes, normalised
  * per channel to the block's range, and the stb endpoints) and a candidate MLP
  * g (32 -> 128 -> 64 over an index word's bits) score window candidates by
  * f(block) . g(candidate). With a model attached, the inter search scores

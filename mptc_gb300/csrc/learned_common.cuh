@@ -1,4 +1,4 @@
-// Learned candidate proposal: a block MLP f (54 -> 256 -> 256 -> 64) and a
+// Learned candidate proposal: a block MLP f (54 -> 128 -> 128 -> 64) and a
 // candidate MLP g (32 -> 128 -> 64) whose dot product scores how likely an
 // index word is to pass a block's exact error test. Only the top-K scored
 // window positions get the exact test; a block none of them passes falls back
@@ -20,7 +20,7 @@
 namespace mptc {
 
 constexpr int kFeatIn = 54, kFeatPad = 64;  // block features, padded K
-constexpr int kH1 = 256, kH2 = 256, kEmb = 64;
+constexpr int kH1 = 128, kH2 = 128, kEmb = 64;  // hidden widths of f, embedding width
 constexpr int kCandIn = 32, kCandH = 128;
 constexpr int kMaxBatch = 32;              // streams (jobs) one learned-proposal launch covers
 constexpr int kMaxK = 16;                  // proposals per block

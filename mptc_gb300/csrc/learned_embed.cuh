@@ -4,7 +4,7 @@
 // ReLU epilogues that turn the accumulator into the next layer's bf16 operand
 // in shared memory).
 //
-// Model: f(block) 54 -> 256 -> 256 -> 64 over the block's 48 pixel bytes
+// Model: f(block) 54 -> 128 -> 128 -> 64 over the block's 48 pixel bytes
 // (normalised per channel to the block's own range) and its stb endpoints
 // (5/6/5-bit values normalised to [0, 1]); g(word) 32 -> 128 -> 64 over the
 // bits of an index word; score = f . g. Operands BF16, accumulation FP32.
@@ -23,12 +23,13 @@ namespace mptc {
 // Every layer's weight as the MMA's B operand: output rows (N) x input columns
 // (K, padded to a multiple of 64), K-major, 128-byte swizzled, in chunks of
 // 64 input columns (chunk kc holds N rows x 128 bytes). f1 | f2 | f3 | g1 | g2.
-constexpr uint32_t kImgF1 = 0;          // 256 x 64
-constexpr uint32_t kImgF2 = 32768;      // 256 x 256: 4 chunks of 32 KB
-constexpr uint32_t kImgF3 = 163840;     // 64 x 256: 4 chunks of 8 KB
-constexpr uint32_t kImgG1 = 196608;     // 128 x 64 (32 inputs, zero padded)
-constexpr uint32_t kImgG2 = 212992;     // 64 x 128: 2 chunks of 8 KB
-constexpr uint32_t kImgBytes = 229376;
+constexpr uint32_t kImgF1 = 0;                                       // kH1 x 64
+constexpr uint32_t kImgF2 = kImgF1 + (uint32_t)kH1 * kFeatPad * 2;   // kH2 x kH1: kH1 / 64 chunks
+constexpr uint32_t kImgF3 = kImgF2 + (uint32_t)kH2 * kH1 * 2;        // 64 x kH2: kH2 / 64 chunks
+constexpr uint32_t kImgG1 = kImgF3 + (uint32_t)kEmb * kH2 * 2;       // kCandH x 64 (32 inputs, zero padded)
+constexpr uint32_t kImgG2 = kImgG1 + (uint32_t)kCandH * 64 * 2;      // 64 x kCandH: kCandH / 64 chunks
+constexpr uint32_t kImgBytes = kImgG2 + (uint32_t)kEmb * kCandH * 2;
+static_assert(kH1 % 64 == 0 && kH2 % 64 == 0 && kH1 + kH2 <= 512, "f's accumulators fit in TMEM");
 
 // Image element (n, k) of a layer with `in` inputs and `out` outputs from the
 // fp32 master weight W[in][out] (y = x W + b).
@@ -67,11 +68,11 @@ struct EmbedBatch {
   uint32_t *next;            // tile counter (zero before the launch)
 };
 
-// The f network (three layers, TMEM 512 columns: acc1 [0,256), acc2
-// [256,512), acc3 [0,64)) and the g network (two layers, TMEM 256 columns:
-// acc1 [0,128), acc2 [128,192)).
+// The f network (three layers, TMEM kH1 + kH2 columns: acc1 [0, kH1), acc2
+// [kH1, kH1 + kH2), acc3 [0, 64)) and the g network (two layers, TMEM 256
+// columns: acc1 [0,128), acc2 [128,192)).
 struct NetF {
-  static constexpr int kLayers = 3, N1 = 256, N2 = 256, N3 = 64, kTmem = 512;
+  static constexpr int kLayers = 3, N1 = kH1, N2 = kH2, N3 = kEmb, kTmem = kH1 + kH2;
   static constexpr uint32_t kW = kImgF1, kWBytes = kImgG1 - kImgF1;
   static constexpr uint32_t kW1 = kImgF1 - kW, kW2 = kImgF2 - kW, kW3 = kImgF3 - kW;
 };

@@ -266,13 +266,16 @@ void repack(mptc_model *m, cudaStream_t s) {
 }
 
 // Dynamic shared memory of the embedding kernels, set once per device. The f
-// kernel needs all but 2 KB of an SM's shared memory (one CTA per SM, its
-// 512 TMEM columns); the g kernel asks for 80 KB so that at most two CTAs
-// (256 TMEM columns each) share an SM.
+// kernel's weights and operand buffers (98 KB with 128-wide hidden layers)
+// let at most two CTAs share an SM, which is what their TMEM columns
+// (kH1 + kH2 = 256 each) allow; the g kernel asks for 80 KB so that at most
+// two CTAs (256 TMEM columns each) share an SM.
 constexpr int kMaxDev = 64;
 std::mutex g_attr_mu;
 bool g_attr_done[kMaxDev] = {};
 constexpr size_t kSmemF = mptc::embed_smem_bytes<mptc::NetF>();
+constexpr int kCtasF = 512 / mptc::NetF::kTmem;  // f CTAs per SM
+static_assert(kCtasF == 1 || kSmemF * 3 > 228 * 1024, "shared memory keeps f's CTAs within the TMEM columns");
 constexpr size_t kSmemG = mptc::embed_smem_bytes<mptc::NetG>() > 81920 ? mptc::embed_smem_bytes<mptc::NetG>() : 81920;
 
 cudaError_t ensure_embed_attrs() {
@@ -333,7 +336,7 @@ mptc_status model_embed(const mptc_model *m, bool blocks, const EmbedJob *jobs, 
   if (tiles == 0) return MPTC_OK;
   const int sms = sm_count_now();
   if (blocks)
-    mptc::embed_kernel<mptc::NetF, true><<<std::min(tiles, sms), mptc::kEmbedThreads, kSmemF, s>>>(b);
+    mptc::embed_kernel<mptc::NetF, true><<<std::min(tiles, kCtasF * sms), mptc::kEmbedThreads, kSmemF, s>>>(b);
   else
     mptc::embed_kernel<mptc::NetG, false><<<std::min(tiles, 2 * sms), mptc::kEmbedThreads, kSmemG, s>>>(b);
   return cudaGetLastError() == cudaSuccess ? MPTC_OK : MPTC_ECUDA;

@@ -3,7 +3,7 @@ training loop over the C ABI (mptc_model_*). Training runs on the GPU in the
 library's own tensor-core kernels; this module only prepares index arrays.
 
 Layers (flat fp32 parameter vector, weight [in x out] then bias per layer):
-f1 64(54 used) -> 256, f2 256 -> 256, f3 256 -> 64 (block MLP, ReLU between),
+f1 64(54 used) -> 128, f2 128 -> 128, f3 128 -> 64 (block MLP, ReLU between),
 g1 32 -> 128, g2 128 -> 64 (candidate MLP over the index word's bits).
 """
 from __future__ import annotations
@@ -15,7 +15,7 @@ import numpy as np
 
 from ._lib import check, dev_ptr, lib
 
-LAYERS = [(64, 256), (256, 256), (256, 64), (32, 128), (128, 64)]
+LAYERS = [(64, 128), (128, 128), (128, 64), (32, 128), (128, 64)]
 
 
 def param_slices():
@@ -42,6 +42,8 @@ class ProposalModel:
         check(lib().mptc_model_create(ctypes.c_uint64(seed), ctypes.byref(h)))
         self._m = h
         self.n_params = int(lib().mptc_model_num_params())
+        if self.n_params != param_slices()[1]:
+            raise RuntimeError(f"library has {self.n_params} parameters, LAYERS describe {param_slices()[1]}")
 
     @property
     def handle(self):
