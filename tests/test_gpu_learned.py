@@ -339,6 +339,25 @@ def held_out_stats(torch, frames, sa, model, K):
     return fallback / inter, hit / max(1, total)
 
 
+def test_training_cli_trains_and_saves(torch_cuda, tmp_path, capsys):
+    """python -m mptc_gb300.training: labels seeded 1080p frames with the
+    exhaustive search, trains, prints one JSON line and writes weights that
+    load back into a fresh model."""
+    import json
+
+    from mptc_gb300 import training
+    from mptc_gb300.model import ProposalModel
+    out = tmp_path / "proposal.bin"
+    training.main(["--frames", "3", "--steps", "5", "--out", str(out)])
+    info = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert info["steps"] == 5 and info["examples"] > 0 and np.isfinite(info["last_loss"]), info
+    m = ProposalModel(seed=9)
+    m.load(str(out))
+    p = m.params()
+    m.close()
+    assert p.size > 0 and np.isfinite(p).all()
+
+
 def test_trained_network_gains_over_untrained(torch_cuda):
     """On held-out frames (a separate seed), the trained network needs the
     exhaustive fallback for fewer blocks and proposes the exhaustive search's
