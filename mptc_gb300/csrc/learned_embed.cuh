@@ -53,17 +53,19 @@ struct EmbedArgs {
   int word_stride;
   const uint8_t *wimg;      // packed weight image (kImgBytes)
   const float *b1, *b2, *b3;  // biases (fp32)
-  __nv_bfloat16 *out;       // n x 64
+  __nv_bfloat16 *out;       // n x 64 (row out_rows[i] for row i when out_rows is set)
   uint32_t *status;         // device status word (kDevTimeout on an expired wait)
+  const uint32_t *n_dev;    // rows: min(n, *n_dev) when set (a count written on the device)
+  const uint32_t *out_rows; // output row of row i, or NULL (row i)
 };
 
 // A launch covers the rows of up to kMaxBatch jobs (the streams of a batch,
 // or one): tiles of 128 rows are numbered across the jobs (job j owns tiles
-// [tile_end[j-1], tile_end[j])) and CTAs take them from one counter, so
-// streams of uneven resolution share the persistent grid.
+// [tile_end[j-1], tile_end[j]), counted by each CTA at its start from the
+// jobs' row counts) and CTAs take them from one counter, so streams of uneven
+// resolution share the persistent grid.
 struct EmbedBatch {
   int n;                     // jobs
-  int tile_end[kMaxBatch];   // inclusive prefix of the jobs' tile counts
   EmbedArgs a[kMaxBatch];
   uint32_t *next;            // tile counter (zero before the launch)
 };
@@ -145,6 +147,24 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
   volatile uint32_t *abort_flag = tslot + 1;
   volatile int *s_tile = reinterpret_cast<volatile int *>(tslot + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = warp & 3, h = warp >> 2;
+  // the jobs' row counts and tile ends; the first tile is claimed before the
+  // setup, so that CTAs left without a tile (device-side counts below the
+  // launch's bound) return at once
+  __shared__ int s_rows[kMaxBatch], s_tend[kMaxBatch];
+  if (tid == 0) {
+    int acc = 0;
+    for (int j = 0; j < batch.n; ++j) {
+      const EmbedArgs &aj = batch.a[j];
+      const int rows = aj.n_dev ? min(aj.n, (int)*aj.n_dev) : aj.n;
+      acc += (rows + 127) / 128;
+      s_rows[j] = rows;
+      s_tend[j] = acc;
+    }
+    *s_tile = (int)atomicAdd(batch.next, 1u);
+  }
+  __syncthreads();
+  const int total = s_tend[batch.n - 1];
+  if (*s_tile >= total) return;
   if (tid == 0) {
     for (int i = 0; i < 4; ++i) tc::mbar_init(bar + i, 1);
     *abort_flag = 0;
@@ -168,7 +188,6 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
   };
   const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
   const int row = 32 * q + lane;
-  const int total = batch.tile_end[batch.n - 1];
   // The next tile is drawn while the current one is in its hidden layers and
   // its input words are loaded then, so the feature build never waits on
   // global memory.
@@ -180,8 +199,8 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
   } pf;
   auto locate = [&](int gt, int &jb, int &tile) {
     jb = 0;
-    while (gt >= batch.tile_end[jb]) ++jb;
-    tile = gt - (jb ? batch.tile_end[jb - 1] : 0);
+    while (gt >= s_tend[jb]) ++jb;
+    tile = gt - (jb ? s_tend[jb - 1] : 0);
   };
   auto prefetch = [&](int gt) {
     pf.valid = false;
@@ -190,7 +209,7 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
     locate(gt, jb, tile);
     const EmbedArgs &a = batch.a[jb];
     const int gi = tile * 128 + (tid >> 1);
-    if (gi >= a.n) return;
+    if (gi >= s_rows[jb]) return;
     pf.valid = true;
     if constexpr (kBlocks) {
       const int bi = a.blocks ? (int)__ldg(a.blocks + gi) : gi;
@@ -201,8 +220,6 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
       pf.word = __ldg(a.words + (size_t)gi * a.word_stride);
     }
   };
-  if (tid == 0) *s_tile = (int)atomicAdd(batch.next, 1u);
-  __syncthreads();
   int gt = *s_tile;
   prefetch(gt);
   for (;;) {
@@ -306,14 +323,15 @@ __global__ void __launch_bounds__(kEmbedThreads, 1) embed_kernel(const __grid_co
       }
       tc::tmem_ld32(lane_base + out_col + 32 * h, v);
       const int gi = tile * 128 + row;
-      if (gi < a.n) {
+      if (gi < s_rows[jb]) {
         uint32_t pk[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] + bb[2 * j], v[2 * j + 1] + bb[2 * j + 1]);
           pk[j] = *reinterpret_cast<const uint32_t *>(&b2);
         }
-        uint4 *dst = reinterpret_cast<uint4 *>(a.out + (size_t)gi * kEmb + 32 * h);
+        const size_t orow = a.out_rows ? (size_t)__ldg(a.out_rows + gi) : (size_t)gi;
+        uint4 *dst = reinterpret_cast<uint4 *>(a.out + orow * kEmb + 32 * h);
 #pragma unroll
         for (int j = 0; j < 4; ++j) dst[j] = make_uint4(pk[4 * j], pk[4 * j + 1], pk[4 * j + 2], pk[4 * j + 3]);
       }

@@ -27,7 +27,8 @@ namespace mptc {
 // Per tile, in shared memory:
 //  1. the palette: the union's distinct words by an open-addressed hash
 //     table (1024 slots, linear probing), numbered in slot order, each with
-//     one frame position holding it; every union position's palette id;
+//     the G row of its word (read with the words, a tile ahead); every union
+//     position's palette id;
 //  2. per slice of SL palette entries (the dictionary slice of a stage;
 //     SL = 16 ROWS): the slice's G rows gathered in the 128-byte-swizzled
 //     K-major layout and one tcgen05 MMA of the tile's F rows (eight TMA
@@ -59,7 +60,8 @@ struct ScoreArgs {
   int bw, bh, sa;
   const uint32_t *words;      // the previous frame's index words, words[pos * word_stride]
   int word_stride;
-  const __nv_bfloat16 *gemb;  // G rows of the previous frame's blocks, [bh * bw][64]
+  const __nv_bfloat16 *gemb;  // G rows, [rows][64]
+  const uint32_t *rows;       // G row of the word at each position (NULL: row = position)
   uint16_t *topk;             // n x kMaxK window positions, best first
   uint32_t *status;           // device status word
 };
@@ -147,8 +149,8 @@ struct ScoreSmem {
   static constexpr size_t Hash = Carry + (size_t)128 * K * 4;
   static constexpr size_t Slot = Hash + (size_t)kPalSlots * 8;      // union position -> slot -> palette id
   static constexpr size_t PalIdx = Slot + (size_t)kPalSlots * 2;    // slot -> palette id
-  static constexpr size_t PalPos = PalIdx + (size_t)kPalSlots * 2;  // palette id -> frame position
-  static constexpr size_t Pid = PalPos + (size_t)kPalSlots * 4;      // union position -> palette id | flags
+  static constexpr size_t PalRow = PalIdx + (size_t)kPalSlots * 2;  // palette id -> G row
+  static constexpr size_t Pid = PalRow + (size_t)kPalSlots * 4;      // union position -> palette id | flags
   static constexpr size_t WarpTot = Pid + (size_t)kPalSlots * 2;
   static constexpr size_t Bars = WarpTot + kScoreWarps * 4;
   static constexpr size_t Bytes = Bars + 64;
@@ -177,7 +179,7 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
   unsigned long long *const sHash = reinterpret_cast<unsigned long long *>(sm + L::Hash);
   uint16_t *const sSlot = reinterpret_cast<uint16_t *>(sm + L::Slot);
   uint16_t *const sPalIdx = reinterpret_cast<uint16_t *>(sm + L::PalIdx);
-  uint32_t *const sPalPos = reinterpret_cast<uint32_t *>(sm + L::PalPos);
+  uint32_t *const sPalRow = reinterpret_cast<uint32_t *>(sm + L::PalRow);
   uint16_t *const sPid = reinterpret_cast<uint16_t *>(sm + L::Pid);
   uint32_t *const sWarpTot = reinterpret_cast<uint32_t *>(sm + L::WarpTot);
   uint64_t *const bar = reinterpret_cast<uint64_t *>(sm + L::Bars);  // F, M
@@ -230,10 +232,10 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
       tc::tma_load_3d(sF + cc * kFColBytes, &batch.tmF[t.jb], 0, t.tx0 + cc, t.ty0, bar);
   };
   const int total = batch.tile_end[batch.n - 1];
-  // the union words of a tile, read ahead: thread tid holds cells tid and
-  // tid + 512 (713 at most) of tile pf
+  // the union words of a tile and their G rows, read ahead: thread tid
+  // holds cells tid and tid + 512 (713 at most) of tile pf
   constexpr int kCellsPerThread = (kPalSlots + kScoreThreads - 1) / kScoreThreads;
-  uint32_t pw[kCellsPerThread];
+  uint32_t pw[kCellsPerThread], prow[kCellsPerThread];
   int pf = -1;
   auto read_words = [&](int gt) {
     const TileAt t = locate(gt);
@@ -243,11 +245,15 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
     for (int i = 0; i < kCellsPerThread; ++i) {
       const int q = tid + i * kScoreThreads;
       pw[i] = 0;
+      prow[i] = 0;
       if (q < nU) {
         const int uy = q / UC, ux = q - uy * UC;
         const int gy = t.ty0 - a.sa + uy, gx = t.tx0 - a.sa + ux;
-        if (gy >= 0 && gy < a.bh && gx >= 0 && gx < a.bw)
-          pw[i] = __ldg(a.words + ((size_t)gy * a.bw + gx) * a.word_stride);
+        if (gy >= 0 && gy < a.bh && gx >= 0 && gx < a.bw) {
+          const uint32_t pos = (uint32_t)gy * (uint32_t)a.bw + (uint32_t)gx;
+          pw[i] = __ldg(a.words + (size_t)pos * a.word_stride);
+          prow[i] = a.rows ? __ldg(a.rows + pos) : pos;
+        }
       }
     }
     pf = gt;
@@ -279,9 +285,8 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
       const int gy = ty0 - sa + uy, gx = tx0 - sa + ux;
       uint16_t slot = 0xFFFFu;
       if (gy >= 0 && gy < a.bh && gx >= 0 && gx < a.bw) {
-        const uint32_t pos = (uint32_t)gy * (uint32_t)a.bw + (uint32_t)gx;
         const uint32_t word = pw[i];
-        const unsigned long long entry = ((unsigned long long)word << 32) | (unsigned long long)(pos + 1u);
+        const unsigned long long entry = ((unsigned long long)word << 32) | (unsigned long long)(prow[i] + 1u);
         uint32_t h = pal_hash(word);
         for (int it = 0; it < kPalSlots; ++it) {  // the table never fills: it ends
           const unsigned long long old = atomicCAS(sHash + h, 0ull, entry);
@@ -315,12 +320,12 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
       if (h0) {
         const int id = base + __popc(b0 & lt);
         sPalIdx[s0] = (uint16_t)id;
-        sPalPos[id] = (uint32_t)h0 - 1u;
+        sPalRow[id] = (uint32_t)h0 - 1u;
       }
       if (h1) {
         const int id = base + __popc(b0) + __popc(b1 & lt);
         sPalIdx[s1] = (uint16_t)id;
-        sPalPos[id] = (uint32_t)h1 - 1u;
+        sPalRow[id] = (uint32_t)h1 - 1u;
       }
     }
     __syncthreads();
@@ -332,7 +337,7 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
     for (int i = 0; i < kGPerThread; ++i) {
       const int c = tid + i * kScoreThreads, e = c >> 3, j = c & 7;
       gv[i] = make_uint4(0u, 0u, 0u, 0u);
-      if (e < nc0) gv[i] = __ldg(reinterpret_cast<const uint4 *>(a.gemb + (size_t)sPalPos[e] * kEmb) + j);
+      if (e < nc0) gv[i] = __ldg(reinterpret_cast<const uint4 *>(a.gemb + (size_t)sPalRow[e] * kEmb) + j);
     }
     for (int q = tid; q < nU; q += kScoreThreads) {
       const uint16_t sl = sSlot[q];
@@ -364,7 +369,7 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
         for (int i = tid; i < SL * 8; i += kScoreThreads) {
           const int e = i >> 3, j = i & 7;
           uint4 v = make_uint4(0u, 0u, 0u, 0u);
-          if (e < nc) v = __ldg(reinterpret_cast<const uint4 *>(a.gemb + (size_t)sPalPos[e0 + e] * kEmb) + j);
+          if (e < nc) v = __ldg(reinterpret_cast<const uint4 *>(a.gemb + (size_t)sPalRow[e0 + e] * kEmb) + j);
           *reinterpret_cast<uint4 *>(sG + tc::sw128_offset((uint32_t)e, (uint32_t)j)) = v;
         }
         tc::fence_async_smem();

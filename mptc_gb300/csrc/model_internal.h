@@ -12,7 +12,9 @@ namespace mptc_internal {
 // One embedding job: the f network over `n` blocks of a frame (rgb, width a
 // multiple of 4, 4-byte aligned frame; stb endpoints; blocks NULL = blocks
 // 0 .. n-1 in raster order) or the g network over n index words
-// (words[i * word_stride]); bf16 output n x 64. An expired device-side wait
+// (words[i * word_stride]); bf16 output n x 64, row i at out_rows[i] when
+// out_rows is set. With n_dev set the job has min(n, *n_dev) rows (a count
+// written on the device by an earlier launch). An expired device-side wait
 // ORs kDevTimeout into *status.
 struct EmbedJob {
   const uint8_t *rgb = nullptr;
@@ -24,6 +26,8 @@ struct EmbedJob {
   int n = 0;
   __nv_bfloat16 *out = nullptr;
   uint32_t *status = nullptr;
+  const uint32_t *n_dev = nullptr;
+  const uint32_t *out_rows = nullptr;
 };
 
 // Jobs a single embedding launch takes (the streams of a batch).

@@ -15,6 +15,7 @@
 #include "dxt1_encode.cuh"
 #include "search.cuh"
 #include "learned_search.cuh"
+#include "learned_dict.cuh"
 #include "learned_tc.cuh"
 #include "model_internal.h"
 
@@ -45,10 +46,17 @@ struct mptc_ctx {
   int inter_warps = kSearchWarps, intra_cap = 0;
   // learned proposal (optional): K proposals per block, union rows per
   // scoring stage (4 or 8), bf16 embeddings of this frame's blocks (F) and of
-  // the previous frame's final blocks (G), their TMA tensor maps, top-K lists
+  // the distinct words of the previous frame's final blocks (G, one row per
+  // dictionary table slot), their TMA tensor maps, top-K lists
   const mptc_model *model = nullptr;
   int topk_k = 0, score_rows = 8;
   __nv_bfloat16 *femb = nullptr, *gemb = nullptr;
+  // the previous frame's word dictionary (word_dict_kernel): a table of
+  // 2^dict_log2 entries followed by one word holding the list's count, each
+  // position's table slot, the list of distinct words and their slots
+  unsigned long long *dict = nullptr;
+  int dict_log2 = 0;
+  uint32_t *dict_rows = nullptr, *dict_words = nullptr, *dict_slots = nullptr;
   uint16_t *topk = nullptr;
   CUtensorMap tm_f{};  // F rows in boxes of one block column, 16 rows
   // device scratch
@@ -225,7 +233,7 @@ enum KernelId {
 // learned proposal's kernels when a model is attached)
 const char *kKernelNames[K_COUNT] = {"dxt1_encode_kernel",      "inter_search",
                                      "intra_search_kernel",     "intra_sweep_kernel/inter_frame",
-                                     "unique_scan_kernel",      "embed_kernel/g",
+                                     "unique_scan_kernel",      "word_dict+embed_kernel/g",
                                      "embed_kernel/f",          "score_topk_tc_kernel",
                                      "learned_eval_kernel",     "inter_list_kernel"};
 
@@ -406,6 +414,41 @@ void launch_eval(const mptc::EvalBatch &eb, int sm_count, cudaStream_t s) {
   mptc::learned_eval_kernel<K, WARPS><<<grid, WARPS * 32, 0, s>>>(eb);
 }
 
+// The g half of the learned search for up to kMaxBatch previous frames
+// (prev_words[j]: frame j's final blocks as u32 pairs, the index word second):
+// each context's word dictionary is cleared, one word_dict_kernel launch
+// fills them all, then one g launch embeds every dictionary's distinct words
+// into the contexts' G tables (the row of a word is its table slot). Two
+// kernel launches; `counter` is a zeroed tile counter for the g launch.
+mptc_status launch_g(mptc_ctx *const *ctxs, const uint32_t *const *prev_words, int n, uint32_t *counter,
+                     cudaStream_t s) {
+  mptc::DictBatch db{};
+  db.n = n;
+  mptc_internal::EmbedJob ej[mptc::kMaxBatch];
+  int blocks = 0;
+  for (int j = 0; j < n; ++j) {
+    mptc_ctx *c = ctxs[j];
+    const size_t cap = (size_t)1 << c->dict_log2;
+    if (cudaMemsetAsync(c->dict, 0, (cap + 1) * sizeof(unsigned long long), s) != cudaSuccess) return MPTC_ECUDA;
+    uint32_t *count = reinterpret_cast<uint32_t *>(c->dict + cap);
+    db.a[j] = mptc::DictArgs{prev_words[j], 2, c->nblk, c->dict, c->dict_log2, c->dict_rows,
+                             c->dict_words, c->dict_slots, count};
+    blocks += (c->nblk + mptc::kDictThreads - 1) / mptc::kDictThreads;
+    db.block_end[j] = blocks;
+    ej[j] = mptc_internal::EmbedJob{};
+    ej[j].words = c->dict_words;
+    ej[j].word_stride = 1;
+    ej[j].n = c->nblk;
+    ej[j].n_dev = count;
+    ej[j].out = c->gemb;
+    ej[j].out_rows = c->dict_slots;
+    ej[j].status = c->work + 1;
+  }
+  mptc::word_dict_kernel<<<blocks, mptc::kDictThreads, 0, s>>>(db);
+  if (cudaGetLastError() != cudaSuccess) return MPTC_ECUDA;
+  return mptc_internal::model_embed(ctxs[0]->model, false, ej, n, counter, s);
+}
+
 // One inter frame of a context with a model attached: its frame and the
 // search parameters of the frame.
 struct LearnedJob {
@@ -425,18 +468,15 @@ struct LearnedJob {
 int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream_t s) {
   mptc_ctx *c0 = jobs[0].ctx;
   mptc_internal::EmbedJob ej[mptc::kMaxBatch];
-  for (int j = 0; j < n; ++j) {
-    mptc_ctx *c = jobs[j].ctx;
-    ej[j] = mptc_internal::EmbedJob{};
-    ej[j].words = reinterpret_cast<const uint32_t *>(jobs[j].P.prev) + 1;
-    ej[j].word_stride = 2;
-    ej[j].n = c->nblk;
-    ej[j].out = c->gemb;
-    ej[j].status = c->work + 1;
-  }
   {
     KernelTimer t(c0, K_EMBED_G, s);
-    mptc_internal::model_embed(c0->model, false, ej, n, counters, s);
+    mptc_ctx *ctxs[mptc::kMaxBatch];
+    const uint32_t *prev[mptc::kMaxBatch];
+    for (int j = 0; j < n; ++j) {
+      ctxs[j] = jobs[j].ctx;
+      prev[j] = reinterpret_cast<const uint32_t *>(jobs[j].P.prev) + 1;
+    }
+    launch_g(ctxs, prev, n, counters, s);
   }
   for (int j = 0; j < n; ++j) {
     mptc_ctx *c = jobs[j].ctx;
@@ -468,7 +508,7 @@ int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream
              ((c->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
     sb.tile_end[j] = tiles;
     sb.a[j] = mptc::ScoreArgs{c->bw, c->bh, c->cfg.search_area, reinterpret_cast<const uint32_t *>(jobs[j].P.prev) + 1,
-                              2, c->gemb, c->topk, c->work + 1};
+                              2, c->gemb, c->dict_rows, c->topk, c->work + 1};
     sb.tmF[j] = c->tm_f;
     groups += (c->nblk + bpw - 1) / bpw;
     eb.group_end[j] = groups;
@@ -501,7 +541,7 @@ int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream
     KernelTimer t(c0, K_FALLBACK, s);
     mptc::inter_list_kernel<256><<<sms * 4, 256, 0, s>>>(lb);  // CTAs past the lists' end return at once
   }
-  return 5;
+  return 6;
 }
 
 mptc_status reencode_check(mptc_ctx *ctx, const uint8_t *rgb_dev, const uint64_t *stb_dev,
@@ -656,6 +696,10 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->sweep_part);
   cudaFree(ctx->femb);
   cudaFree(ctx->gemb);
+  cudaFree(ctx->dict);
+  cudaFree(ctx->dict_rows);
+  cudaFree(ctx->dict_words);
+  cudaFree(ctx->dict_slots);
   cudaFree(ctx->topk);
   if (ctx->pin_in) cudaFreeHost(ctx->pin_in);
   if (ctx->pin_out) cudaFreeHost(ctx->pin_out);
@@ -1088,8 +1132,14 @@ mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k
   if (ctx->cfg.search_area > 8) return fail(ctx, MPTC_EINVAL, "learned proposal: search area above 8");
   const size_t n = (size_t)ctx->nblk;
   if (!ctx->femb) {
-    if (dalloc(&ctx->femb, n * mptc::kEmb) || dalloc(&ctx->gemb, n * mptc::kEmb) || dalloc(&ctx->topk, n * mptc::kMaxK))
+    int lg = 1;
+    while (((size_t)1 << lg) < 2 * n) ++lg;  // the dictionary table at most half full
+    const size_t cap = (size_t)1 << lg;
+    if (dalloc(&ctx->femb, n * mptc::kEmb) || dalloc(&ctx->gemb, cap * mptc::kEmb) ||
+        dalloc(&ctx->topk, n * mptc::kMaxK) || dalloc(&ctx->dict, cap + 1) || dalloc(&ctx->dict_rows, n) ||
+        dalloc(&ctx->dict_words, n) || dalloc(&ctx->dict_slots, n))
       return fail(ctx, MPTC_ENOMEM, "learned proposal buffers");
+    ctx->dict_log2 = lg;
     if (!embedding_map(&ctx->tm_f, ctx->femb, ctx->bw, ctx->bh, 1, mptc::kScoreTileH))
       return fail(ctx, MPTC_ECUDA, "learned proposal: tensor map encoding failed");
     MPTC_CUDA((score_attr<8, 4>()));
@@ -1116,13 +1166,9 @@ mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const 
   MPTC_CUDA(cudaMemsetAsync(ctx->work, 0, work_bytes(ctx->ntiles), s));
   MPTC_CUDA(cudaMemsetAsync(ctx->topk, 0xFF, (size_t)n * mptc::kMaxK * sizeof(uint16_t), s));
   // the learned search's embedding and scoring launches for this one frame
+  const uint32_t *prev_words = reinterpret_cast<const uint32_t *>(prev_final_dev) + 1;
+  mptc_status st = launch_g(&ctx, &prev_words, 1, ctx->work + 12, s);
   mptc_internal::EmbedJob ej;
-  ej.words = reinterpret_cast<const uint32_t *>(prev_final_dev) + 1;
-  ej.word_stride = 2;
-  ej.n = n;
-  ej.out = ctx->gemb;
-  ej.status = ctx->work + 1;
-  mptc_status st = mptc_internal::model_embed(ctx->model, false, &ej, 1, ctx->work + 12, s);
   if (st == MPTC_OK) {
     ej = mptc_internal::EmbedJob{};
     ej.rgb = rgb_dev;
@@ -1140,7 +1186,7 @@ mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const 
   sb.tile_end[0] = ((ctx->bw + mptc::kScoreTileW - 1) / mptc::kScoreTileW) *
                    ((ctx->bh + mptc::kScoreTileH - 1) / mptc::kScoreTileH);
   sb.a[0] = mptc::ScoreArgs{ctx->bw, ctx->bh, ctx->cfg.search_area, reinterpret_cast<const uint32_t *>(prev_final_dev) + 1,
-                            2, ctx->gemb, ctx->topk, ctx->work + 1};
+                            2, ctx->gemb, ctx->dict_rows, ctx->topk, ctx->work + 1};
   const bool r8 = ctx->score_rows == 8;
   sb.tmF[0] = ctx->tm_f;
   switch (ctx->topk_k) {

@@ -330,8 +330,9 @@ mptc_status model_embed(const mptc_model *m, bool blocks, const EmbedJob *jobs, 
     a.b3 = blocks ? m->w + kOff.b[2] : nullptr;
     a.out = J.out;
     a.status = J.status ? J.status : m->status;
-    tiles += (J.n + 127) / 128;
-    b.tile_end[j] = tiles;
+    a.n_dev = J.n_dev;
+    a.out_rows = J.out_rows;
+    tiles += (J.n + 127) / 128;  // an upper bound when n_dev is set
   }
   if (tiles == 0) return MPTC_OK;
   const int sms = sm_count_now();
