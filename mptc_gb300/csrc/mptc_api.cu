@@ -1572,7 +1572,8 @@ mptc_status batch_run_frames(mptc_batch *b, int32_t n_frames, const uint8_t *con
   for (int i = 0; i < S; ++i) {
     mptc_ctx *c = b->ctx[i];
     if (cudaStreamWaitEvent(b->streams[i], b->run_start, 0) != cudaSuccess ||
-        cudaStreamWaitEvent(c->lane_s, b->run_start, 0) != cudaSuccess)
+        cudaStreamWaitEvent(c->lane_s, b->run_start, 0) != cudaSuccess ||
+        cudaStreamWaitEvent(c->stb_s, b->run_start, 0) != cudaSuccess)
       return MPTC_ECUDA;
   }
   // every intra frame, on its stream's lane
@@ -1588,9 +1589,12 @@ mptc_status batch_run_frames(mptc_batch *b, int32_t n_frames, const uint8_t *con
       if (cudaEventRecord(b->lane_ev[i][k], c->lane_s) != cudaSuccess) return MPTC_ECUDA;
     }
   }
-  // the inter frames, step by step
+  // the inter frames, step by step; each stream's stb encodes run on its
+  // stb stream into the ring slots, so that they overlap the previous steps
+  // (a slot is reused once the frame that read it has finished)
   std::vector<mptc::SearchParams> P(S);
   std::vector<char> active(S);
+  std::vector<int> n_inter(S, 0), slot(S, 0);
   for (int k = 0; k < n_frames; ++k) {
     std::vector<LearnedJob> jobs;
     for (int i = 0; i < S; ++i) {
@@ -1604,9 +1608,16 @@ mptc_status batch_run_frames(mptc_batch *b, int32_t n_frames, const uint8_t *con
           cudaStreamWaitEvent(si, b->lane_ev[i][k - 1], 0) != cudaSuccess)
         return MPTC_ECUDA;
       const uint8_t *in = frames[i] + k * n * 48;
-      mptc_status st = mptc_dxt1_encode(c, in, c->stb, c->orig_err, si);
+      const int j = n_inter[i] % kStbRing;
+      if (n_inter[i]++ >= kStbRing && cudaStreamWaitEvent(c->stb_s, c->stb_free[j], 0) != cudaSuccess)
+        return MPTC_ECUDA;
+      slot[i] = j;
+      mptc_status st = mptc_dxt1_encode(c, in, c->stb_slot[j], c->orig_slot[j], c->stb_s);
       if (st != MPTC_OK) return st;
-      P[i] = make_params(c, in, c->stb, c->orig_err, prev, fin[i] + k * n, mot[i] + 2 * k * n);
+      if (cudaEventRecord(c->stb_done[j], c->stb_s) != cudaSuccess ||
+          cudaStreamWaitEvent(si, c->stb_done[j], 0) != cudaSuccess)
+        return MPTC_ECUDA;
+      P[i] = make_params(c, in, c->stb_slot[j], c->orig_slot[j], prev, fin[i] + k * n, mot[i] + 2 * k * n);
       st = reencode_begin(c, P[i], si);
       if (st != MPTC_OK) return st;
       if (c->model) {
@@ -1639,6 +1650,7 @@ mptc_status batch_run_frames(mptc_batch *b, int32_t n_frames, const uint8_t *con
       mptc_status st = reencode_finish(c, P[i], uni[i] + k * n, n_uni[i] + k, si);
       if (st != MPTC_OK) return st;
       status_or_kernel<<<1, 32, 0, si>>>(c->work, b->run_status);
+      if (cudaEventRecord(c->stb_free[slot[i]], si) != cudaSuccess) return MPTC_ECUDA;
     }
   }
   // `stream` completes after every stream and lane; each stream's last frame
