@@ -144,8 +144,10 @@ struct ScoreSmem {
   static constexpr size_t F = 0;
   static constexpr size_t G = F + tc::kTileBytes;
   static constexpr size_t First = G + (size_t)SL * 128;
-  static constexpr size_t Part = First + (size_t)128 * kRow * 4;    // 128 x 4 x K rank keys
-  static constexpr size_t Carry = Part + (size_t)128 * 4 * K * 4;   // 128 x K rank keys
+  // rank keys, block index fastest (a warp's 32 blocks in 32 banks):
+  // Part [4 groups x K][128 blocks], Carry [K][128 blocks]
+  static constexpr size_t Part = First + (size_t)128 * kRow * 4;
+  static constexpr size_t Carry = Part + (size_t)128 * 4 * K * 4;
   static constexpr size_t Hash = Carry + (size_t)128 * K * 4;
   static constexpr size_t Slot = Hash + (size_t)kPalSlots * 8;      // union position -> slot -> palette id
   static constexpr size_t PalIdx = Slot + (size_t)kPalSlots * 2;    // slot -> palette id
@@ -432,9 +434,8 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
         for (int c = 0; c < 32; c += K) sort_desc<K>(rk + c);
 #pragma unroll
         for (int c = K; c < 32; c += K) merge_top<K>(rk, rk + c);
-        uint32_t *const part = sPart + (mt * 4 + g) * K;
 #pragma unroll
-        for (int i = 0; i < K; i += 4) *reinterpret_cast<uint4 *>(part + i) = make_uint4(rk[i], rk[i + 1], rk[i + 2], rk[i + 3]);
+        for (int i = 0; i < K; ++i) sPart[(g * K + i) * 128 + mt] = rk[i];
       }
       tc::tc_fence_before();
       __syncthreads();  // partial lists written; TMEM and the F rows free
@@ -445,26 +446,24 @@ __global__ void __launch_bounds__(kScoreThreads, 1) score_topk_tc_kernel(const _
       }
       if (g == 0 && t_in) {  // the block's best K: its four lists and the best K so far
         uint32_t best[K], other[K];
-        const uint32_t *part = sPart + mt * 4 * K;
 #pragma unroll
-        for (int i = 0; i < K; ++i) best[i] = part[i];
+        for (int i = 0; i < K; ++i) best[i] = sPart[i * 128 + mt];
 #pragma unroll
         for (int gg = 1; gg < 4; ++gg) {
           if (32 * gg < nc) {
 #pragma unroll
-            for (int i = 0; i < K; ++i) other[i] = part[gg * K + i];
+            for (int i = 0; i < K; ++i) other[i] = sPart[(gg * K + i) * 128 + mt];
             merge_top<K>(best, other);
           }
         }
-        uint32_t *const carry = sCarry + mt * K;
         if (sl > 0) {
 #pragma unroll
-          for (int i = 0; i < K; ++i) other[i] = carry[i];
+          for (int i = 0; i < K; ++i) other[i] = sCarry[i * 128 + mt];
           merge_top<K>(best, other);
         }
         if (!last) {
 #pragma unroll
-          for (int i = 0; i < K; ++i) carry[i] = best[i];
+          for (int i = 0; i < K; ++i) sCarry[i * 128 + mt] = best[i];
         } else {
           uint32_t o[kMaxK / 2];
 #pragma unroll
