@@ -57,6 +57,10 @@ struct mptc_ctx {
   unsigned long long *dict = nullptr;
   int dict_log2 = 0;
   uint32_t *dict_rows = nullptr, *dict_words = nullptr, *dict_slots = nullptr;
+  // side stream of the learned search: g (dictionary + embedding) runs there
+  // beside f, forked from and joined back to the search's stream by events
+  cudaStream_t side_s = nullptr;
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   uint16_t *topk = nullptr;
   CUtensorMap tm_f{};  // F rows in boxes of one block column, 16 rows
   // device scratch
@@ -468,16 +472,21 @@ struct LearnedJob {
 int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream_t s) {
   mptc_ctx *c0 = jobs[0].ctx;
   mptc_internal::EmbedJob ej[mptc::kMaxBatch];
+  // g (the previous frames' dictionaries and their embeddings, latency-bound)
+  // on the side stream while f runs on s; the scoring waits for both
+  cudaEventRecord(c0->side_fork, s);
+  cudaStreamWaitEvent(c0->side_s, c0->side_fork, 0);
   {
-    KernelTimer t(c0, K_EMBED_G, s);
+    KernelTimer t(c0, K_EMBED_G, c0->side_s);
     mptc_ctx *ctxs[mptc::kMaxBatch];
     const uint32_t *prev[mptc::kMaxBatch];
     for (int j = 0; j < n; ++j) {
       ctxs[j] = jobs[j].ctx;
       prev[j] = reinterpret_cast<const uint32_t *>(jobs[j].P.prev) + 1;
     }
-    launch_g(ctxs, prev, n, counters, s);
+    launch_g(ctxs, prev, n, counters, c0->side_s);
   }
+  cudaEventRecord(c0->side_join, c0->side_s);
   for (int j = 0; j < n; ++j) {
     mptc_ctx *c = jobs[j].ctx;
     ej[j] = mptc_internal::EmbedJob{};
@@ -492,6 +501,7 @@ int launch_learned(const LearnedJob *jobs, int n, uint32_t *counters, cudaStream
     KernelTimer t(c0, K_EMBED_F, s);
     mptc_internal::model_embed(c0->model, true, ej, n, counters + 1, s);
   }
+  cudaStreamWaitEvent(s, c0->side_join, 0);
   mptc::ScoreBatch sb{};
   sb.n = n;
   sb.next = counters + 2;
@@ -696,6 +706,9 @@ mptc_status mptc_ctx_destroy(mptc_ctx *ctx) {
   cudaFree(ctx->sweep_part);
   cudaFree(ctx->femb);
   cudaFree(ctx->gemb);
+  if (ctx->side_s) cudaStreamDestroy(ctx->side_s);
+  if (ctx->side_fork) cudaEventDestroy(ctx->side_fork);
+  if (ctx->side_join) cudaEventDestroy(ctx->side_join);
   cudaFree(ctx->dict);
   cudaFree(ctx->dict_rows);
   cudaFree(ctx->dict_words);
@@ -1140,6 +1153,10 @@ mptc_status mptc_ctx_set_model(mptc_ctx *ctx, const mptc_model *model, int32_t k
         dalloc(&ctx->dict_words, n) || dalloc(&ctx->dict_slots, n))
       return fail(ctx, MPTC_ENOMEM, "learned proposal buffers");
     ctx->dict_log2 = lg;
+    if (cudaStreamCreateWithFlags(&ctx->side_s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->side_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->side_join, cudaEventDisableTiming) != cudaSuccess)
+      return fail(ctx, MPTC_ECUDA, "learned proposal: side stream");
     if (!embedding_map(&ctx->tm_f, ctx->femb, ctx->bw, ctx->bh, 1, mptc::kScoreTileH))
       return fail(ctx, MPTC_ECUDA, "learned proposal: tensor map encoding failed");
     MPTC_CUDA((score_attr<8, 4>()));
@@ -1167,7 +1184,10 @@ mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const 
   MPTC_CUDA(cudaMemsetAsync(ctx->topk, 0xFF, (size_t)n * mptc::kMaxK * sizeof(uint16_t), s));
   // the learned search's embedding and scoring launches for this one frame
   const uint32_t *prev_words = reinterpret_cast<const uint32_t *>(prev_final_dev) + 1;
-  mptc_status st = launch_g(&ctx, &prev_words, 1, ctx->work + 12, s);
+  MPTC_CUDA(cudaEventRecord(ctx->side_fork, s));
+  MPTC_CUDA(cudaStreamWaitEvent(ctx->side_s, ctx->side_fork, 0));
+  mptc_status st = launch_g(&ctx, &prev_words, 1, ctx->work + 12, ctx->side_s);
+  MPTC_CUDA(cudaEventRecord(ctx->side_join, ctx->side_s));
   mptc_internal::EmbedJob ej;
   if (st == MPTC_OK) {
     ej = mptc_internal::EmbedJob{};
@@ -1179,6 +1199,7 @@ mptc_status mptc_learned_proposals(mptc_ctx *ctx, const uint8_t *rgb_dev, const 
     ej.status = ctx->work + 1;
     st = mptc_internal::model_embed(ctx->model, true, &ej, 1, ctx->work + 13, s);
   }
+  MPTC_CUDA(cudaStreamWaitEvent(s, ctx->side_join, 0));
   if (st != MPTC_OK) return fail(ctx, st, "mptc_learned_proposals: embedding launch failed");
   mptc::ScoreBatch sb{};
   sb.n = 1;
